@@ -1,0 +1,143 @@
+/*
+ * tt.h — C ABI of the GB300 path-tracing core (libtt.so).
+ *
+ * The reference (TrenchantTracer) has no plugin or FFI layer: its hot path sits behind C++
+ * classes and device functions. Every entry point below replaces one of those interfaces
+ * and names it (file:line in the reference project). Conventions:
+ *   - every call returns a tt_status; tt_last_error_string() describes the last failure
+ *     on the calling thread;
+ *   - device buffers are plain pointers into the current CUDA device's memory; host
+ *     buffers are plain host pointers; `stream` is a cudaStream_t (NULL = legacy stream);
+ *   - handles are not thread-safe; distinct handles may be used from distinct threads.
+ */
+#ifndef TT_H
+#define TT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum tt_status {
+    TT_OK = 0,
+    TT_ERR_INVALID = 1,  /* bad argument */
+    TT_ERR_IO = 2,       /* file missing, short read or write */
+    TT_ERR_CUDA = 3,     /* a CUDA runtime call failed */
+    TT_ERR_TIMEOUT = 4,  /* a device-side bounded wait ran out */
+    TT_ERR_BOUNDS = 5,   /* a device-side bounds check fired (stack / queue overflow) */
+    TT_ERR_OOM = 6,      /* host or device allocation failed */
+    TT_ERR_FORMAT = 7,   /* malformed JSON / OBJ / .hdr / bvh.cache */
+    TT_ERR_NO_DEVICE = 8 /* no CUDA device visible */
+} tt_status;
+
+/* A ray, byte-compatible with the reference's Ray (include/geometry/Ray.h:10-13): 32 B. */
+typedef struct tt_ray {
+    float ox, oy, oz;
+    float dx, dy, dz;
+    float tmin, tmax;
+} tt_ray;
+
+/* The closest/any hit: Hit::index (original triangle id, -1 = miss) and Hit::distance
+ * (include/geometry/Hit.h:7-15). On a miss t = ray.tmax, as in the reference. 8 B. */
+typedef struct tt_hit {
+    int32_t id;
+    float t;
+} tt_hit;
+
+/* The full hit record of intersect(): id, Hit::matIndex, t and the interpolated,
+ * unnormalised Hit::normal (IntersectKernel.cuh:264,288-289). 24 B. */
+typedef struct tt_hit_ext {
+    int32_t id;
+    int32_t mat;
+    float t;
+    float nx, ny, nz;
+} tt_hit_ext;
+
+/* The 7 x u32 header of bvh.cache, in file order (BVHCompact.cpp:319-338). */
+typedef struct tt_bvh_header {
+    uint32_t nodes;       /* float4 count of the node array (4 per inner node) */
+    uint32_t tri_count;   /* triangle references emitted into leaves */
+    uint32_t leaf_count;
+    uint32_t vertices;    /* float4 count: 3 per triangle + 1 terminator per leaf */
+    uint32_t normals;     /* same indexing as vertices */
+    uint32_t tri_indices; /* int32 count, same indexing as vertices */
+    uint32_t mat_indices; /* uint32 count, same indexing as vertices */
+} tt_bvh_header;
+
+typedef struct tt_scene tt_scene; /* host triangle soup + materials (core/Scene.h) */
+typedef struct tt_bvh tt_bvh;     /* host compact SBVH arrays (bvh/BVHCompact.h) */
+typedef struct tt_dbvh tt_dbvh;   /* device-resident compact SBVH */
+
+/* ---- errors ---------------------------------------------------------------------- */
+const char *tt_last_error_string(void);
+const char *tt_version(void);
+
+/* ---- scene ingest (host) ---------------------------------------------------------- */
+/* Config(path) + SceneLoader::load (src/util/Config.cpp:3-22, src/loader/SceneLoader.cpp:8-29):
+ * the same scene JSON, OBJ, material-JSON and RGBE .hdr formats. */
+tt_status tt_scene_load_json(const char *config_path, tt_scene **out);
+/* Scene::add(Object*) on arrays already in memory (src/core/Scene.cpp:7-23): vertices and
+ * normals are xyz float triples; vidx/nidx are 3 indices per triangle; mat is one material
+ * index per triangle (may be NULL = all 0). */
+tt_status tt_scene_create(const float *vertices, int32_t num_vertices, const float *normals,
+                          int32_t num_normals, const int32_t *vidx, const int32_t *nidx,
+                          const uint32_t *mat, int32_t num_triangles, tt_scene **out);
+/* counts: [triangles, vertices, normals, materials, analytic geometries] */
+tt_status tt_scene_counts(const tt_scene *scene, int32_t counts[5]);
+/* copies of the triangle soup: any pointer may be NULL */
+tt_status tt_scene_arrays(const tt_scene *scene, float *vertices, float *normals, int32_t *vidx,
+                          int32_t *nidx, uint32_t *mat);
+void tt_scene_free(tt_scene *scene);
+
+/* ---- SBVH build and the compact layout (host) ------------------------------------ */
+/* BVH::BVH(scene, SAHHelper, splitAlpha) + BVHCompact::createCompact
+ * (src/bvh/BVH.cpp:3-63, src/bvh/BVHCompact.cpp:88-250). SAHHelper::setLeafPreferences
+ * (src/bvh/SAHHelper.cpp:51-54) gives leaf_min/leaf_max; the reference defaults are
+ * split_alpha 1e-5, leaf_min 1, leaf_max 0x7FFFFFF. threads <= 0 uses all host cores; the
+ * output does not depend on the thread count. */
+tt_status tt_bvh_build(const tt_scene *scene, float split_alpha, int32_t leaf_min,
+                       int32_t leaf_max, int32_t threads, tt_bvh **out);
+/* BVHCompact::save / BVHCompact(FILE*) (src/bvh/BVHCompact.cpp:319-375, :23-79). */
+tt_status tt_bvh_save(const tt_bvh *bvh, const char *path);
+tt_status tt_bvh_load(const char *path, tt_bvh **out);
+tt_status tt_bvh_header_get(const tt_bvh *bvh, tt_bvh_header *out);
+/* borrowed pointers to the host arrays (valid until tt_bvh_free) */
+tt_status tt_bvh_arrays(const tt_bvh *bvh, const void **nodes, const void **vertices,
+                        const void **normals, const int32_t **tri_indices,
+                        const uint32_t **mat_indices);
+void tt_bvh_free(tt_bvh *bvh);
+
+/* ---- device BVH and traversal ----------------------------------------------------- */
+/* The device half of BVHCompact (cudaMalloc + cudaMemcpy + texture objects,
+ * src/bvh/BVHCompact.cpp:196-317): uploads the arrays to the current device. */
+tt_status tt_bvh_upload(const tt_bvh *bvh, tt_dbvh **out);
+void tt_dbvh_free(tt_dbvh *dbvh);
+
+/* intersect(ray, bvh, needClosestHit) (include/geometry/IntersectKernel.cuh:78-296) over n
+ * rays in device memory; hits are written to device memory. closest = 1 is the closest hit,
+ * 0 the any hit (first accepted triangle in traversal order). */
+tt_status tt_trace(const tt_dbvh *bvh, const tt_ray *d_rays, int64_t n, tt_hit *d_hits,
+                   int32_t closest, void *stream);
+/* as tt_trace, writing the full hit record (material index and interpolated normal). */
+tt_status tt_trace_ext(const tt_dbvh *bvh, const tt_ray *d_rays, int64_t n, tt_hit_ext *d_hits,
+                       int32_t closest, void *stream);
+/* as tt_trace with HOST buffers: copies rays in, traces and copies hits out on `stream`
+ * through a device staging area owned by `bvh`, and synchronises the stream before returning
+ * (page-locked host buffers get full copy bandwidth). Returns the device error word like
+ * tt_dbvh_check. */
+tt_status tt_trace_host(const tt_dbvh *bvh, const tt_ray *h_rays, int64_t n, tt_hit *h_hits,
+                        int32_t closest, void *stream);
+/* Synchronises `stream`, then reads and clears the device error word that tt_trace /
+ * tt_trace_ext calls on `bvh` set: TT_ERR_BOUNDS if a traversal stack would have overflowed
+ * (the reference's 64-entry stack has no check, IntersectKernel.cuh:8,164-165), TT_ERR_TIMEOUT
+ * if a traversal reached its iteration cap (a corrupt BVH), TT_OK otherwise. Rays that fail
+ * this way are reported as misses. */
+tt_status tt_dbvh_check(const tt_dbvh *bvh, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TT_H */

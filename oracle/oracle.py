@@ -1,0 +1,100 @@
+"""Build and ctypes access for the oracle's C restatement (oracle/tt_oracle.c).
+
+ORACLE — test infrastructure. Used only by tests/, __graft_entry__.smoke() and bench.py's CPU
+baseline leg, as the checker or the reported CPU baseline; the product never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+SRC = HERE / "tt_oracle.c"
+LIB = HERE / "_build" / "liboracle.so"
+
+SLAB_FMA, CROSS_A, CROSS_B, DOT_A, DOT_B, INTERP_A, INTERP_B = 1, 2, 4, 8, 16, 32, 64
+PLAIN = 0
+# The contraction nvcc applies to the reference's intersect() on sm_103a; pinned against the
+# reference kernel's own outputs in tests/golden (see tests/test_oracle_golden.py).
+DEVICE = SLAB_FMA | CROSS_A | DOT_A | INTERP_A
+
+_h = None
+
+
+def build(force: bool = False) -> Path:
+    if LIB.exists() and not force and LIB.stat().st_mtime >= SRC.stat().st_mtime:
+        return LIB
+    LIB.parent.mkdir(exist_ok=True)
+    tmp = LIB.with_suffix(".so.tmp")
+    cmd = ["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", str(SRC), "-o", str(tmp),
+           "-lm"]
+    proc = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if proc.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + proc.stdout)
+    tmp.replace(LIB)
+    return LIB
+
+
+def _load():
+    global _h
+    if _h is None:
+        build()
+        h = C.CDLL(str(LIB))
+        h.oracle_intersect.restype = C.c_int64
+        h.oracle_intersect.argtypes = [C.c_void_p] * 5 + [C.c_void_p, C.c_int64, C.c_int, C.c_int] + \
+            [C.c_void_p] * 5 + [C.c_int]
+        h.oracle_max_threads.restype = C.c_int
+        h.oracle_wang_hash.restype = C.c_uint32
+        h.oracle_wang_hash.argtypes = [C.c_uint32]
+        _h = h
+    return _h
+
+
+def intersect(bvh_arrays: dict, rays: np.ndarray, closest: bool, arith: int = DEVICE, counters: bool = False,
+              normals: bool = False, threads: int = 0) -> dict:
+    """bvh_arrays: the dict of BVHCompact.arrays() (or of a loaded bvh.cache)."""
+    rays = np.ascontiguousarray(rays, dtype=np.float32)
+    n = rays.shape[0]
+    out = {"id": np.empty(n, np.int32), "t": np.empty(n, np.float32), "mat": np.empty(n, np.int32)}
+    if normals:
+        out["normal"] = np.empty((n, 3), np.float32)
+    if counters:
+        out["counters"] = np.empty((n, 4), np.uint32)
+    a = [np.ascontiguousarray(bvh_arrays[k]) for k in ["nodes", "vertices", "normals", "tri_indices", "mat_indices"]]
+    ov = _load().oracle_intersect(*(x.ctypes.data for x in a), rays.ctypes.data, n, int(closest), arith,
+                                  out["id"].ctypes.data, out["t"].ctypes.data, out["mat"].ctypes.data,
+                                  out["normal"].ctypes.data if normals else None,
+                                  out["counters"].ctypes.data if counters else None, threads)
+    out["overflow"] = int(ov)
+    return out
+
+
+def max_threads() -> int:
+    return int(_load().oracle_max_threads())
+
+
+def wang_hash(a: int) -> int:
+    return int(_load().oracle_wang_hash(a))
+
+
+def read_cache(path: str | Path) -> dict:
+    """Reads a bvh.cache (7 x u32 header, then the five arrays) without libtt."""
+    raw = np.fromfile(path, dtype=np.uint8)
+    hdr = raw[:28].view(np.uint32)
+    nodes, tri_count, leaf_count, nv, nn, nt, nm = (int(x) for x in hdr)
+    off = 28
+
+    def take(count, dtype, cols=None):
+        nonlocal off
+        size = count * np.dtype(dtype).itemsize * (cols or 1)
+        a = raw[off:off + size].view(dtype)
+        off += size
+        return a.reshape(-1, cols) if cols else a
+
+    return {"header": {"nodes": nodes, "tri_count": tri_count, "leaf_count": leaf_count, "vertices": nv,
+                       "normals": nn, "tri_indices": nt, "mat_indices": nm},
+            "nodes": take(nodes, np.int32, 4), "vertices": take(nv, np.int32, 4), "normals": take(nn, np.int32, 4),
+            "tri_indices": take(nt, np.int32), "mat_indices": take(nm, np.uint32)}

@@ -1,0 +1,146 @@
+// Runs the reference's own intersect() kernel (oracle/_ref/ref_intersect.cubin, built by
+// oracle/build_ref.py) on the GPU: loads the cubin through the driver API into the primary
+// context, uploads the compact BVH, creates texture objects with the descriptors of
+// BVHCompact::createTexture (src/bvh/BVHCompact.cpp:276-317) and launches one ray per thread,
+// 256 threads per block. Also times the kernel with CUDA events (the GPU baseline).
+//
+// Test infrastructure only: compiled into oracle/_build/libref_gpu.so, never into libtt.so.
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+static std::string g_err;
+
+#define CK(x)                                                                 \
+    do {                                                                      \
+        cudaError_t e_ = (x);                                                 \
+        if (e_ != cudaSuccess) {                                              \
+            g_err = std::string(#x) + ": " + cudaGetErrorString(e_);          \
+            goto done;                                                        \
+        }                                                                     \
+    } while (0)
+#define CKD(x)                                                                \
+    do {                                                                      \
+        CUresult r_ = (x);                                                    \
+        if (r_ != CUDA_SUCCESS) {                                             \
+            const char *s_ = nullptr;                                         \
+            cuGetErrorString(r_, &s_);                                        \
+            g_err = std::string(#x) + ": " + (s_ ? s_ : "?");                 \
+            goto done;                                                        \
+        }                                                                     \
+    } while (0)
+
+static cudaError_t make_tex(cudaTextureObject_t *tex, void *ptr, size_t bytes, bool vec4) {
+    cudaResourceDesc res;
+    memset(&res, 0, sizeof(res));
+    res.resType = cudaResourceTypeLinear;
+    res.res.linear.devPtr = ptr;
+    res.res.linear.desc.f = cudaChannelFormatKindFloat;
+    res.res.linear.desc.x = 32;
+    res.res.linear.desc.y = vec4 ? 32 : 0;
+    res.res.linear.desc.z = vec4 ? 32 : 0;
+    res.res.linear.desc.w = vec4 ? 32 : 0;
+    res.res.linear.sizeInBytes = bytes;
+    cudaTextureDesc td;
+    memset(&td, 0, sizeof(td));
+    td.readMode = cudaReadModeElementType;
+    td.filterMode = cudaFilterModeLinear;
+    return cudaCreateTextureObject(tex, &res, &td, nullptr);
+}
+
+extern "C" {
+
+const char *ref_gpu_error(void) { return g_err.c_str(); }
+
+// Host arrays in, host results out. ms_out (may be NULL) receives the median kernel time over
+// `reps` launches (>= 1). Returns 0 on success.
+int ref_gpu_trace(const char *cubin_path, const void *nodes, uint32_t n_nodes, const void *verts, uint32_t n_verts,
+                  const void *norms, const int32_t *tri_idx, const uint32_t *mat_idx, const float *rays, int64_t n,
+                  int closest, int32_t *out_id, int32_t *out_mat, float *out_t, float *out_normal, int reps,
+                  float *ms_out) {
+    int rc = -1;
+    CUmodule mod = nullptr;
+    CUfunction fn = nullptr;
+    void *d_nodes = nullptr, *d_verts = nullptr, *d_norms = nullptr, *d_tri = nullptr, *d_mat = nullptr;
+    float *d_rays = nullptr, *d_t = nullptr, *d_normal = nullptr;
+    int *d_id = nullptr, *d_matout = nullptr;
+    cudaTextureObject_t tex[5] = {0, 0, 0, 0, 0};
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    float times[64];
+    int nrep = reps < 1 ? 1 : (reps > 64 ? 64 : reps);
+    int n32 = (int)n;
+    if (n <= 0 || n > 0x7fffffff) {
+        g_err = "ray count out of range";
+        return -1;
+    }
+    CK(cudaFree(0));  // create / bind the primary context
+    CKD(cuModuleLoad(&mod, cubin_path));
+    CKD(cuModuleGetFunction(&fn, mod, "ref_trace_kernel"));
+    CK(cudaMalloc(&d_nodes, 16ull * n_nodes));
+    CK(cudaMalloc(&d_verts, 16ull * n_verts));
+    CK(cudaMalloc(&d_norms, 16ull * n_verts));
+    CK(cudaMalloc(&d_tri, 4ull * n_verts));
+    CK(cudaMalloc(&d_mat, 4ull * n_verts));
+    CK(cudaMemcpy(d_nodes, nodes, 16ull * n_nodes, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(d_verts, verts, 16ull * n_verts, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(d_norms, norms, 16ull * n_verts, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(d_tri, tri_idx, 4ull * n_verts, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(d_mat, mat_idx, 4ull * n_verts, cudaMemcpyHostToDevice));
+    CK(make_tex(&tex[0], d_nodes, 16ull * n_nodes, true));
+    CK(make_tex(&tex[1], d_verts, 16ull * n_verts, true));
+    CK(make_tex(&tex[2], d_norms, 16ull * n_verts, true));
+    CK(make_tex(&tex[3], d_tri, 4ull * n_verts, false));
+    CK(make_tex(&tex[4], d_mat, 4ull * n_verts, false));
+    CK(cudaMalloc(&d_rays, 32ull * n));
+    CK(cudaMalloc(&d_id, 4ull * n));
+    CK(cudaMalloc(&d_matout, 4ull * n));
+    CK(cudaMalloc(&d_t, 4ull * n));
+    CK(cudaMalloc(&d_normal, 12ull * n));
+    CK(cudaMemcpy(d_rays, rays, 32ull * n, cudaMemcpyHostToDevice));
+    CK(cudaEventCreate(&ev[0]));
+    CK(cudaEventCreate(&ev[1]));
+    {
+        int cl = closest;
+        void *args[] = {&d_rays, &n32, &tex[0], &tex[1], &tex[2], &tex[3], &tex[4], &cl,
+                        &d_id, &d_matout, &d_t, &d_normal};
+        const unsigned grid = (unsigned)((n + 255) / 256);
+        for (int r = 0; r < nrep; r++) {
+            CK(cudaEventRecord(ev[0], 0));
+            CKD(cuLaunchKernel(fn, grid, 1, 1, 256, 1, 1, 0, nullptr, args, nullptr));
+            CK(cudaEventRecord(ev[1], 0));
+            CK(cudaEventSynchronize(ev[1]));
+            CK(cudaEventElapsedTime(&times[r], ev[0], ev[1]));
+        }
+    }
+    CK(cudaGetLastError());
+    CK(cudaMemcpy(out_id, d_id, 4ull * n, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(out_t, d_t, 4ull * n, cudaMemcpyDeviceToHost));
+    if (out_mat) CK(cudaMemcpy(out_mat, d_matout, 4ull * n, cudaMemcpyDeviceToHost));
+    if (out_normal) CK(cudaMemcpy(out_normal, d_normal, 12ull * n, cudaMemcpyDeviceToHost));
+    if (ms_out) {
+        for (int i = 1; i < nrep; i++)  // insertion sort for the median
+            for (int j = i; j > 0 && times[j] < times[j - 1]; j--) {
+                float s = times[j];
+                times[j] = times[j - 1];
+                times[j - 1] = s;
+            }
+        *ms_out = times[nrep / 2];
+    }
+    rc = 0;
+done:
+    for (auto &t : tex)
+        if (t) cudaDestroyTextureObject(t);
+    for (auto &e : ev)
+        if (e) cudaEventDestroy(e);
+    for (void *p : {d_nodes, d_verts, d_norms, d_tri, d_mat, (void *)d_rays, (void *)d_id, (void *)d_matout,
+                    (void *)d_t, (void *)d_normal})
+        if (p) cudaFree(p);
+    if (mod) cuModuleUnload(mod);
+    return rc;
+}
+
+}  // extern "C"

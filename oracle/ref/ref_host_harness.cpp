@@ -1,0 +1,125 @@
+// C entry points around the reference's OWN host code, compiled from the reference sources by
+// oracle/build_ref.py into oracle/_ref/libttref_host.so (never committed, never shipped in
+// libtt.so). They let the tests run the reference's scene loader, SBVH builder and a
+// host-compiled intersect() on the same inputs as this project's code.
+//
+// Test infrastructure only.
+#include <omp.h>
+
+#include <cstdio>
+#include <cstring>
+#include <exception>
+#include <string>
+
+#include <bvh/BVH.h>
+#include <bvh/BVHCompact.h>
+#include <bvh/SAHHelper.h>
+#include <core/Camera.h>
+#include <core/Scene.h>
+#include <loader/SceneLoader.h>
+#include <util/Config.h>
+#include <util/WangHash.h>
+
+#include "ref_host_compat.h"
+#include <geometry/IntersectKernel.cuh>
+
+extern "C" {
+
+// Config -> SceneLoader::load -> BVH(scene, SAHHelper{leaf prefs}, alpha) -> BVHCompact::save,
+// the sequence of src/main.cpp:34-75.
+int ref_build_json(const char *config_path, const char *cache_path, float split_alpha, int leaf_min,
+                   int leaf_max) {
+    try {
+        Config config(config_path);
+        SceneLoader loader(&config);
+        Scene *scene = loader.load();
+        SAHHelper sah;
+        sah.setLeafPreferences(leaf_min, leaf_max);
+        BVH bvh(scene, sah, split_alpha);
+        BVHCompact *compact = bvh.createHolder();
+        compact->save(cache_path);
+        delete compact;
+        delete scene;
+        return 0;
+    } catch (const std::exception &e) {
+        fprintf(stderr, "ref_build_json: %s\n", e.what());
+        return -1;
+    }
+}
+
+// Scene arrays as the reference's loader leaves them: counts[0..2] = triangles, vertices,
+// normals; then the caller passes buffers of those sizes (NULL to query counts only).
+int ref_scene_arrays(const char *config_path, int *counts, float *vertices, float *normals, int *vidx, int *nidx,
+                     unsigned *mat) {
+    try {
+        Config config(config_path);
+        SceneLoader loader(&config);
+        Scene *scene = loader.load();
+        counts[0] = scene->getTrianglesNum();
+        counts[1] = scene->getVerticesNum();
+        counts[2] = scene->getNormalNum();
+        if (vertices) memcpy(vertices, scene->getVertexPtr(), 12ull * counts[1]);
+        if (normals) memcpy(normals, scene->getNormalPtr(), 12ull * counts[2]);
+        if (vidx) memcpy(vidx, scene->getTrianglePtr(), 12ull * counts[0]);
+        if (nidx) memcpy(nidx, scene->getNormalIndexPtr(), 12ull * counts[0]);
+        if (mat) memcpy(mat, scene->getMatIndexPtr(), 4ull * counts[0]);
+        delete scene;
+        return 0;
+    } catch (const std::exception &e) {
+        fprintf(stderr, "ref_scene_arrays: %s\n", e.what());
+        return -1;
+    }
+}
+
+// Camera(config) + setFovx(45) + getCameraMeta(), as src/main.cpp:37-38 and Renderer::display
+// use them. out = position xyz, view xyz, up xyz, fov xy, aperture, focal (13 floats).
+int ref_camera_meta(const char *config_path, float fovx, float *out) {
+    try {
+        Config config(config_path);
+        Camera camera(&config);
+        camera.setFovx(fovx);
+        CameraMeta m = camera.getCameraMeta();
+        const float v[13] = {m.position.x, m.position.y, m.position.z, m.view.x, m.view.y, m.view.z,
+                             m.up.x, m.up.y, m.up.z, m.fov.x, m.fov.y, m.apertureRadius, m.focalDistance};
+        memcpy(out, v, sizeof(v));
+        return 0;
+    } catch (const std::exception &e) {
+        fprintf(stderr, "ref_camera_meta: %s\n", e.what());
+        return -1;
+    }
+}
+
+unsigned ref_wang_hash(unsigned a) { return WangHash::encode(a); }
+
+// The reference's intersect() compiled for the host (ballot -> this lane only; video min/max ->
+// integer min/max), over n rays of 8 floats under OpenMP. Loads the BVH from bvh.cache with
+// the reference's own reader (BVHCompact(FILE*)).
+int ref_intersect_host(const char *cache_path, const float *rays, long long n, int closest, int *idx, int *mat,
+                       float *t, float *normal, int threads) {
+    FILE *f = fopen(cache_path, "rb");
+    if (!f) return -1;
+    try {
+        BVHCompact bvh(f);
+        if (threads > 0) omp_set_num_threads(threads);
+#pragma omp parallel for schedule(dynamic, 4096)
+        for (long long i = 0; i < n; i++) {
+            const float *r = rays + 8 * i;
+            Ray ray(Vec3f(r[0], r[1], r[2]), Vec3f(r[3], r[4], r[5]), r[6], r[7]);
+            Hit h = intersect(ray, &bvh, closest != 0);
+            idx[i] = h.index;
+            t[i] = h.distance;
+            if (mat) mat[i] = h.index != -1 ? h.matIndex : -1;
+            if (normal) {
+                normal[3 * i + 0] = h.normal.x;
+                normal[3 * i + 1] = h.normal.y;
+                normal[3 * i + 2] = h.normal.z;
+            }
+        }
+        return 0;
+    } catch (const std::exception &e) {
+        fprintf(stderr, "ref_intersect_host: %s\n", e.what());
+        return -1;
+    }
+}
+
+}  // extern "C"

@@ -1,0 +1,72 @@
+"""The reference's own device intersect() on the GPU (oracle/_ref/ref_intersect.cubin through
+oracle/ref/ref_gpu_loader.cpp).
+
+Test infrastructure only: the device oracle that pins hit ids and distances bit for bit, and the
+reference GPU baseline. `available()` is False without a GPU or without the prebuilt cubin.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import shutil
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+SRC = HERE / "ref" / "ref_gpu_loader.cpp"
+LIB = HERE / "_build" / "libref_gpu.so"
+CUBIN = HERE / "_ref" / "ref_intersect.cubin"
+_h = None
+
+
+def build(force: bool = False) -> Path:
+    if LIB.exists() and not force and LIB.stat().st_mtime >= SRC.stat().st_mtime:
+        return LIB
+    cuda = Path(shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc").resolve().parent.parent
+    LIB.parent.mkdir(exist_ok=True)
+    tmp = LIB.with_suffix(".so.tmp")
+    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-I" + str(cuda / "include"), str(SRC), "-o", str(tmp),
+           "-L" + str(cuda / "lib64"), "-L" + str(cuda / "lib64" / "stubs"), "-lcudart_static", "-lcuda",
+           "-lpthread", "-ldl", "-lrt"]
+    proc = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if proc.returncode != 0:
+        raise RuntimeError("ref_gpu_loader build failed:\n" + proc.stdout)
+    tmp.replace(LIB)
+    return LIB
+
+
+def available() -> bool:
+    return CUBIN.exists() and LIB.exists()
+
+
+def _load():
+    global _h
+    if _h is None:
+        h = C.CDLL(str(LIB))
+        h.ref_gpu_error.restype = C.c_char_p
+        h.ref_gpu_trace.restype = C.c_int
+        h.ref_gpu_trace.argtypes = [C.c_char_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p,
+                                    C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_void_p, C.c_void_p,
+                                    C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
+        _h = h
+    return _h
+
+
+def intersect(bvh_arrays: dict, rays: np.ndarray, closest: bool, reps: int = 1) -> dict:
+    rays = np.ascontiguousarray(rays, dtype=np.float32)
+    n = rays.shape[0]
+    a = {k: np.ascontiguousarray(bvh_arrays[k]) for k in ["nodes", "vertices", "normals", "tri_indices",
+                                                         "mat_indices"]}
+    out = {"id": np.empty(n, np.int32), "mat": np.empty(n, np.int32), "t": np.empty(n, np.float32),
+           "normal": np.empty((n, 3), np.float32)}
+    ms = C.c_float(0.0)
+    rc = _load().ref_gpu_trace(str(CUBIN).encode(), a["nodes"].ctypes.data, a["nodes"].shape[0],
+                               a["vertices"].ctypes.data, a["vertices"].shape[0], a["normals"].ctypes.data,
+                               a["tri_indices"].ctypes.data, a["mat_indices"].ctypes.data, rays.ctypes.data, n,
+                               int(closest), out["id"].ctypes.data, out["mat"].ctypes.data, out["t"].ctypes.data,
+                               out["normal"].ctypes.data, reps, C.byref(ms))
+    if rc != 0:
+        raise RuntimeError("reference GPU intersect failed: " + _load().ref_gpu_error().decode())
+    out["ms"] = float(ms.value)
+    return out

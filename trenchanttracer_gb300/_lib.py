@@ -1,0 +1,79 @@
+"""ctypes binding of libtt.so (the C ABI declared in include/tt.h).
+
+The library is built in-tree by trenchanttracer_gb300.build; importing this module never
+falls back to anything else: if libtt.so is missing the import fails loudly.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "libtt.so"
+
+TT_OK = 0
+STATUS_NAMES = {0: "TT_OK", 1: "TT_ERR_INVALID", 2: "TT_ERR_IO", 3: "TT_ERR_CUDA", 4: "TT_ERR_TIMEOUT",
+                5: "TT_ERR_BOUNDS", 6: "TT_ERR_OOM", 7: "TT_ERR_FORMAT", 8: "TT_ERR_NO_DEVICE"}
+
+
+class TTError(RuntimeError):
+    """A libtt call returned a non-zero tt_status."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+class BvhHeader(C.Structure):
+    _fields_ = [("nodes", C.c_uint32), ("tri_count", C.c_uint32), ("leaf_count", C.c_uint32),
+                ("vertices", C.c_uint32), ("normals", C.c_uint32), ("tri_indices", C.c_uint32),
+                ("mat_indices", C.c_uint32)]
+
+
+P = C.c_void_p
+I32 = C.c_int32
+I64 = C.c_int64
+F32 = C.c_float
+SIGNATURES = {
+    "tt_last_error_string": (C.c_char_p, []),
+    "tt_version": (C.c_char_p, []),
+    "tt_scene_load_json": (I32, [C.c_char_p, C.POINTER(P)]),
+    "tt_scene_create": (I32, [P, I32, P, I32, P, P, P, I32, C.POINTER(P)]),
+    "tt_scene_counts": (I32, [P, C.POINTER(I32)]),
+    "tt_scene_arrays": (I32, [P, P, P, P, P, P]),
+    "tt_scene_free": (None, [P]),
+    "tt_bvh_build": (I32, [P, F32, I32, I32, I32, C.POINTER(P)]),
+    "tt_bvh_save": (I32, [P, C.c_char_p]),
+    "tt_bvh_load": (I32, [C.c_char_p, C.POINTER(P)]),
+    "tt_bvh_header_get": (I32, [P, C.POINTER(BvhHeader)]),
+    "tt_bvh_arrays": (I32, [P, C.POINTER(P), C.POINTER(P), C.POINTER(P), C.POINTER(P), C.POINTER(P)]),
+    "tt_bvh_free": (None, [P]),
+    "tt_bvh_upload": (I32, [P, C.POINTER(P)]),
+    "tt_dbvh_free": (None, [P]),
+    "tt_trace": (I32, [P, P, I64, P, I32, P]),
+    "tt_trace_ext": (I32, [P, P, I64, P, I32, P]),
+    "tt_trace_host": (I32, [P, P, I64, P, I32, P]),
+    "tt_dbvh_check": (I32, [P, P]),
+}
+
+_lib: C.CDLL | None = None
+
+
+def lib() -> C.CDLL:
+    """Loads libtt.so once and declares every exported signature."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise ImportError(f"{LIB_PATH} is missing: run `python -c 'import __graft_entry__ as g; g.build()'`")
+        h = C.CDLL(str(LIB_PATH))
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(h, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = h
+    return _lib
+
+
+def check(status: int) -> None:
+    if status != TT_OK:
+        msg = lib().tt_last_error_string()
+        raise TTError(status, msg.decode() if msg else "")

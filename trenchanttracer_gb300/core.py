@@ -1,0 +1,165 @@
+"""Python mirror of the reference's scene / BVH / traversal interfaces over libtt.so.
+
+Names follow the reference's classes: ``Scene`` (core/Scene.h), ``BVHCompact``
+(bvh/BVHCompact.h: build, ``save``, load from ``bvh.cache``) and ``DeviceBVH`` holding the
+device arrays that intersect() reads. ``DeviceBVH.intersect`` is intersect(ray, bvh,
+needClosestHit) (include/geometry/IntersectKernel.cuh:78) over a whole batch of rays.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _lib
+from ._lib import check, lib
+
+RAY_DTYPE = np.float32  # a ray is 8 float32: origin xyz, direction xyz, tmin, tmax
+
+
+def _ptr(a: np.ndarray | None) -> C.c_void_p:
+    return C.c_void_p(0 if a is None else a.ctypes.data)
+
+
+class Scene:
+    """Triangle soup + materials (reference core/Scene.h)."""
+
+    def __init__(self, handle: C.c_void_p, materials: list | None = None):
+        self._h = handle
+        self.materials = materials or []
+
+    @classmethod
+    def load_json(cls, path: str | os.PathLike) -> "Scene":
+        """Config + SceneLoader::load: the reference's scene JSON / OBJ / material / .hdr."""
+        h = C.c_void_p()
+        check(lib().tt_scene_load_json(os.fsencode(path), C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def from_arrays(cls, vertices, normals, vidx, nidx=None, mat=None, materials=None) -> "Scene":
+        v = np.ascontiguousarray(vertices, dtype=np.float32).reshape(-1, 3)
+        n = np.ascontiguousarray(normals, dtype=np.float32).reshape(-1, 3)
+        vi = np.ascontiguousarray(vidx, dtype=np.int32).reshape(-1, 3)
+        ni = vi if nidx is None else np.ascontiguousarray(nidx, dtype=np.int32).reshape(-1, 3)
+        m = None if mat is None else np.ascontiguousarray(mat, dtype=np.uint32).reshape(-1)
+        h = C.c_void_p()
+        check(lib().tt_scene_create(_ptr(v), v.shape[0], _ptr(n), n.shape[0], _ptr(vi), _ptr(ni), _ptr(m),
+                                    vi.shape[0], C.byref(h)))
+        return cls(h, materials)
+
+    @classmethod
+    def from_mesh(cls, mesh) -> "Scene":
+        return cls.from_arrays(mesh.vertices, mesh.normals, mesh.vidx, mesh.nidx, mesh.mat, mesh.materials)
+
+    def counts(self) -> dict:
+        c = (C.c_int32 * 5)()
+        check(lib().tt_scene_counts(self._h, c))
+        return dict(zip(["triangles", "vertices", "normals", "materials", "geometries"], list(c)))
+
+    def arrays(self) -> dict:
+        c = self.counts()
+        out = {"vertices": np.empty((c["vertices"], 3), np.float32),
+               "normals": np.empty((c["normals"], 3), np.float32),
+               "vidx": np.empty((c["triangles"], 3), np.int32),
+               "nidx": np.empty((c["triangles"], 3), np.int32),
+               "mat": np.empty(c["triangles"], np.uint32)}
+        check(lib().tt_scene_arrays(self._h, *(_ptr(out[k]) for k in ["vertices", "normals", "vidx", "nidx", "mat"])))
+        return out
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().tt_scene_free(self._h)
+            self._h = None
+
+
+class BVHCompact:
+    """Host-side compact SBVH arrays (reference bvh/BVHCompact.h), built or read from bvh.cache."""
+
+    def __init__(self, handle: C.c_void_p):
+        self._h = handle
+
+    @classmethod
+    def build(cls, scene: Scene, split_alpha: float = 1e-5, leaf_min: int = 1, leaf_max: int = 0x7FFFFFF,
+              threads: int = 0) -> "BVHCompact":
+        h = C.c_void_p()
+        check(lib().tt_bvh_build(scene._h, split_alpha, leaf_min, leaf_max, threads, C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def load(cls, path: str | os.PathLike) -> "BVHCompact":
+        h = C.c_void_p()
+        check(lib().tt_bvh_load(os.fsencode(path), C.byref(h)))
+        return cls(h)
+
+    def save(self, path: str | os.PathLike) -> None:
+        check(lib().tt_bvh_save(self._h, os.fsencode(path)))
+
+    @property
+    def header(self) -> dict:
+        hd = _lib.BvhHeader()
+        check(lib().tt_bvh_header_get(self._h, C.byref(hd)))
+        return {f: getattr(hd, f) for f, _ in hd._fields_}
+
+    def arrays(self) -> dict:
+        """Copies of the five arrays: nodes/vertices/normals as (n, 4) int32 bit patterns."""
+        hd = self.header
+        p = [C.c_void_p() for _ in range(5)]
+        check(lib().tt_bvh_arrays(self._h, *(C.byref(x) for x in p)))
+
+        def grab(ptr, count, dtype, cols=None):
+            n = count * (cols or 1)
+            if n == 0:
+                return np.zeros((0, cols) if cols else 0, dtype)
+            buf = (C.c_char * (n * np.dtype(dtype).itemsize)).from_address(ptr.value)
+            a = np.frombuffer(buf, dtype=dtype).copy()
+            return a.reshape(-1, cols) if cols else a
+
+        return {"nodes": grab(p[0], hd["nodes"], np.int32, 4),
+                "vertices": grab(p[1], hd["vertices"], np.int32, 4),
+                "normals": grab(p[2], hd["normals"], np.int32, 4),
+                "tri_indices": grab(p[3], hd["tri_indices"], np.int32),
+                "mat_indices": grab(p[4], hd["mat_indices"], np.uint32)}
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().tt_bvh_free(self._h)
+            self._h = None
+
+
+class DeviceBVH:
+    """The compact BVH resident on the current CUDA device."""
+
+    def __init__(self, bvh: BVHCompact):
+        h = C.c_void_p()
+        check(lib().tt_bvh_upload(bvh._h, C.byref(h)))
+        self._h = h
+        self.header = bvh.header
+
+    def intersect(self, rays, hits, closest: bool = True, stream: int = 0, ext: bool = False) -> None:
+        """rays: CUDA tensor (n, 8) float32; hits: CUDA tensor (n, 2) int32 [id, t bits]
+        (or (n, 6) for ext = id, mat, t, normal xyz). Launch only; no synchronisation."""
+        n = rays.shape[0]
+        fn = lib().tt_trace_ext if ext else lib().tt_trace
+        check(fn(self._h, C.c_void_p(rays.data_ptr()), n, C.c_void_p(hits.data_ptr()), int(bool(closest)),
+                 C.c_void_p(stream)))
+
+    def intersect_host(self, rays: np.ndarray, hits: np.ndarray, closest: bool = True, stream: int = 0) -> None:
+        """Host buffers: rays (n, 8) float32, hits (n, 2) int32; synchronous."""
+        assert rays.dtype == np.float32 and rays.flags.c_contiguous and hits.flags.c_contiguous
+        check(lib().tt_trace_host(self._h, _ptr(rays), rays.shape[0], _ptr(hits), int(bool(closest)),
+                                  C.c_void_p(stream)))
+
+    def check(self, stream: int = 0) -> None:
+        check(lib().tt_dbvh_check(self._h, C.c_void_p(stream)))
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().tt_dbvh_free(self._h)
+            self._h = None
+
+
+def hits_to_numpy(hits: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    """(n, 2) int32 [id, t bits] -> (ids int32, t float32)."""
+    h = np.ascontiguousarray(hits).view(np.int32).reshape(-1, 2)
+    return h[:, 0].copy(), h[:, 1].copy().view(np.float32)

@@ -1,0 +1,552 @@
+// Host SBVH builder (Stich et al. 2009 spatial-split BVH) emitting the reference's compact
+// two-wide layout and its bvh.cache file.
+//
+// The build reproduces every decision of the reference builder (src/bvh/BVH.cpp) so that the
+// emitted arrays are byte-identical to what BVHCompact::createCompact writes
+// (src/bvh/BVHCompact.cpp:88-250):
+//   - SAH costs of SAHHelper's defaults: triangle cost n * 1, node cost 2 * 1
+//     (src/bvh/SAHHelper.cpp:19-25, include/bvh/SAHHelper.h:73-81);
+//   - leaf if numRef <= leaf_min or depth >= 64; spatial splits only above depth 48 and when
+//     the object-split children overlap by >= alpha * rootArea (BVH.cpp:70-111, BVH.h:96-100);
+//   - object splits: full sweep of the references sorted on (min+max) along each axis, ties
+//     broken by triangle index (BVH.cpp:122-154, :343-351);
+//   - spatial splits: 32 bins per axis, reference clipping against the split plane, and the
+//     unsplit-left / unsplit-right / duplicate choice (BVH.cpp:166-341);
+//   - AABB growth semantics, including that growing a box by an EMPTY box makes it unbounded
+//     (src/bvh/AABB.cpp:35-39; an empty bin therefore disqualifies a spatial split);
+//   - leaf triangle order: the reference pops its reference stack, so a leaf lists its
+//     references in reverse partition order (BVH.cpp:113-120);
+//   - compact emission: DFS from an explicit stack, inner children addressed by float4 index,
+//     leaves by ~vertexIndex, -0.0 in vertex0.x rewritten to +0.0, a (0x80000000,0,0,0)
+//     terminator after each leaf (BVHCompact.cpp:88-192).
+// Sorting uses std::sort: within one node every triangle index appears at most once, so the
+// comparator is a strict total order and any correct sort yields the same permutation.
+// Subtrees are built as OpenMP tasks; each task owns the reference list of its node, in the
+// order the reference's shared stack would hold it, so the output does not depend on threads.
+#include <algorithm>
+#include <cfloat>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <omp.h>
+
+#include "tt_internal.h"
+
+namespace tt {
+namespace {
+
+constexpr int kMaxDepth = 64;
+constexpr int kMaxSpatialDepth = 48;
+constexpr int kBins = 32;
+constexpr int kTaskThreshold = 2048;
+
+struct AABB {
+    V3 lo{FLT_MAX, FLT_MAX, FLT_MAX};
+    V3 hi{-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    void grow(const V3 &p) {
+        lo = vmin3(lo, p);
+        hi = vmax3(hi, p);
+    }
+    // Grows by the two corner points, as the reference does: an empty box (lo = +MAX,
+    // hi = -MAX) turns this box into [-MAX, +MAX].
+    void grow(const AABB &b) {
+        grow(b.lo);
+        grow(b.hi);
+    }
+    void intersect(const AABB &b) {
+        lo = vmax3(lo, b.lo);
+        hi = vmin3(hi, b.hi);
+    }
+    bool valid() const { return lo.x <= hi.x && lo.y <= hi.y && lo.z <= hi.z; }
+    float area() const {
+        if (!valid()) return 0.0f;
+        V3 d = hi - lo;
+        return (d.x * d.y + d.y * d.z + d.z * d.x) * 2.0f;
+    }
+};
+
+struct Ref {
+    int32_t tri;
+    AABB b;
+};
+
+struct Node {
+    AABB b;
+    std::unique_ptr<Node> child[2];  // [0] = left, [1] = right
+    std::vector<int32_t> tris;       // leaf triangles, in emission order
+    bool leaf = false;
+};
+
+struct ObjectSplit {
+    float sah = FLT_MAX;
+    int dim = 0;
+    int num_left = 0;
+    AABB left, right;
+};
+
+struct SpatialSplit {
+    float sah = FLT_MAX;
+    int dim = 0;
+    float pos = 0.0f;
+};
+
+struct Bin {
+    AABB b;
+    int enter = 0, exit = 0;
+};
+
+inline float min1f(float a, float b) { return (a > b) ? b : a; }
+inline int clamp1i(int v, int lo, int hi) { return v < lo ? lo : v > hi ? hi : v; }
+
+// float -> int32 with the x86 cvttss2si result for NaN and out-of-range values (0x80000000),
+// so that flat nodes (0 * inf bin coordinates) bin the same way on every host.
+inline int f2i_trunc(float f) {
+    if (!(f > -2147483648.0f && f < 2147483648.0f)) return INT32_MIN;
+    return (int)f;
+}
+
+class Builder {
+public:
+    Builder(const Scene &s, const BuildParams &p) : sc_(s), p_(p) {}
+
+    std::unique_ptr<Node> run(int64_t &duplicates) {
+        const int n = sc_.num_tris();
+        std::vector<Ref> refs(n);
+        AABB root;
+        for (int i = 0; i < n; i++) {
+            refs[i].tri = i;
+            for (int k = 0; k < 3; k++) refs[i].b.grow(sc_.vertices[sc_.vidx[3 * i + k]]);
+            root.grow(refs[i].b);
+        }
+        min_overlap_ = root.area() * p_.split_alpha;
+        std::unique_ptr<Node> out;
+        dup_ = 0;
+        int threads = p_.threads > 0 ? p_.threads : omp_get_max_threads();
+#pragma omp parallel num_threads(threads)
+#pragma omp single
+        out = build(std::move(refs), root, 0);
+        duplicates = dup_;
+        return out;
+    }
+
+private:
+    const Scene &sc_;
+    BuildParams p_;
+    float min_overlap_ = 0.0f;
+    int64_t dup_ = 0;
+
+    const V3 &vert(int tri, int k) const { return sc_.vertices[sc_.vidx[3 * tri + k]]; }
+
+    std::unique_ptr<Node> leaf(const std::vector<Ref> &refs, const AABB &b) {
+        auto nd = std::make_unique<Node>();
+        nd->leaf = true;
+        nd->b = b;
+        nd->tris.resize(refs.size());
+        for (size_t i = 0; i < refs.size(); i++) nd->tris[i] = refs[refs.size() - 1 - i].tri;
+        return nd;
+    }
+
+    static void sort_dim(std::vector<Ref> &refs, int dim) {
+        std::sort(refs.begin(), refs.end(), [dim](const Ref &a, const Ref &b) {
+            float ca = a.b.lo[dim] + a.b.hi[dim];
+            float cb = b.b.lo[dim] + b.b.hi[dim];
+            if (ca < cb) return true;
+            if (ca > cb) return false;
+            return a.tri < b.tri;
+        });
+    }
+
+    ObjectSplit find_object_split(std::vector<Ref> &refs, float node_sah) {
+        ObjectSplit split;
+        const int n = (int)refs.size();
+        std::vector<AABB> right_bounds(n > 1 ? n - 1 : 1);
+        for (int dim = 0; dim < 3; dim++) {
+            sort_dim(refs, dim);
+            AABB rb;
+            for (int i = n - 1; i > 0; i--) {
+                rb.grow(refs[i].b);
+                right_bounds[i - 1] = rb;
+            }
+            AABB lb;
+            for (int i = 1; i < n; i++) {
+                lb.grow(refs[i - 1].b);
+                float sah = node_sah + lb.area() * (float)i + right_bounds[i - 1].area() * (float)(n - i);
+                if (sah < split.sah) {
+                    split.sah = sah;
+                    split.dim = dim;
+                    split.num_left = i;
+                    split.left = lb;
+                    split.right = right_bounds[i - 1];
+                }
+            }
+        }
+        return split;
+    }
+
+    void split_reference(Ref &left, Ref &right, const Ref &ref, int dim, float pos) const {
+        left.tri = right.tri = ref.tri;
+        left.b = right.b = AABB();
+        const V3 *v1 = &vert(ref.tri, 2);
+        for (int k = 0; k < 3; k++) {
+            const V3 *v0 = v1;
+            v1 = &vert(ref.tri, k);
+            float v0p = (*v0)[dim];
+            float v1p = (*v1)[dim];
+            if (v0p <= pos) left.b.grow(*v0);
+            if (v0p >= pos) right.b.grow(*v0);
+            if ((v0p < pos && v1p > pos) || (v0p > pos && v1p < pos)) {
+                float t = (pos - v0p) / (v1p - v0p);
+                t = t < 0.0f ? 0.0f : (t > 1.0f ? 1.0f : t);
+                V3 a = (*v0) * (1.0f - t);
+                V3 b = (*v1) * t;
+                V3 q = a + b;
+                left.b.grow(q);
+                right.b.grow(q);
+            }
+        }
+        left.b.hi[dim] = pos;
+        right.b.lo[dim] = pos;
+        left.b.intersect(ref.b);
+        right.b.intersect(ref.b);
+    }
+
+    SpatialSplit find_spatial_split(const std::vector<Ref> &refs, const AABB &bounds, float node_sah) {
+        const V3 origin = bounds.lo;
+        const V3 bin_size = (bounds.hi - origin) * (1.0f / (float)kBins);
+        const V3 inv_bin(1.0f / bin_size.x, 1.0f / bin_size.y, 1.0f / bin_size.z);
+        Bin bins[3][kBins];
+        for (const Ref &ref : refs) {
+            V3 f = (ref.b.lo - origin) * inv_bin;
+            V3 l = (ref.b.hi - origin) * inv_bin;
+            int first[3], last[3];
+            for (int d = 0; d < 3; d++) first[d] = clamp1i(f2i_trunc(f[d]), 0, kBins - 1);
+            for (int d = 0; d < 3; d++) last[d] = clamp1i(f2i_trunc(l[d]), first[d], kBins - 1);
+            for (int dim = 0; dim < 3; dim++) {
+                Ref curr = ref;
+                for (int i = first[dim]; i < last[dim]; i++) {
+                    Ref lr, rr;
+                    split_reference(lr, rr, curr, dim, origin[dim] + bin_size[dim] * (float)(i + 1));
+                    bins[dim][i].b.grow(lr.b);
+                    curr = rr;
+                }
+                bins[dim][last[dim]].b.grow(curr.b);
+                bins[dim][first[dim]].enter++;
+                bins[dim][last[dim]].exit++;
+            }
+        }
+        SpatialSplit split;
+        const int n = (int)refs.size();
+        AABB right_bounds[kBins - 1];
+        for (int dim = 0; dim < 3; dim++) {
+            AABB rb;
+            for (int i = kBins - 1; i > 0; i--) {
+                rb.grow(bins[dim][i].b);
+                right_bounds[i - 1] = rb;
+            }
+            AABB lb;
+            int left_num = 0, right_num = n;
+            for (int i = 1; i < kBins; i++) {
+                lb.grow(bins[dim][i - 1].b);
+                left_num += bins[dim][i - 1].enter;
+                right_num -= bins[dim][i - 1].exit;
+                float sah = node_sah + lb.area() * (float)left_num + right_bounds[i - 1].area() * (float)right_num;
+                if (sah < split.sah) {
+                    split.sah = sah;
+                    split.dim = dim;
+                    split.pos = origin[dim] + bin_size[dim] * (float)i;
+                }
+            }
+        }
+        return split;
+    }
+
+    // Partitions `refs` in place (plus appended duplicates): left = [0, left_end),
+    // right = [left_end, size).
+    void perform_spatial_split(std::vector<Ref> &refs, const SpatialSplit &split, int &left_n, AABB &left_b,
+                               int &right_n, AABB &right_b) {
+        const int dim = split.dim;
+        const float pos = split.pos;
+        int left_start = 0, left_end = 0, right_start = (int)refs.size();
+        left_b = right_b = AABB();
+        for (int i = left_end; i < right_start; i++) {
+            if (refs[i].b.hi[dim] <= pos) {
+                left_b.grow(refs[i].b);
+                std::swap(refs[i], refs[left_end++]);
+            } else if (refs[i].b.lo[dim] >= pos) {
+                right_b.grow(refs[i].b);
+                std::swap(refs[i], refs[--right_start]);
+                i--;
+            }
+        }
+        while (left_end < right_start) {
+            Ref lr, rr;
+            split_reference(lr, rr, refs[left_end], dim, pos);
+            AABB lub = left_b, rub = right_b, ldb = left_b, rdb = right_b;
+            lub.grow(refs[left_end].b);
+            rub.grow(refs[left_end].b);
+            ldb.grow(lr.b);
+            rdb.grow(rr.b);
+            float lac = (float)(left_end - left_start);
+            float rac = (float)((int)refs.size() - right_start);
+            float lbc = (float)(left_end - left_start + 1);
+            float rbc = (float)((int)refs.size() - right_start + 1);
+            float unsplit_left = lub.area() * lbc + right_b.area() * rac;
+            float unsplit_right = left_b.area() * lac + rub.area() * rbc;
+            float duplicate = ldb.area() * lbc + rdb.area() * rbc;
+            float m = min1f(min1f(unsplit_left, unsplit_right), duplicate);
+            if (m == unsplit_left) {
+                left_b = lub;
+                left_end++;
+            } else if (m == unsplit_right) {
+                right_b = rub;
+                std::swap(refs[left_end], refs[--right_start]);
+            } else {
+                left_b = ldb;
+                right_b = rdb;
+                refs[left_end++] = lr;
+                refs.push_back(rr);
+            }
+        }
+        left_n = left_end - left_start;
+        right_n = (int)refs.size() - right_start;
+    }
+
+    std::unique_ptr<Node> build(std::vector<Ref> refs, AABB bounds, int level) {
+        const int n = (int)refs.size();
+        if (n <= p_.leaf_min || level >= kMaxDepth) return leaf(refs, bounds);
+
+        const float area = bounds.area();
+        const float leaf_sah = area * (float)n;
+        const float node_sah = area * 2.0f;
+        ObjectSplit object = find_object_split(refs, node_sah);
+
+        SpatialSplit spatial;
+        if (level < kMaxSpatialDepth) {
+            AABB overlap = object.left;
+            overlap.intersect(object.right);
+            if (overlap.area() >= min_overlap_) spatial = find_spatial_split(refs, bounds, node_sah);
+        }
+
+        const float min_sah = min1f(min1f(leaf_sah, object.sah), spatial.sah);
+        if (min_sah == leaf_sah && n <= p_.leaf_max) return leaf(refs, bounds);
+
+        int left_n = 0, right_n = 0;
+        AABB left_b, right_b;
+        if (min_sah == spatial.sah) perform_spatial_split(refs, spatial, left_n, left_b, right_n, right_b);
+        if (!left_n || !right_n) {
+            // The references are sorted along axis 2 by find_object_split; sort along the
+            // chosen axis again exactly as the reference does (BVH.cpp:156-164).
+            if (refs.size() != (size_t)n) refs.resize(n);  // (never: no duplicates were appended)
+            sort_dim(refs, object.dim);
+            left_n = object.num_left;
+            left_b = object.left;
+            right_n = n - object.num_left;
+            right_b = object.right;
+        }
+
+        const int total = left_n + right_n;
+        if (total > n) {
+#pragma omp atomic
+            dup_ += total - n;
+        }
+        std::vector<Ref> right_refs(refs.begin() + left_n, refs.begin() + total);
+        refs.resize(left_n);
+        std::vector<Ref> left_refs = std::move(refs);
+
+        auto nd = std::make_unique<Node>();
+        nd->b = bounds;
+        if (total >= kTaskThreshold) {
+            std::unique_ptr<Node> r;
+#pragma omp task shared(r) firstprivate(right_b, level)
+            r = build(std::move(right_refs), right_b, level + 1);
+            nd->child[0] = build(std::move(left_refs), left_b, level + 1);
+#pragma omp taskwait
+            nd->child[1] = std::move(r);
+        } else {
+            nd->child[1] = build(std::move(right_refs), right_b, level + 1);
+            nd->child[0] = build(std::move(left_refs), left_b, level + 1);
+        }
+        return nd;
+    }
+};
+
+inline int32_t fbits(float f) { return (int32_t)f2u(f); }
+
+void emit_leaf(const Scene &sc, const Node &leaf, CompactBVH &out) {
+    for (int32_t id : leaf.tris) {
+        V3 v[3], nrm[3];
+        for (int k = 0; k < 3; k++) {
+            v[k] = sc.vertices[sc.vidx[3 * id + k]];
+            nrm[k] = sc.normals[sc.nidx[3 * id + k]];
+        }
+        out.hdr.tri_count++;
+        if (v[0].x == 0.0f) v[0].x = 0.0f;  // -0.0 would read as the leaf terminator
+        for (int k = 0; k < 3; k++) {
+            out.vertices.push_back(I4{fbits(v[k].x), fbits(v[k].y), fbits(v[k].z), 0});
+            out.normals.push_back(I4{fbits(nrm[k].x), fbits(nrm[k].y), fbits(nrm[k].z), 0});
+        }
+        out.tri_idx.push_back(id);
+        out.tri_idx.push_back(0);
+        out.tri_idx.push_back(0);
+        out.mat_idx.push_back(sc.mat[id]);
+        out.mat_idx.push_back(0);
+        out.mat_idx.push_back(0);
+    }
+    out.vertices.push_back(I4{(int32_t)0x80000000, 0, 0, 0});
+    out.normals.push_back(I4{(int32_t)0x80000000, 0, 0, 0});
+    out.tri_idx.push_back(0);
+    out.mat_idx.push_back(0);
+    out.hdr.leaf_count++;
+}
+
+void emit_compact(const Scene &sc, const Node &root, CompactBVH &out) {
+    out.nodes.assign(4, I4{0, 0, 0, 0});
+    struct Entry {
+        const Node *node;
+        int32_t idx;
+    };
+    std::vector<Entry> stack{{&root, 0}};
+    while (!stack.empty()) {
+        Entry e = stack.back();
+        stack.pop_back();
+        const AABB *box[2];
+        int32_t cidx[2];
+        for (int i = 0; i < 2; i++) {
+            const Node *c = e.node->child[i].get();
+            box[i] = &c->b;
+            if (!c->leaf) {
+                cidx[i] = (int32_t)out.nodes.size();  // float4 index = bytes / 16
+                stack.push_back({c, (int32_t)out.nodes.size()});
+                out.nodes.resize(out.nodes.size() + 4, I4{0, 0, 0, 0});
+                continue;
+            }
+            cidx[i] = ~(int32_t)out.vertices.size();
+            emit_leaf(sc, *c, out);
+        }
+        I4 *dst = &out.nodes[e.idx];
+        dst[0] = I4{fbits(box[0]->lo.x), fbits(box[0]->hi.x), fbits(box[0]->lo.y), fbits(box[0]->hi.y)};
+        dst[1] = I4{fbits(box[1]->lo.x), fbits(box[1]->hi.x), fbits(box[1]->lo.y), fbits(box[1]->hi.y)};
+        dst[2] = I4{fbits(box[0]->lo.z), fbits(box[0]->hi.z), fbits(box[1]->lo.z), fbits(box[1]->hi.z)};
+        dst[3] = I4{cidx[0], cidx[1], 0, 0};
+    }
+}
+
+}  // namespace
+
+tt_status build_compact(const Scene &sc, const BuildParams &p, CompactBVH &out) {
+    const int n = sc.num_tris();
+    if (sc.vidx.size() != (size_t)3 * n || sc.nidx.size() != (size_t)3 * n)
+        return fail(TT_ERR_INVALID, "scene index arrays do not match the triangle count");
+    for (int i = 0; i < 3 * n; i++) {
+        if (sc.vidx[i] < 0 || (size_t)sc.vidx[i] >= sc.vertices.size())
+            return fail(TT_ERR_INVALID, "vertex index out of range");
+        if (sc.nidx[i] < 0 || (size_t)sc.nidx[i] >= sc.normals.size())
+            return fail(TT_ERR_INVALID, "normal index out of range");
+    }
+    if (p.leaf_min < 0 || p.leaf_max < 1) return fail(TT_ERR_INVALID, "bad leaf size preferences");
+    out = CompactBVH();
+    std::unique_ptr<Node> root;
+    if (n > 0) {
+        Builder b(sc, p);
+        int64_t dups = 0;
+        root = b.run(dups);
+    }
+    // The reference requires an inner root (BVHCompact.cpp:104 asserts two children and
+    // dereferences them). A scene that ends in a single leaf -- or has no triangles -- gets an
+    // inner root whose missing child is an empty leaf with an empty box, which no ray enters.
+    if (!root || root->leaf) {
+        auto top = std::make_unique<Node>();
+        auto empty = std::make_unique<Node>();
+        empty->leaf = true;
+        if (root) {
+            top->b = root->b;
+            top->child[0] = std::move(root);
+        } else {
+            auto empty0 = std::make_unique<Node>();
+            empty0->leaf = true;
+            top->child[0] = std::move(empty0);
+        }
+        top->child[1] = std::move(empty);
+        root = std::move(top);
+    }
+    emit_compact(sc, *root, out);
+    out.hdr.nodes = (uint32_t)out.nodes.size();
+    out.hdr.vertices = (uint32_t)out.vertices.size();
+    out.hdr.normals = (uint32_t)out.normals.size();
+    out.hdr.tri_indices = (uint32_t)out.tri_idx.size();
+    out.hdr.mat_indices = (uint32_t)out.mat_idx.size();
+    return TT_OK;
+}
+
+// ---- bvh.cache ------------------------------------------------------------------------
+tt_status save_compact(const CompactBVH &b, const std::string &path) {
+    FILE *f = fopen(path.c_str(), "wb");
+    if (!f) return fail(TT_ERR_IO, "cannot open " + path + " for writing");
+    const tt_bvh_header &h = b.hdr;
+    const uint32_t words[7] = {h.nodes, h.tri_count, h.leaf_count, h.vertices, h.normals, h.tri_indices,
+                               h.mat_indices};
+    bool ok = fwrite(words, 4, 7, f) == 7;
+    ok = ok && fwrite(b.nodes.data(), 16, b.nodes.size(), f) == b.nodes.size();
+    ok = ok && fwrite(b.vertices.data(), 16, b.vertices.size(), f) == b.vertices.size();
+    ok = ok && fwrite(b.normals.data(), 16, b.normals.size(), f) == b.normals.size();
+    ok = ok && fwrite(b.tri_idx.data(), 4, b.tri_idx.size(), f) == b.tri_idx.size();
+    ok = ok && fwrite(b.mat_idx.data(), 4, b.mat_idx.size(), f) == b.mat_idx.size();
+    ok = (fclose(f) == 0) && ok;
+    if (!ok) return fail(TT_ERR_IO, "short write to " + path);
+    return TT_OK;
+}
+
+tt_status load_compact(const std::string &path, CompactBVH &out) {
+    FILE *f = fopen(path.c_str(), "rb");
+    if (!f) return fail(TT_ERR_IO, "cannot open " + path);
+    uint32_t w[7];
+    if (fread(w, 4, 7, f) != 7) {
+        fclose(f);
+        return fail(TT_ERR_FORMAT, "bvh.cache header truncated: " + path);
+    }
+    fseek(f, 0, SEEK_END);
+    long long size = ftell(f);
+    fseek(f, 28, SEEK_SET);
+    const long long need = 28 + 16LL * w[0] + 16LL * w[3] + 16LL * w[4] + 4LL * w[5] + 4LL * w[6];
+    if (size != need) {
+        fclose(f);
+        return fail(TT_ERR_FORMAT, "bvh.cache size " + std::to_string(size) + " does not match its header (" +
+                                       std::to_string(need) + "): " + path);
+    }
+    if (w[3] != w[4] || w[3] != w[5] || w[3] != w[6] || (w[0] % 4) != 0 || w[0] == 0) {
+        fclose(f);
+        return fail(TT_ERR_FORMAT, "bvh.cache header is inconsistent: " + path);
+    }
+    out = CompactBVH();
+    out.hdr = tt_bvh_header{w[0], w[1], w[2], w[3], w[4], w[5], w[6]};
+    out.nodes.resize(w[0]);
+    out.vertices.resize(w[3]);
+    out.normals.resize(w[4]);
+    out.tri_idx.resize(w[5]);
+    out.mat_idx.resize(w[6]);
+    bool ok = fread(out.nodes.data(), 16, w[0], f) == w[0];
+    ok = ok && fread(out.vertices.data(), 16, w[3], f) == w[3];
+    ok = ok && fread(out.normals.data(), 16, w[4], f) == w[4];
+    ok = ok && fread(out.tri_idx.data(), 4, w[5], f) == w[5];
+    ok = ok && fread(out.mat_idx.data(), 4, w[6], f) == w[6];
+    fclose(f);
+    if (!ok) return fail(TT_ERR_FORMAT, "bvh.cache truncated: " + path);
+    // Structural validation: every child address must land inside its array, so that a
+    // corrupt file is rejected here instead of steering a traversal out of bounds.
+    for (uint32_t i = 0; i < w[0]; i += 4) {
+        const I4 &c = out.nodes[i + 3];
+        for (int32_t a : {c.x, c.y}) {
+            if (a >= 0) {
+                if ((a % 4) != 0 || (uint32_t)a + 3 >= w[0])
+                    return fail(TT_ERR_FORMAT, "bvh.cache inner child address out of range");
+            } else if ((uint32_t)(~a) >= w[3]) {
+                return fail(TT_ERR_FORMAT, "bvh.cache leaf address out of range");
+            }
+        }
+    }
+    if (w[3] > 0 && (uint32_t)out.vertices[w[3] - 1].x != 0x80000000u)
+        return fail(TT_ERR_FORMAT, "bvh.cache vertex array does not end with a leaf terminator");
+    return TT_OK;
+}
+
+}  // namespace tt

@@ -1,0 +1,677 @@
+// Scene ingest: the reference's scene JSON (src/util/Config.cpp:3-22), OBJ meshes
+// (src/loader/OBJLoader.cpp:3-105), material JSON files (src/loader/MaterialLoader.cpp:9-36)
+// and RGBE .hdr maps (src/loader/HDRLoader.cpp:5-152), assembled as Scene::add does
+// (src/core/Scene.cpp:7-36).
+//
+// Arithmetic that decides vertex bits follows the reference step by step so that a scene
+// loaded here equals the reference's: OBJ numbers are parsed straight to float (strtof, as
+// libstdc++'s operator>> does), JSON numbers through double then cast to float (as the
+// vendored JSON library stores them), per-object normalisation into [-1,1]
+// (src/core/Object.cpp:40-83) and the S*T*R transform as 4x4 float matrices multiplied in
+// the reference's loop order (include/math/LinearMath.h Mat4f::operator*, Transform.cpp:13-33).
+#include <cerrno>
+#include <cfloat>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <sstream>
+
+#include "tt_internal.h"
+
+namespace tt {
+
+// ---- minimal JSON --------------------------------------------------------------------------
+struct Json {
+    enum Kind { NUL, BOOL, NUM, STR, ARR, OBJ } kind = NUL;
+    bool b = false;
+    double num = 0.0;
+    bool is_int = false;
+    long long inum = 0;
+    std::string str;
+    std::vector<Json> arr;
+    std::map<std::string, Json> obj;  // sorted by key, like the reference's JSON objects
+
+    const Json *find(const std::string &k) const {
+        if (kind != OBJ) return nullptr;
+        auto it = obj.find(k);
+        return it == obj.end() ? nullptr : &it->second;
+    }
+    float as_float() const { return is_int ? (float)inum : (float)num; }
+};
+
+class JsonParser {
+public:
+    explicit JsonParser(const std::string &s) : s_(s) {}
+    bool parse(Json &out, std::string &err) {
+        pos_ = 0;
+        if (!value(out)) {
+            err = "JSON syntax error at byte " + std::to_string(pos_);
+            return false;
+        }
+        ws();
+        if (pos_ != s_.size()) {
+            err = "trailing characters after JSON value at byte " + std::to_string(pos_);
+            return false;
+        }
+        return true;
+    }
+
+private:
+    const std::string &s_;
+    size_t pos_ = 0;
+    int depth_ = 0;
+
+    void ws() {
+        while (pos_ < s_.size() && (s_[pos_] == ' ' || s_[pos_] == '\t' || s_[pos_] == '\n' || s_[pos_] == '\r'))
+            pos_++;
+    }
+    bool lit(const char *w) {
+        size_t n = strlen(w);
+        if (s_.compare(pos_, n, w) != 0) return false;
+        pos_ += n;
+        return true;
+    }
+    bool string(std::string &out) {
+        if (pos_ >= s_.size() || s_[pos_] != '"') return false;
+        pos_++;
+        while (pos_ < s_.size() && s_[pos_] != '"') {
+            char c = s_[pos_++];
+            if (c == '\\') {
+                if (pos_ >= s_.size()) return false;
+                char e = s_[pos_++];
+                switch (e) {
+                    case 'n': out += '\n'; break;
+                    case 't': out += '\t'; break;
+                    case 'r': out += '\r'; break;
+                    case 'b': out += '\b'; break;
+                    case 'f': out += '\f'; break;
+                    case 'u': {
+                        if (pos_ + 4 > s_.size()) return false;
+                        unsigned cp = (unsigned)strtoul(s_.substr(pos_, 4).c_str(), nullptr, 16);
+                        pos_ += 4;
+                        if (cp < 0x80) out += (char)cp;
+                        else if (cp < 0x800) { out += (char)(0xC0 | (cp >> 6)); out += (char)(0x80 | (cp & 63)); }
+                        else { out += (char)(0xE0 | (cp >> 12)); out += (char)(0x80 | ((cp >> 6) & 63));
+                               out += (char)(0x80 | (cp & 63)); }
+                        break;
+                    }
+                    default: out += e;
+                }
+            } else {
+                out += c;
+            }
+        }
+        if (pos_ >= s_.size()) return false;
+        pos_++;
+        return true;
+    }
+    bool value(Json &v) {
+        if (++depth_ > 256) return false;
+        ws();
+        bool ok = false;
+        if (pos_ >= s_.size()) ok = false;
+        else if (s_[pos_] == '{') {
+            v.kind = Json::OBJ;
+            pos_++;
+            ws();
+            if (pos_ < s_.size() && s_[pos_] == '}') { pos_++; ok = true; }
+            else {
+                while (true) {
+                    ws();
+                    std::string k;
+                    if (!string(k)) break;
+                    ws();
+                    if (pos_ >= s_.size() || s_[pos_] != ':') break;
+                    pos_++;
+                    Json item;
+                    if (!value(item)) break;
+                    v.obj[k] = std::move(item);
+                    ws();
+                    if (pos_ < s_.size() && s_[pos_] == ',') { pos_++; continue; }
+                    if (pos_ < s_.size() && s_[pos_] == '}') { pos_++; ok = true; }
+                    break;
+                }
+            }
+        } else if (s_[pos_] == '[') {
+            v.kind = Json::ARR;
+            pos_++;
+            ws();
+            if (pos_ < s_.size() && s_[pos_] == ']') { pos_++; ok = true; }
+            else {
+                while (true) {
+                    Json item;
+                    if (!value(item)) break;
+                    v.arr.push_back(std::move(item));
+                    ws();
+                    if (pos_ < s_.size() && s_[pos_] == ',') { pos_++; continue; }
+                    if (pos_ < s_.size() && s_[pos_] == ']') { pos_++; ok = true; }
+                    break;
+                }
+            }
+        } else if (s_[pos_] == '"') {
+            v.kind = Json::STR;
+            ok = string(v.str);
+        } else if (lit("true")) { v.kind = Json::BOOL; v.b = true; ok = true; }
+        else if (lit("false")) { v.kind = Json::BOOL; v.b = false; ok = true; }
+        else if (lit("null")) { v.kind = Json::NUL; ok = true; }
+        else {
+            const char *start = s_.c_str() + pos_;
+            char *end = nullptr;
+            size_t n = 0;
+            while (pos_ + n < s_.size() && strchr("+-0123456789.eE", s_[pos_ + n])) n++;
+            std::string tok = s_.substr(pos_, n);
+            if (n > 0) {
+                bool integral = tok.find_first_of(".eE") == std::string::npos;
+                v.kind = Json::NUM;
+                if (integral) {
+                    errno = 0;
+                    v.inum = strtoll(tok.c_str(), &end, 10);
+                    v.is_int = errno == 0 && end && *end == 0;
+                    v.num = (double)v.inum;
+                }
+                if (!v.is_int) {
+                    v.num = strtod(tok.c_str(), &end);
+                    if (!end || *end != 0) n = 0;
+                }
+            }
+            (void)start;
+            ok = n > 0;
+            pos_ += n;
+        }
+        depth_--;
+        return ok;
+    }
+};
+
+static bool read_file(const std::string &path, std::string &out) {
+    std::ifstream f(path, std::ios::binary);
+    if (!f.good()) return false;
+    std::stringstream ss;
+    ss << f.rdbuf();
+    out = ss.str();
+    return true;
+}
+
+static tt_status parse_json_file(const std::string &path, Json &out) {
+    std::string text;
+    if (!read_file(path, text)) return fail(TT_ERR_IO, "cannot read " + path);
+    std::string err;
+    if (!JsonParser(text).parse(out, err)) return fail(TT_ERR_FORMAT, path + ": " + err);
+    return TT_OK;
+}
+
+static bool json_vec3(const Json *j, V3 &out) {
+    if (!j || j->kind != Json::ARR || j->arr.size() < 3) return false;
+    for (int i = 0; i < 3; i++)
+        if (j->arr[i].kind != Json::NUM) return false;
+    out = V3(j->arr[0].as_float(), j->arr[1].as_float(), j->arr[2].as_float());
+    return true;
+}
+
+// ---- 4x4 float matrices, in the reference's arithmetic order --------------------------------
+struct M4 {
+    float m[4][4];
+    static M4 identity() {
+        M4 r;
+        for (int i = 0; i < 4; i++)
+            for (int j = 0; j < 4; j++) r.m[i][j] = i == j ? 1.0f : 0.0f;
+        return r;
+    }
+    M4 operator*(const M4 &b) const {
+        M4 r;
+        for (int i = 0; i < 4; i++)
+            for (int j = 0; j < 4; j++) {
+                r.m[i][j] = 0;
+                for (int k = 0; k < 4; k++) r.m[i][j] += m[i][k] * b.m[k][j];
+            }
+        return r;
+    }
+    // Mat4f * Vec4f: each row dotted with v, accumulated from 0 in index order.
+    void apply(const float v[4], float out[4]) const {
+        for (int i = 0; i < 4; i++) {
+            float s = 0;
+            for (int k = 0; k < 4; k++) s += m[i][k] * v[k];
+            out[i] = s;
+        }
+    }
+};
+
+static M4 row_matrix(const float rows[4][4]) {
+    M4 r;
+    memcpy(r.m, rows, sizeof(r.m));
+    return r;
+}
+
+// Transform(geometryJson) (src/geometry/Transform.cpp:13-33): I * S * T * R, with
+// R = rotY(y) * rotX(x) * rotZ(z) from degrees (include/math/PoseMath.h:24-57).
+static M4 transform_matrix(const Json &geom) {
+    M4 m = M4::identity();
+    const Json *t = geom.find("transform");
+    if (!t || t->kind != Json::OBJ) return m;
+    V3 v;
+    if (json_vec3(t->find("scale"), v)) {
+        const float r[4][4] = {{v.x, 0, 0, 0}, {0, v.y, 0, 0}, {0, 0, v.z, 0}, {0, 0, 0, 1}};
+        m = m * row_matrix(r);
+    }
+    if (json_vec3(t->find("translate"), v)) {
+        const float r[4][4] = {{1, 0, 0, v.x}, {0, 1, 0, v.y}, {0, 0, 1, v.z}, {0, 0, 0, 1}};
+        m = m * row_matrix(r);
+    }
+    if (json_vec3(t->find("orientation"), v)) {
+        V3 a = (v / 180.0f) * (float)M_PI;
+        const float ry[4][4] = {{cosf(a.y), 0, sinf(a.y), 0}, {0, 1, 0, 0}, {-sinf(a.y), 0, cosf(a.y), 0}, {0, 0, 0, 1}};
+        const float rx[4][4] = {{1, 0, 0, 0}, {0, cosf(a.x), -sinf(a.x), 0}, {0, sinf(a.x), cosf(a.x), 0}, {0, 0, 0, 1}};
+        const float rz[4][4] = {{cosf(a.z), -sinf(a.z), 0, 0}, {sinf(a.z), cosf(a.z), 0, 0}, {0, 0, 1, 0}, {0, 0, 0, 1}};
+        m = m * (row_matrix(ry) * row_matrix(rx) * row_matrix(rz));
+    }
+    return m;
+}
+
+// ---- materials -------------------------------------------------------------------------
+static tt_status parse_material(const std::string &name, const Json &j, MaterialRec &out) {
+    memset(&out, 0, sizeof(out));
+    out.ior = 1.5f;
+    const Json *type = j.find("type");
+    if (!type || type->kind != Json::STR) return fail(TT_ERR_FORMAT, "material " + name + " has no type");
+    V3 v;
+    if (json_vec3(j.find("emission"), v)) { out.emission[0] = v.x; out.emission[1] = v.y; out.emission[2] = v.z; }
+    auto color = [&](const char *key, float *dst) -> bool {
+        V3 c;
+        if (!json_vec3(j.find(key), c)) return false;
+        dst[0] = c.x; dst[1] = c.y; dst[2] = c.z;
+        return true;
+    };
+    const std::string &t = type->str;
+    if (t == "Diff") { out.kind = MAT_DIFF; if (!color("diffuseColor", out.color)) goto missing; }
+    else if (t == "Metal") { out.kind = MAT_METAL; if (!color("color", out.color)) goto missing; }
+    else if (t == "Spec") { out.kind = MAT_SPEC; if (!color("color", out.color)) goto missing; }
+    else if (t == "Refr") { out.kind = MAT_REFR; out.ior = 1.4f; }
+    else if (t == "Coat") {
+        out.kind = MAT_COAT;
+        if (!color("diffuseColor", out.color) || !color("specularColor", out.color2)) goto missing;
+    } else if (t == "GGX") {
+        out.kind = MAT_GGX;
+        if (!color("F0", out.color) && !color("color", out.color)) goto missing;
+        const Json *r = j.find("roughness");
+        out.roughness = (r && r->kind == Json::NUM) ? r->as_float() : 0.5f;
+    } else if (t == "Dielectric") {
+        out.kind = MAT_DIELECTRIC;
+        const Json *r = j.find("ior");
+        out.ior = (r && r->kind == Json::NUM) ? r->as_float() : 1.5f;
+    } else {
+        return fail(TT_ERR_FORMAT, "material " + name + " has unknown type " + t);
+    }
+    return TT_OK;
+missing:
+    return fail(TT_ERR_FORMAT, "material " + name + " misses its colour");
+}
+
+// MaterialLoader::load + Scene::add(MaterialPool*): materials take consecutive scene indices
+// in key order (the pool is a std::map, src/material/MaterialPool.cpp:12-24).
+static tt_status load_material_pool(const std::string &path, Scene &sc, std::map<std::string, int32_t> &pool) {
+    Json j;
+    tt_status st = parse_json_file(path, j);
+    if (st != TT_OK) return st;
+    if (j.kind != Json::OBJ) return fail(TT_ERR_FORMAT, path + ": material file is not a JSON object");
+    for (auto &kv : j.obj) {
+        MaterialRec m;
+        if ((st = parse_material(kv.first, kv.second, m)) != TT_OK) return st;
+        pool[kv.first] = (int32_t)sc.materials.size();
+        sc.materials.push_back(m);
+        sc.material_names.push_back(kv.first);
+    }
+    return TT_OK;
+}
+
+// ---- OBJ ---------------------------------------------------------------------------------
+struct ObjGroup {
+    std::vector<int32_t> v, n;  // 3 per triangle
+    int32_t mat = -1;
+};
+
+static bool next_float(const char *&p, float &out) {
+    while (*p == ' ' || *p == '\t' || *p == '\r') p++;
+    if (!*p) return false;
+    char *end = nullptr;
+    out = strtof(p, &end);
+    if (end == p) return false;
+    p = end;
+    return true;
+}
+
+// OBJLoader::load + Object::postProcess + Object::apply + Scene::add(Object*).
+static tt_status load_obj(const std::string &file, const M4 &xf, Scene &sc) {
+    std::ifstream ifs(file);
+    if (!ifs.good()) return fail(TT_ERR_IO, "cannot read OBJ " + file);
+    std::vector<V3> verts, norms;
+    std::vector<ObjGroup> groups;
+    std::map<std::string, int32_t> pool;
+    bool have_pool = false;
+    std::string line;
+    while (std::getline(ifs, line)) {
+        const char *p = line.c_str();
+        while (*p == ' ' || *p == '\t') p++;
+        const char *k = p;
+        while (*p && *p != ' ' && *p != '\t' && *p != '\r') p++;
+        std::string key(k, p);
+        while (*p == ' ' || *p == '\t') p++;
+        std::string rest(p);
+        while (!rest.empty() && (rest.back() == '\r' || rest.back() == ' ')) rest.pop_back();
+        if (key == "g") {
+            groups.emplace_back();
+        } else if (key == "mtllib") {
+            std::string prefix;
+            size_t slash = file.find_last_of('/');
+            if (slash != std::string::npos) prefix = file.substr(0, slash + 1);
+            std::string name = rest.substr(0, rest.find_first_of(" \t"));
+            tt_status st = load_material_pool(prefix + name, sc, pool);
+            if (st != TT_OK) return st;
+            have_pool = true;
+        } else if (key == "usemtl") {
+            std::string name = rest.substr(0, rest.find_first_of(" \t"));
+            if (!have_pool) return fail(TT_ERR_FORMAT, file + ": usemtl before mtllib");
+            auto it = pool.find(name);
+            if (it == pool.end()) return fail(TT_ERR_FORMAT, "Material " + name + " not found");
+            if (groups.empty()) groups.emplace_back();
+            groups.back().mat = it->second;
+        } else if (key == "v" || key == "vn") {
+            const char *q = rest.c_str();
+            float x, y, z;
+            while (next_float(q, x)) {
+                if (!next_float(q, y) || !next_float(q, z)) return fail(TT_ERR_FORMAT, file + ": short " + key + " line");
+                (key == "v" ? verts : norms).push_back(V3(x, y, z));
+            }
+        } else if (key == "f") {
+            if (groups.empty()) groups.emplace_back();
+            std::vector<int> fv, fn;
+            int v = 1, n = 1;
+            const char *q = rest.c_str();
+            while (*q) {
+                char *end = nullptr;
+                long a = strtol(q, &end, 10);
+                if (end == q) break;
+                v = (int)a;
+                q = end;
+                if (*q == '/') {
+                    q++;
+                    if (*q == '/') {
+                        q++;
+                        n = (int)strtol(q, &end, 10);
+                        q = end;
+                    } else {
+                        strtol(q, &end, 10);  // texture index: unused
+                        q = end;
+                        if (*q == '/') {
+                            q++;
+                            n = (int)strtol(q, &end, 10);
+                            q = end;
+                        }
+                    }
+                }
+                fv.push_back(v - 1);
+                fn.push_back(n - 1);
+                while (*q == ' ' || *q == '\t' || *q == '\r') q++;
+            }
+            for (int i = 0; i + 2 < (int)fv.size(); i++) {
+                ObjGroup &g = groups.back();
+                g.v.insert(g.v.end(), {fv[0], fv[i + 1], fv[i + 2]});
+                g.n.insert(g.n.end(), {fn[0], fn[i + 1], fn[i + 2]});
+            }
+        }
+    }
+    if (!have_pool) return fail(TT_ERR_FORMAT, file + ": OBJ has no mtllib (the scene needs its material pool)");
+    for (const ObjGroup &g : groups) {
+        if (!g.v.empty() && g.mat < 0) return fail(TT_ERR_FORMAT, file + ": group without usemtl");
+        for (int32_t i : g.v)
+            if (i < 0 || (size_t)i >= verts.size()) return fail(TT_ERR_FORMAT, file + ": face vertex out of range");
+        for (int32_t i : g.n)
+            if (i < 0 || (size_t)i >= norms.size()) return fail(TT_ERR_FORMAT, file + ": face normal out of range");
+    }
+    if (norms.size() < verts.size())
+        return fail(TT_ERR_FORMAT, file + ": fewer vn than v lines (the transform needs one normal per vertex)");
+
+    // Object::postProcess: centre the face-referenced bounds at the origin, scale into [-1,1].
+    V3 minp(FLT_MAX, FLT_MAX, FLT_MAX), maxp(-FLT_MAX, -FLT_MAX, -FLT_MAX);
+    for (const ObjGroup &g : groups)
+        for (int32_t i : g.v) {
+            minp = vmin3(minp, verts[i]);
+            maxp = vmax3(maxp, verts[i]);
+        }
+    V3 c((maxp.x + minp.x) * 0.5f, (maxp.y + minp.y) * 0.5f, (maxp.z + minp.z) * 0.5f);
+    minp = minp - c;
+    maxp = maxp - c;
+    float maxi = 0;
+    for (float a : {minp.x, minp.y, minp.z, maxp.x, maxp.y, maxp.z}) maxi = std::max(maxi, std::fabs(a));
+    float scale = 1.0f / maxi;
+    for (V3 &v : verts) {
+        v = v - c;
+        v = v * scale;
+    }
+    // Object::apply(Transform): vertices with w = 1, normals with w = 0 then normalised.
+    for (size_t i = 0; i < verts.size(); i++) {
+        float in[4] = {verts[i].x, verts[i].y, verts[i].z, 1.0f}, out[4];
+        xf.apply(in, out);
+        verts[i] = V3(out[0], out[1], out[2]);
+        float nin[4] = {norms[i].x, norms[i].y, norms[i].z, 0.0f};
+        xf.apply(nin, out);
+        norms[i] = normalized(V3(out[0], out[1], out[2]));
+    }
+    // Scene::add(Object*)
+    const int32_t vbase = (int32_t)sc.vertices.size(), nbase = (int32_t)sc.normals.size();
+    sc.vertices.insert(sc.vertices.end(), verts.begin(), verts.end());
+    sc.normals.insert(sc.normals.end(), norms.begin(), norms.end());
+    for (const ObjGroup &g : groups) {
+        for (size_t t = 0; t < g.v.size() / 3; t++) {
+            for (int k = 0; k < 3; k++) {
+                sc.vidx.push_back(g.v[3 * t + k] + vbase);
+                sc.nidx.push_back(g.n[3 * t + k] + nbase);
+            }
+            sc.mat.push_back((uint32_t)g.mat);
+        }
+    }
+    return TT_OK;
+}
+
+// ---- RGBE .hdr ------------------------------------------------------------------------------
+static bool old_decrunch(unsigned char (*scan)[4], int len, FILE *f) {
+    int rshift = 0;
+    while (len > 0) {
+        for (int c = 0; c < 4; c++) scan[0][c] = (unsigned char)fgetc(f);
+        if (feof(f)) return false;
+        if (scan[0][0] == 1 && scan[0][1] == 1 && scan[0][2] == 1) {
+            for (int i = scan[0][3] << rshift; i > 0 && len > 0; i--) {
+                memcpy(scan[0], scan[-1], 4);
+                scan++;
+                len--;
+            }
+            rshift += 8;
+        } else {
+            scan++;
+            len--;
+            rshift = 0;
+        }
+    }
+    return true;
+}
+
+static bool decrunch(unsigned char (*scan)[4], int len, FILE *f) {
+    if (len < 8 || len > 0x7fff) return old_decrunch(scan, len, f);
+    int i = fgetc(f);
+    if (i != 2) {
+        fseek(f, -1, SEEK_CUR);
+        return old_decrunch(scan, len, f);
+    }
+    scan[0][1] = (unsigned char)fgetc(f);
+    scan[0][2] = (unsigned char)fgetc(f);
+    i = fgetc(f);
+    if (scan[0][1] != 2 || (scan[0][2] & 128)) {
+        scan[0][0] = 2;
+        scan[0][3] = (unsigned char)i;
+        return old_decrunch(scan + 1, len - 1, f);
+    }
+    for (int c = 0; c < 4; c++) {
+        for (int j = 0; j < len;) {
+            int code = fgetc(f);
+            if (code == EOF) return false;
+            if (code > 128) {
+                code &= 127;
+                int val = fgetc(f);
+                while (code-- && j < len) scan[j++][c] = (unsigned char)val;
+            } else {
+                while (code-- && j < len) scan[j++][c] = (unsigned char)fgetc(f);
+            }
+        }
+    }
+    return feof(f) == 0;
+}
+
+tt_status load_hdr(const std::string &path, int32_t &w_out, int32_t &h_out, std::vector<float> &rgb) {
+    FILE *f = fopen(path.c_str(), "rb");
+    if (!f) return fail(TT_ERR_IO, "HDR environment map not found: " + path);
+    char magic[10];
+    if (fread(magic, 10, 1, f) != 1 || memcmp(magic, "#?RADIANCE", 10) != 0) {
+        fclose(f);
+        return fail(TT_ERR_FORMAT, path + ": not a RADIANCE file");
+    }
+    fseek(f, 1, SEEK_CUR);
+    // header lines end at an empty line
+    int c = 0, oldc = 0, guard = 0;
+    while (true) {
+        oldc = c;
+        c = fgetc(f);
+        if (c == EOF || ++guard > 65536) {
+            fclose(f);
+            return fail(TT_ERR_FORMAT, path + ": header not terminated");
+        }
+        if (c == '\n' && oldc == '\n') break;
+    }
+    char reso[256];
+    int n = 0;
+    while (n < 255) {
+        c = fgetc(f);
+        if (c == EOF) break;
+        reso[n++] = (char)c;
+        if (c == '\n') break;
+    }
+    reso[n] = 0;
+    long w = 0, h = 0;
+    if (sscanf(reso, "-Y %ld +X %ld", &h, &w) != 2 || w <= 0 || h <= 0 || w * h > (1L << 28)) {
+        fclose(f);
+        return fail(TT_ERR_FORMAT, path + ": bad resolution line");
+    }
+    rgb.assign((size_t)w * h * 3, 0.0f);
+    std::vector<unsigned char> line((size_t)(w + 1) * 4, 0);
+    unsigned char (*scan)[4] = reinterpret_cast<unsigned char (*)[4]>(line.data() + 4);
+    for (long y = 0; y < h; y++) {
+        if (!decrunch(scan, (int)w, f)) break;
+        float *dst = rgb.data() + (size_t)y * w * 3;
+        for (long x = 0; x < w; x++) {
+            int e = (int)scan[x][3] - 128;
+            float d = ldexpf(1.0f, e);
+            dst[3 * x + 0] = (scan[x][0] / 256.0f) * d;
+            dst[3 * x + 1] = (scan[x][1] / 256.0f) * d;
+            dst[3 * x + 2] = (scan[x][2] / 256.0f) * d;
+        }
+    }
+    fclose(f);
+    w_out = (int32_t)w;
+    h_out = (int32_t)h;
+    return TT_OK;
+}
+
+// ---- scene JSON -------------------------------------------------------------------------------
+static std::string resolve(const std::string &base_dir, const std::string &p) {
+    if (p.empty() || p[0] == '/') return p;
+    std::ifstream probe(p);
+    if (probe.good()) return p;  // relative to the working directory, as the reference reads it
+    return base_dir + p;
+}
+
+tt_status load_scene_json(const std::string &path, Scene &sc) {
+    Json cfg;
+    tt_status st = parse_json_file(path, cfg);
+    if (st != TT_OK) return st;
+    std::string base_dir;
+    size_t slash = path.find_last_of('/');
+    if (slash != std::string::npos) base_dir = path.substr(0, slash + 1);
+    auto req = [&](const char *k, Json::Kind kind) -> const Json * {
+        const Json *j = cfg.find(k);
+        return (j && j->kind == kind) ? j : nullptr;
+    };
+    const Json *camera = req("camera", Json::OBJ);
+    const Json *workdir = req("work-dir", Json::STR);
+    const Json *hdr = req("hdr-file-name", Json::STR);
+    const Json *mtl = req("material-file", Json::STR);
+    const Json *samples = req("samples", Json::NUM);
+    const Json *objects = req("objects", Json::ARR);
+    if (!camera || !workdir || !hdr || !mtl || !samples || !objects)
+        return fail(TT_ERR_FORMAT, path + ": missing one of camera, work-dir, hdr-file-name, material-file, samples, objects");
+    const Json *w = camera->find("width"), *h = camera->find("height");
+    if (!w || !h || w->kind != Json::NUM || h->kind != Json::NUM) return fail(TT_ERR_FORMAT, path + ": camera width/height");
+    sc = Scene();
+    sc.work_dir = workdir->str;
+    sc.hdr_file = resolve(base_dir, hdr->str);
+    sc.material_file = resolve(base_dir, mtl->str);
+    sc.samples = (int32_t)samples->inum;
+    if (const Json *b = cfg.find("bvh-reload")) sc.bvh_reload = b->b;
+    if (const Json *b = cfg.find("material-reload")) sc.material_reload = b->b;
+    if (const Json *d = cfg.find("max-depth")) sc.max_depth = (int32_t)d->inum;
+    if (const Json *d = cfg.find("rr-depth")) sc.rr_depth = (int32_t)d->inum;
+    CameraConfig &cam = sc.camera;
+    cam.width = (int32_t)w->inum;
+    cam.height = (int32_t)h->inum;
+    V3 v;
+    if (json_vec3(camera->find("position"), v)) cam.position = v;
+    if (const Json *j = camera->find("yaw")) cam.yaw = j->as_float();
+    if (const Json *j = camera->find("pitch")) cam.pitch = j->as_float();
+    if (const Json *j = camera->find("focal")) cam.focal = j->as_float();
+    if (const Json *j = camera->find("aperture")) cam.aperture = j->as_float();
+
+    std::map<std::string, int32_t> master;
+    if ((st = load_material_pool(sc.material_file, sc, master)) != TT_OK) return st;
+    for (const Json &obj : objects->arr) {
+        const Json *type = obj.find("type");
+        if (!type || type->kind != Json::STR) return fail(TT_ERR_FORMAT, path + ": object without type");
+        if (type->str == "Mesh") {
+            const Json *file = obj.find("file");
+            if (!file || file->kind != Json::STR) return fail(TT_ERR_FORMAT, path + ": Mesh without file");
+            if ((st = load_obj(resolve(base_dir, file->str), transform_matrix(obj), sc)) != TT_OK) return st;
+        } else if (type->str == "Plane" || type->str == "Sphere") {
+            GeomRec g;
+            memset(&g, 0, sizeof(g));
+            const Json *m = obj.find("material");
+            if (!m || m->kind != Json::STR || !master.count(m->str))
+                return fail(TT_ERR_FORMAT, path + ": object material missing from the material file");
+            g.mat = master[m->str];
+            if (type->str == "Plane") {
+                g.kind = GEOM_PLANE;
+                V3 a, b, c;
+                if (!json_vec3(obj.find("p0"), a) || !json_vec3(obj.find("p1"), b) || !json_vec3(obj.find("p2"), c))
+                    return fail(TT_ERR_FORMAT, path + ": Plane needs p0, p1, p2");
+                memcpy(g.p0, &a, 12);
+                memcpy(g.p1, &b, 12);
+                memcpy(g.p2, &c, 12);
+            } else {
+                g.kind = GEOM_SPHERE;
+                const Json *r = obj.find("radius");
+                if (!r || r->kind != Json::NUM || !json_vec3(obj.find("position"), v))
+                    return fail(TT_ERR_FORMAT, path + ": Sphere needs radius and position");
+                g.radius = r->as_float();
+                memcpy(g.p0, &v, 12);
+            }
+            sc.geoms.push_back(g);
+        }
+        // other types are ignored, as in the reference
+    }
+    // An empty hdr-file-name means "no environment" (black on miss); a named file must load,
+    // as HDRLoader::load throws when it is missing (src/loader/HDRLoader.cpp:11-17).
+    if (!hdr->str.empty()) {
+        if ((st = load_hdr(sc.hdr_file, sc.env_w, sc.env_h, sc.env_rgb)) != TT_OK) return st;
+    }
+    return TT_OK;
+}
+
+}  // namespace tt
