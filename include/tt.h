@@ -89,6 +89,9 @@ tt_status tt_scene_counts(const tt_scene *scene, int32_t counts[5]);
 /* copies of the triangle soup: any pointer may be NULL */
 tt_status tt_scene_arrays(const tt_scene *scene, float *vertices, float *normals, int32_t *vidx,
                           int32_t *nidx, uint32_t *mat);
+/* The environment map HDRLoader::load read for the scene (src/loader/HDRLoader.cpp:5-65):
+ * width, height and, when rgb != NULL, w*h*3 linear floats, row 0 first. 0 x 0 = none. */
+tt_status tt_scene_env(const tt_scene *scene, int32_t *width, int32_t *height, float *rgb);
 void tt_scene_free(tt_scene *scene);
 
 /* ---- SBVH build and the compact layout (host) ------------------------------------ */

@@ -17,9 +17,12 @@ LIB = HERE / "_build" / "liboracle.so"
 
 SLAB_FMA, CROSS_A, CROSS_B, DOT_A, DOT_B, INTERP_A, INTERP_B = 1, 2, 4, 8, 16, 32, 64
 PLAIN = 0
-# The contraction nvcc applies to the reference's intersect() on sm_103a; pinned against the
-# reference kernel's own outputs in tests/golden (see tests/test_oracle_golden.py).
-DEVICE = SLAB_FMA | CROSS_A | DOT_A | INTERP_A
+# The contraction nvcc 13.0 applies to the reference's intersect() on sm_103a: x*y - z and
+# a*b - c*d fuse the LEFT product, a*b + c*d + e*f fuses the first sum's left product and then
+# the last product. Pinned against the reference kernel's own outputs on a GB300
+# (tests/golden/trace_gpu_golden.npz, tests/test_oracle_golden.py); of the five candidate
+# patterns only this one reproduces every id, distance and normal bit.
+DEVICE = SLAB_FMA | CROSS_A | DOT_B | INTERP_B
 
 _h = None
 

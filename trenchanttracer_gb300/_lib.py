@@ -40,6 +40,7 @@ SIGNATURES = {
     "tt_scene_create": (I32, [P, I32, P, I32, P, P, P, I32, C.POINTER(P)]),
     "tt_scene_counts": (I32, [P, C.POINTER(I32)]),
     "tt_scene_arrays": (I32, [P, P, P, P, P, P]),
+    "tt_scene_env": (I32, [P, C.POINTER(I32), C.POINTER(I32), P]),
     "tt_scene_free": (None, [P]),
     "tt_bvh_build": (I32, [P, F32, I32, I32, I32, C.POINTER(P)]),
     "tt_bvh_save": (I32, [P, C.c_char_p]),

@@ -67,6 +67,16 @@ class Scene:
         check(lib().tt_scene_arrays(self._h, *(_ptr(out[k]) for k in ["vertices", "normals", "vidx", "nidx", "mat"])))
         return out
 
+    def env(self) -> np.ndarray | None:
+        """The scene's environment map as (h, w, 3) float32, or None."""
+        w, h = C.c_int32(), C.c_int32()
+        check(lib().tt_scene_env(self._h, C.byref(w), C.byref(h), None))
+        if w.value == 0:
+            return None
+        out = np.empty((h.value, w.value, 3), np.float32)
+        check(lib().tt_scene_env(self._h, C.byref(w), C.byref(h), _ptr(out)))
+        return out
+
     def __del__(self):
         if getattr(self, "_h", None):
             lib().tt_scene_free(self._h)

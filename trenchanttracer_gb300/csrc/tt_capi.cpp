@@ -102,6 +102,15 @@ tt_status tt_scene_arrays(const tt_scene *scene, float *vertices, float *normals
     return TT_OK;
 }
 
+tt_status tt_scene_env(const tt_scene *scene, int32_t *width, int32_t *height, float *rgb) {
+    if (!scene || !width || !height) return fail(TT_ERR_INVALID, "null argument");
+    const Scene &sc = scene->s;
+    *width = sc.env_w;
+    *height = sc.env_h;
+    if (rgb && !sc.env_rgb.empty()) memcpy(rgb, sc.env_rgb.data(), 4 * sc.env_rgb.size());
+    return TT_OK;
+}
+
 void tt_scene_free(tt_scene *scene) { delete scene; }
 
 tt_status tt_bvh_build(const tt_scene *scene, float split_alpha, int32_t leaf_min, int32_t leaf_max,

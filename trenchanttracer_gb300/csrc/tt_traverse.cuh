@@ -53,13 +53,13 @@ __device__ __forceinline__ float slab(float b, float idir, float ood) { return _
 __device__ __forceinline__ float cross_c(float ay, float bz, float az, float by) {
     return __fmaf_rn(ay, bz, -__fmul_rn(az, by));
 }
-// a.x*b.x + a.y*b.y + a.z*b.z  ->  fma(a.z, b.z, fma(a.y, b.y, a.x*b.x))
+// a.x*b.x + a.y*b.y + a.z*b.z  ->  fma(a.z, b.z, fma(a.x, b.x, a.y*b.y))
 __device__ __forceinline__ float dot_c(float ax, float ay, float az, float bx, float by, float bz) {
-    return __fmaf_rn(az, bz, __fmaf_rn(ay, by, __fmul_rn(ax, bx)));
+    return __fmaf_rn(az, bz, __fmaf_rn(ax, bx, __fmul_rn(ay, by)));
 }
-// n0*(1-u-v) + n1*u + n2*v per component  ->  fma(n2, v, fma(n1, u, n0*w))
+// n0*(1-u-v) + n1*u + n2*v per component  ->  fma(n2, v, fma(n0, w, n1*u))
 __device__ __forceinline__ float interp_c(float n0, float n1, float n2, float w, float u, float v) {
-    return __fmaf_rn(n2, v, __fmaf_rn(n1, u, __fmul_rn(n0, w)));
+    return __fmaf_rn(n2, v, __fmaf_rn(n0, w, __fmul_rn(n1, u)));
 }
 
 // Signed-integer min/max on float bit patterns (the reference's vmin/vmax).
