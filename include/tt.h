@@ -118,6 +118,31 @@ void tt_bvh_free(tt_bvh *bvh);
 tt_status tt_bvh_upload(const tt_bvh *bvh, tt_dbvh **out);
 void tt_dbvh_free(tt_dbvh *dbvh);
 
+/* Kernel shape used by the traversal calls on `bvh` (a tuning knob; the reference launches one
+ * ray per thread, src/core/RenderKernel.cu:221-231):
+ *   0 TT_VARIANT_WARP       each warp traces 32 consecutive rays, stack in local memory
+ *   1 TT_VARIANT_WARP_SH16  (default) as 0, the lowest 16 stack entries in shared memory
+ *   2 TT_VARIANT_WARP_SH32  as 0, the lowest 32 stack entries in shared memory
+ *   3 TT_VARIANT_DYNAMIC    every lane claims a new ray as soon as it finishes one
+ *   4 TT_VARIANT_WARP_VOTE  as 0, with the reference's warp-vote leaf postponement
+ *                           (IntersectKernel.cuh:180-203)
+ * All variants but 4 return the per-ray result of the reference's algorithm and are identical;
+ * variant 4 can differ from them in float corner cases, as the reference's own kernel does. */
+#define TT_VARIANT_WARP 0
+#define TT_VARIANT_WARP_SH16 1
+#define TT_VARIANT_WARP_SH32 2
+#define TT_VARIANT_DYNAMIC 3
+#define TT_VARIANT_WARP_VOTE 4
+#define TT_NUM_VARIANTS 5
+tt_status tt_dbvh_set_variant(tt_dbvh *bvh, int32_t variant);
+tt_status tt_dbvh_get_variant(const tt_dbvh *bvh, int32_t *variant);
+/* Autotuner: traces the n device rays with every variant (the warp-vote one only when
+ * include_vote != 0), three launches each, keeps the fastest for `bvh` and writes each
+ * variant's best time in ms to ms_out[variant] (TT_NUM_VARIANTS floats; skipped variants get
+ * 0; may be NULL). Synchronises `stream`. */
+tt_status tt_dbvh_autotune(tt_dbvh *bvh, const tt_ray *d_rays, int64_t n, tt_hit *d_hits,
+                           int32_t closest, int32_t include_vote, void *stream, float *ms_out);
+
 /* intersect(ray, bvh, needClosestHit) (include/geometry/IntersectKernel.cuh:78-296) over n
  * rays in device memory; hits are written to device memory. closest = 1 is the closest hit,
  * 0 the any hit (first accepted triangle in traversal order). */

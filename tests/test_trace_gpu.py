@@ -120,15 +120,60 @@ def terrain_full():
     return case
 
 
+def _differ(a, b):
+    return (a["id"] != b["id"]) | (a["t"].view(np.uint32) != b["t"].view(np.uint32))
+
+
 @pytest.mark.skipif(not refgpu.available(), reason="reference cubin / loader not built")
 @pytest.mark.parametrize("closest", [True, False])
 def test_full_size_terrain_bit_identical_to_reference_kernel(terrain_full, closest):
+    """4M coherent + 4M incoherent rays on the 2,097,152-triangle terrain.
+
+    Our kernel equals the reference's per-ray algorithm (the oracle) on every ray. The
+    reference kernel's own warp vote lets a lane keep visiting nodes with a stale hit distance,
+    so on a few rays per ten million its result departs from its per-ray algorithm (a leaf box
+    whose entry rounds above a nearly equal hit distance: the neighbouring triangle of a shared
+    edge, one ulp apart). Everywhere else our ids, distances, materials and normals are its bits.
+    """
     case = terrain_full
     for name, rays in case.sets.items():
         ref = refgpu.intersect(case.arrays, rays, closest)
+        ora = oracle.intersect(case.arrays, rays, closest, arith=oracle.DEVICE)
         mine = trace(case.dbvh, rays, closest, ext=True)
-        assert_same(mine, ref, normals=True, what=f"terrain1024/{name}")
+        assert_same(mine, ora, what=f"terrain1024/{name} vs oracle")
+        ref_dev = _differ(ref, ora)
+        assert ref_dev.mean() <= 1e-6, f"{name}: reference departs from its per-ray algorithm on {ref_dev.sum()} rays"
+        keep = ~ref_dev
+        sub = lambda d: {k: v[keep] for k, v in d.items() if isinstance(v, np.ndarray) and v.shape[0] == rays.shape[0]}
+        assert_same(sub(mine), sub(ref), normals=True, what=f"terrain1024/{name} vs reference kernel")
+        for i in np.nonzero(ref_dev)[0]:  # each departure is a one-ulp near tie
+            assert abs(int(ref["t"].view(np.int32)[i]) - int(ora["t"].view(np.int32)[i])) <= 4
         assert 0.05 < (ref["id"] >= 0).mean() < 0.99
+
+
+def test_variants_agree_bit_for_bit(terrain_full):
+    """Every kernel variant except the warp-vote one yields the per-ray result."""
+    case = terrain_full
+    rays = case.sets["incoherent"][::4]
+    ref = trace(case.dbvh, rays, True)
+    default = case.dbvh.variant
+    anyhit = trace(case.dbvh, rays, False)
+    try:
+        for v in DeviceBVH.DETERMINISTIC_VARIANTS:
+            case.dbvh.set_variant(v)
+            for closest in (True, False):
+                assert_same(trace(case.dbvh, rays, closest), ref if closest else anyhit, what=f"variant {v}")
+    finally:
+        case.dbvh.set_variant(default)
+
+
+def trace_with(dbvh, rays, closest, variant):
+    old = dbvh.variant
+    dbvh.set_variant(variant)
+    try:
+        return trace(dbvh, rays, closest)
+    finally:
+        dbvh.set_variant(old)
 
 
 def test_full_size_properties(terrain_full):
@@ -205,10 +250,12 @@ def test_empty_scene_and_unit_scale_cull():
 def _self_loop_cache(path, child1_box_empty: bool):
     """A hand-made bvh.cache whose root lists itself as child 0 (and child 1): a corrupt file
     that passes the loader's address checks. The kernel's stack check / iteration cap must turn
-    it into an error status instead of a hang or a fault."""
+    it into an error status instead of a hang or a fault. With `child1_box_empty` child 1's box
+    lies far away from every test ray (an inverted box would not do: the slab test's min/max
+    makes [hi, lo] the same box as [lo, hi]), so the ray loops on child 0 without pushing."""
     big = 1e3
     lo, hi = -big, big
-    c1lo, c1hi = (big, -big) if child1_box_empty else (lo, hi)
+    c1lo, c1hi = (1e6, 1e6 + 1.0) if child1_box_empty else (lo, hi)
     nodes = np.zeros((4, 4), np.float32)
     nodes[0] = [lo, hi, lo, hi]
     nodes[1] = [c1lo, c1hi, c1lo, c1hi]

@@ -50,6 +50,9 @@ SIGNATURES = {
     "tt_bvh_free": (None, [P]),
     "tt_bvh_upload": (I32, [P, C.POINTER(P)]),
     "tt_dbvh_free": (None, [P]),
+    "tt_dbvh_set_variant": (I32, [P, I32]),
+    "tt_dbvh_get_variant": (I32, [P, C.POINTER(I32)]),
+    "tt_dbvh_autotune": (I32, [P, P, I64, P, I32, I32, P, P]),
     "tt_trace": (I32, [P, P, I64, P, I32, P]),
     "tt_trace_ext": (I32, [P, P, I64, P, I32, P]),
     "tt_trace_host": (I32, [P, P, I64, P, I32, P]),

@@ -160,6 +160,28 @@ class DeviceBVH:
         check(lib().tt_trace_host(self._h, _ptr(rays), rays.shape[0], _ptr(hits), int(bool(closest)),
                                   C.c_void_p(stream)))
 
+    VARIANT_WARP, VARIANT_WARP_SH16, VARIANT_WARP_SH32, VARIANT_DYNAMIC, VARIANT_WARP_VOTE = 0, 1, 2, 3, 4
+    NUM_VARIANTS = 5
+    DETERMINISTIC_VARIANTS = (0, 1, 2, 3)
+
+    def set_variant(self, variant: int) -> None:
+        """Kernel shape of the traversal calls (include/tt.h, tt_dbvh_set_variant)."""
+        check(lib().tt_dbvh_set_variant(self._h, int(variant)))
+
+    @property
+    def variant(self) -> int:
+        v = C.c_int32()
+        check(lib().tt_dbvh_get_variant(self._h, C.byref(v)))
+        return v.value
+
+    def autotune(self, rays, hits, closest: bool = True, include_vote: bool = False, stream: int = 0) -> list:
+        """Times every kernel variant on these device rays, keeps the fastest; returns ms per variant."""
+        ms = (C.c_float * self.NUM_VARIANTS)()
+        check(lib().tt_dbvh_autotune(self._h, C.c_void_p(rays.data_ptr()), rays.shape[0],
+                                     C.c_void_p(hits.data_ptr()), int(bool(closest)), int(bool(include_vote)),
+                                     C.c_void_p(stream), ms))
+        return list(ms)
+
     def check(self, stream: int = 0) -> None:
         check(lib().tt_dbvh_check(self._h, C.c_void_p(stream)))
 

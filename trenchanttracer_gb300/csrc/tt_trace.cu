@@ -1,14 +1,26 @@
 // Ray-cast kernels (closest-hit / any-hit) and the device half of the compact BVH.
 //
-// Kernel shape: persistent warps. The grid is sized to fill every SM (152 on GB300) with
-// resident blocks; each warp claims 32 consecutive rays with one atomic on a per-BVH work
-// counter, so lane i of a warp always traces ray base+i, as in a one-ray-per-thread launch,
-// while warps that finish early take more work instead of idling at the tail.
+// All kernels are persistent grids sized to fill every SM of the GB300 with resident blocks.
+// Kernel shapes (tt_dbvh_set_variant; tt_dbvh_autotune times them and keeps the fastest):
+//   TT_VARIANT_WARP       each warp claims 32 consecutive rays (lane i traces ray base+i, as a
+//                         one-ray-per-thread launch would) and traces them with the per-ray
+//                         semantics; the whole traversal stack is in local memory.
+//   TT_VARIANT_WARP_SH16  as WARP, the lowest 16 stack entries in shared memory (the rest, rarely
+//   TT_VARIANT_WARP_SH32  touched, in local memory), so stack traffic does not evict BVH nodes
+//                         from L1; SH32 keeps 32 entries.
+//   TT_VARIANT_DYNAMIC    every lane claims a new ray (one warp-aggregated atomic per claim
+//                         round: ballot + popc + one atomicAdd) as soon as it finishes one.
+//   TT_VARIANT_WARP_VOTE  as WARP, but a lane that has postponed a leaf keeps visiting inner
+//                         nodes until a warp vote says every active lane holds one, as the
+//                         reference kernel does (IntersectKernel.cuh:180-203). Which lanes are
+//                         active at the vote depends on how the warp re-converges, so in float
+//                         corner cases (a leaf box whose entry rounds above a nearly equal hit
+//                         distance) the result can depend on the other rays of the warp.
+// All but WARP_VOTE return the per-ray result of the reference's algorithm, bit for bit.
 #include <cuda_runtime.h>
 
 #include <cstdio>
 #include <cstring>
-#include <mutex>
 #include <string>
 
 #include "tt_internal.h"
@@ -17,19 +29,26 @@
 namespace tt {
 
 constexpr int kTraceBlock = 128;
+enum TraceVariant : int {
+    VARIANT_WARP = 0,
+    VARIANT_WARP_SH16 = 1,
+    VARIANT_WARP_SH32 = 2,
+    VARIANT_DYNAMIC = 3,
+    VARIANT_WARP_VOTE = 4,
+    NUM_VARIANTS = 5
+};
 
 struct DeviceBVH {
     BvhView view;
     void *base = nullptr;          // one allocation holding all five arrays
     size_t bytes = 0;
     uint32_t num_nodes = 0, num_verts = 0;
-    uint32_t *scratch = nullptr;   // [0] work counter, [1] error word
+    unsigned long long *scratch = nullptr;  // [0] work counter, [1] error word (low 32 bits)
     int device = 0;
     int num_sms = 0;
-    int blocks_per_sm = 0;
-    // pinned staging for the host-buffer entry point
-    void *h_stage = nullptr;
-    size_t h_stage_bytes = 0;
+    int blocks_per_sm[NUM_VARIANTS] = {1, 1, 1, 1, 1};
+    int variant = VARIANT_WARP_SH16;
+    // device staging for the host-buffer entry point
     void *d_stage = nullptr;
     size_t d_stage_bytes = 0;
 };
@@ -39,56 +58,123 @@ struct TraceArgs {
     const float4 *rays;  // 2 float4 per ray
     int64_t n;
     void *hits;
-    uint32_t *counter;
-    uint32_t *err;
+    unsigned long long *counter;
+    unsigned int *err;
 };
 
-template <bool kClosest, bool kExt>
-__global__ void __launch_bounds__(kTraceBlock) trace_kernel(TraceArgs a) {
+template <bool kExt>
+__device__ __forceinline__ void store_hit(const TraceArgs &a, int64_t i, const TravState &s) {
+    int id = -1;
+    if (s.addr >= 0) id = __ldg(a.bvh.tri_idx + s.addr);
+    if (!kExt) {
+        reinterpret_cast<int2 *>(a.hits)[i] = make_int2(id, __float_as_int(s.t));
+    } else {
+        int mat = -1;
+        float nx = 0.f, ny = 0.f, nz = 0.f;
+        if (s.addr >= 0) {
+            mat = (int)__ldg(a.bvh.mat_idx + s.addr);
+            hit_normal(a.bvh, s.addr, s.u, s.v, nx, ny, nz);
+        }
+        tt_hit_ext *o = reinterpret_cast<tt_hit_ext *>(a.hits) + i;
+        o->id = id;
+        o->mat = mat;
+        o->t = s.t;
+        o->nx = nx;
+        o->ny = ny;
+        o->nz = nz;
+    }
+}
+
+// Warp-batched: each warp claims 32 consecutive rays. kSh stack entries live in shared memory.
+template <bool kClosest, bool kExt, bool kSpec, int kSh>
+__global__ void __launch_bounds__(kTraceBlock) trace_warp_kernel(TraceArgs a) {
+    __shared__ int sh_stack[(kSh > 0 ? kSh : 1) * kTraceBlock];
     const int lane = threadIdx.x & 31;
     uint32_t err = 0;
+    TravStack<kSh, kTraceBlock> stack;
+    stack.sh = sh_stack + threadIdx.x;
     for (;;) {
-        uint32_t base = 0;
-        if (lane == 0) base = atomicAdd(a.counter, 32u);
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(a.counter, 32ull);
         base = __shfl_sync(0xffffffffu, base, 0);
         if ((int64_t)base >= a.n) break;
         const int64_t i = (int64_t)base + lane;
         if (i < a.n) {
-            const float4 r0 = __ldg(a.rays + 2 * i);
-            const float4 r1 = __ldg(a.rays + 2 * i + 1);
-            TraceResult h = traverse<kClosest>(a.bvh, r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, err);
-            int id = -1;
-            if (h.addr >= 0) id = __ldg(a.bvh.tri_idx + h.addr);
-            if (!kExt) {
-                reinterpret_cast<int2 *>(a.hits)[i] = make_int2(id, __float_as_int(h.t));
-            } else {
-                int mat = -1;
-                float nx = 0.f, ny = 0.f, nz = 0.f;
-                if (h.addr >= 0) {
-                    mat = (int)__ldg(a.bvh.mat_idx + h.addr);
-                    hit_normal(a.bvh, h.addr, h.u, h.v, nx, ny, nz);
-                }
-                tt_hit_ext *o = reinterpret_cast<tt_hit_ext *>(a.hits) + i;
-                o->id = id;
-                o->mat = mat;
-                o->t = h.t;
-                o->nx = nx;
-                o->ny = ny;
-                o->nz = nz;
+            TravState s;
+            const float4 r0 = __ldg(a.rays + 2 * i), r1 = __ldg(a.rays + 2 * i + 1);
+            trav_init(s, stack, r0, r1);
+            while (!trav_iterate<kClosest, kSpec>(s, stack, a.bvh, err, r1.w)) {
             }
+            store_hit<kExt>(a, i, s);
         }
         __syncwarp();
     }
     if (err) atomicOr(a.err, err);
 }
 
+// Dynamic per-lane fetch: a lane that finishes its ray claims the next one at the top of the
+// following outer iteration; claims are aggregated per warp.
+template <bool kClosest, bool kExt, int kSh>
+__global__ void __launch_bounds__(kTraceBlock) trace_dynamic_kernel(TraceArgs a) {
+    __shared__ int sh_stack[(kSh > 0 ? kSh : 1) * kTraceBlock];
+    const int lane = threadIdx.x & 31;
+    const unsigned lanemask_lt = (1u << lane) - 1u;
+    uint32_t err = 0;
+    TravStack<kSh, kTraceBlock> stack;
+    stack.sh = sh_stack + threadIdx.x;
+    TravState s;
+    int64_t ray = -1;
+    float tmax = 0.f;
+    bool exhausted = false;
+    for (;;) {
+        const bool need = (ray < 0) && !exhausted;
+        const unsigned needmask = __ballot_sync(0xffffffffu, need);
+        if (needmask) {
+            const int leader = __ffs(needmask) - 1;
+            unsigned long long base = 0;
+            if (lane == leader) base = atomicAdd(a.counter, (unsigned long long)__popc(needmask));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (need) {
+                const int64_t idx = (int64_t)base + __popc(needmask & lanemask_lt);
+                if (idx < a.n) {
+                    ray = idx;
+                    const float4 r0 = __ldg(a.rays + 2 * idx), r1 = __ldg(a.rays + 2 * idx + 1);
+                    tmax = r1.w;
+                    trav_init(s, stack, r0, r1);
+                } else {
+                    exhausted = true;
+                }
+            }
+        }
+        if (__all_sync(0xffffffffu, exhausted)) break;
+        if (ray >= 0) {
+            if (trav_iterate<kClosest, false>(s, stack, a.bvh, err, tmax)) {
+                store_hit<kExt>(a, ray, s);
+                ray = -1;
+            }
+        }
+    }
+    if (err) atomicOr(a.err, err);
+}
+
+template <bool kClosest, bool kExt>
+static const void *kernel_for(int variant) {
+    switch (variant) {
+        case VARIANT_WARP: return (const void *)trace_warp_kernel<kClosest, kExt, false, 0>;
+        case VARIANT_WARP_SH16: return (const void *)trace_warp_kernel<kClosest, kExt, false, 16>;
+        case VARIANT_WARP_SH32: return (const void *)trace_warp_kernel<kClosest, kExt, false, 32>;
+        case VARIANT_DYNAMIC: return (const void *)trace_dynamic_kernel<kClosest, kExt, 16>;
+        default: return (const void *)trace_warp_kernel<kClosest, kExt, true, 0>;
+    }
+}
+
 static tt_status cuda_fail(cudaError_t e, const char *what) {
     return fail(TT_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-#define TT_CUDA(call)                                   \
-    do {                                                \
-        cudaError_t e_ = (call);                        \
+#define TT_CUDA(call)                                       \
+    do {                                                    \
+        cudaError_t e_ = (call);                            \
         if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
     } while (0)
 
@@ -97,9 +183,11 @@ static tt_status upload(const CompactBVH &b, DeviceBVH &d) {
     TT_CUDA(cudaGetDevice(&dev));
     d.device = dev;
     TT_CUDA(cudaDeviceGetAttribute(&d.num_sms, cudaDevAttrMultiProcessorCount, dev));
-    int bps = 0;
-    TT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, trace_kernel<true, false>, kTraceBlock, 0));
-    d.blocks_per_sm = bps > 0 ? bps : 1;
+    for (int v = 0; v < NUM_VARIANTS; v++) {
+        int bps = 0;
+        TT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kernel_for<true, false>(v), kTraceBlock, 0));
+        d.blocks_per_sm[v] = bps > 0 ? bps : 1;
+    }
     const size_t nb = 16ull * b.nodes.size(), vb = 16ull * b.vertices.size(), mb = 16ull * b.normals.size();
     const size_t tb = 4ull * b.tri_idx.size(), ab = 4ull * b.mat_idx.size();
     auto align = [](size_t x) { return (x + 255) & ~size_t(255); };
@@ -132,48 +220,68 @@ static tt_status upload(const CompactBVH &b, DeviceBVH &d) {
 static void release(DeviceBVH &d) {
     if (d.base) cudaFree(d.base);
     if (d.scratch) cudaFree(d.scratch);
-    if (d.h_stage) cudaFreeHost(d.h_stage);
     if (d.d_stage) cudaFree(d.d_stage);
     d = DeviceBVH();
 }
 
+template <bool kClosest, bool kExt>
+static void launch_variant(int variant, unsigned blocks, cudaStream_t stream, const TraceArgs &a) {
+    switch (variant) {
+        case VARIANT_WARP:
+            trace_warp_kernel<kClosest, kExt, false, 0><<<blocks, kTraceBlock, 0, stream>>>(a);
+            break;
+        case VARIANT_WARP_SH16:
+            trace_warp_kernel<kClosest, kExt, false, 16><<<blocks, kTraceBlock, 0, stream>>>(a);
+            break;
+        case VARIANT_WARP_SH32:
+            trace_warp_kernel<kClosest, kExt, false, 32><<<blocks, kTraceBlock, 0, stream>>>(a);
+            break;
+        case VARIANT_DYNAMIC:
+            trace_dynamic_kernel<kClosest, kExt, 16><<<blocks, kTraceBlock, 0, stream>>>(a);
+            break;
+        default:
+            trace_warp_kernel<kClosest, kExt, true, 0><<<blocks, kTraceBlock, 0, stream>>>(a);
+    }
+}
+
 static tt_status launch_trace(const DeviceBVH &d, const void *d_rays, int64_t n, void *d_hits, bool closest,
                               bool ext, cudaStream_t stream) {
-    if (n < 0 || n > (int64_t)0xFFFFFFFF - 64) return fail(TT_ERR_INVALID, "ray count out of range");
+    if (n < 0 || n > ((int64_t)1 << 40)) return fail(TT_ERR_INVALID, "ray count out of range");
     if (n == 0) return TT_OK;
     if (!d_rays || !d_hits) return fail(TT_ERR_INVALID, "null ray or hit buffer");
     if ((reinterpret_cast<uintptr_t>(d_rays) & 15) || (reinterpret_cast<uintptr_t>(d_hits) & 7))
         return fail(TT_ERR_INVALID, "ray buffer must be 16-byte aligned and hit buffer 8-byte aligned");
-    TT_CUDA(cudaMemsetAsync(d.scratch, 0, 4, stream));
+    TT_CUDA(cudaMemsetAsync(d.scratch, 0, 8, stream));
     TraceArgs a;
     a.bvh = d.view;
     a.rays = reinterpret_cast<const float4 *>(d_rays);
     a.n = n;
     a.hits = d_hits;
     a.counter = d.scratch;
-    a.err = d.scratch + 1;
+    a.err = reinterpret_cast<unsigned int *>(d.scratch + 1);
     const int64_t warps_needed = (n + 31) / 32;
-    int64_t blocks = (int64_t)d.num_sms * d.blocks_per_sm;
+    int64_t blocks = (int64_t)d.num_sms * d.blocks_per_sm[d.variant];
     const int64_t max_useful = (warps_needed * 32 + kTraceBlock - 1) / kTraceBlock;
     if (blocks > max_useful) blocks = max_useful;
     if (blocks < 1) blocks = 1;
     if (closest) {
-        if (ext) trace_kernel<true, true><<<(unsigned)blocks, kTraceBlock, 0, stream>>>(a);
-        else trace_kernel<true, false><<<(unsigned)blocks, kTraceBlock, 0, stream>>>(a);
+        if (ext) launch_variant<true, true>(d.variant, (unsigned)blocks, stream, a);
+        else launch_variant<true, false>(d.variant, (unsigned)blocks, stream, a);
     } else {
-        if (ext) trace_kernel<false, true><<<(unsigned)blocks, kTraceBlock, 0, stream>>>(a);
-        else trace_kernel<false, false><<<(unsigned)blocks, kTraceBlock, 0, stream>>>(a);
+        if (ext) launch_variant<false, true>(d.variant, (unsigned)blocks, stream, a);
+        else launch_variant<false, false>(d.variant, (unsigned)blocks, stream, a);
     }
     TT_CUDA(cudaGetLastError());
     return TT_OK;
 }
 
 static tt_status read_error_word(const DeviceBVH &d, cudaStream_t stream) {
-    uint32_t w = 0;
+    unsigned int w = 0;
     TT_CUDA(cudaMemcpyAsync(&w, d.scratch + 1, 4, cudaMemcpyDeviceToHost, stream));
     TT_CUDA(cudaStreamSynchronize(stream));
     if (w) {
-        TT_CUDA(cudaMemsetAsync(d.scratch + 1, 0, 4, stream));
+        TT_CUDA(cudaMemsetAsync(d.scratch + 1, 0, 8, stream));
+        TT_CUDA(cudaStreamSynchronize(stream));
         if (w & kErrStack) return fail(TT_ERR_BOUNDS, "traversal stack overflow (BVH deeper than 66 levels)");
         return fail(TT_ERR_TIMEOUT, "traversal iteration cap reached (corrupt BVH?)");
     }
@@ -209,6 +317,56 @@ void tt_dbvh_free(tt_dbvh *dbvh) {
     if (!dbvh) return;
     release(dbvh->d);
     delete dbvh;
+}
+
+tt_status tt_dbvh_set_variant(tt_dbvh *bvh, int32_t variant) {
+    if (!bvh || variant < 0 || variant >= NUM_VARIANTS) return fail(TT_ERR_INVALID, "unknown traversal variant");
+    bvh->d.variant = variant;
+    return TT_OK;
+}
+
+tt_status tt_dbvh_get_variant(const tt_dbvh *bvh, int32_t *variant) {
+    if (!bvh || !variant) return fail(TT_ERR_INVALID, "null argument");
+    *variant = bvh->d.variant;
+    return TT_OK;
+}
+
+tt_status tt_dbvh_autotune(tt_dbvh *bvh, const tt_ray *d_rays, int64_t n, tt_hit *d_hits, int32_t closest,
+                           int32_t include_vote, void *stream, float *ms_out) {
+    if (!bvh) return fail(TT_ERR_INVALID, "null BVH");
+    cudaStream_t s = (cudaStream_t)stream;
+    DeviceBVH &d = bvh->d;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    TT_CUDA(cudaEventCreate(&e0));
+    TT_CUDA(cudaEventCreate(&e1));
+    float best = 1e30f;
+    int best_v = d.variant;
+    tt_status st = TT_OK;
+    for (int v = 0; v < NUM_VARIANTS && st == TT_OK; v++) {
+        if (ms_out) ms_out[v] = 0.f;
+        if (v == VARIANT_WARP_VOTE && !include_vote) continue;
+        d.variant = v;
+        float ms_min = 1e30f;
+        for (int rep = 0; rep < 3 && st == TT_OK; rep++) {
+            cudaEventRecord(e0, s);
+            st = launch_trace(d, d_rays, n, d_hits, closest != 0, false, s);
+            cudaEventRecord(e1, s);
+            cudaEventSynchronize(e1);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (rep > 0 && ms < ms_min) ms_min = ms;  // the first launch is a warm-up
+        }
+        if (ms_out) ms_out[v] = ms_min;
+        if (ms_min < best) {
+            best = ms_min;
+            best_v = v;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    d.variant = best_v;
+    if (st != TT_OK) return st;
+    return read_error_word(d, s);
 }
 
 tt_status tt_trace(const tt_dbvh *bvh, const tt_ray *d_rays, int64_t n, tt_hit *d_hits, int32_t closest,

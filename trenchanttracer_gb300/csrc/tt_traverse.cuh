@@ -8,8 +8,9 @@
 //     bits for z and the tmin / hit-distance operand (the Kepler video min/max, :22-60);
 //   - a child is entered iff entry <= exit, entry >= tmin and entry <= 1e20 (:145-147);
 //     near-first order, the far child pushed, swap only when c1 entry < c0 entry (:149-167);
-//   - one postponed leaf per lane and a warp vote that ends the inner-node loop once every
-//     active lane holds a leaf (:169-203);
+//   - one postponed leaf per lane (:169-178); the reference's warp vote (:180-203) is available
+//     as an option, but by default a lane processes its leaf without visiting further nodes, so
+//     the result is the per-ray result of the reference's algorithm whatever the other lanes do;
 //   - Moller-Trumbore on the three raw float4 vertices, accepting only det > 1e-5 with
 //     u in [0,1], v >= 0, u+v <= 1; the det < -1e-5 branch keeps the reference's comparisons
 //     (which reject every finite u) (:209-271); a hit needs tmin < t < current distance;
@@ -20,10 +21,11 @@
 // the reference kernel's own outputs.
 //
 // GB300 choices: all BVH and triangle reads are 16-byte read-only vector loads
-// (ld.global.nc.v4) so they go through the L1/tex path without texture objects; the
-// traversal stack lives in a per-thread local array that stays in L1; every loop carries an
-// iteration cap and the stack a bounds check, both reported through an error word instead of
-// faulting or hanging.
+// (ld.global.nc.v4) so they go through the L1/tex path without texture objects; the traversal
+// stack keeps its lower entries in a per-thread column of shared memory (conflict-free: lane i
+// of entry k sits at k*blockDim + i) and spills only entries beyond that into local memory, so
+// stack traffic does not evict BVH nodes from L1; every loop carries an iteration cap and the
+// stack a bounds check, both reported through an error word instead of faulting or hanging.
 #pragma once
 
 #include <cstdint>
@@ -76,149 +78,218 @@ __device__ __forceinline__ float span_end(float a0, float a1, float b0, float b1
     return __int_as_float(imin(x, y));
 }
 
+// ---- traversal stack ---------------------------------------------------------------------------
+// Entries [0, kSh) live in shared memory at sh[i * kStride]; the rest in a local array.
+template <int kSh, int kStride>
+struct TravStack {
+    int *sh;
+    int loc[kStackSize - kSh + 1];
+    __device__ __forceinline__ int get(int i) const {
+        if (kSh > 0 && i < kSh) return sh[i * kStride];
+        return loc[i - kSh];
+    }
+    __device__ __forceinline__ void set(int i, int v) {
+        if (kSh > 0 && i < kSh) sh[i * kStride] = v;
+        else loc[i - kSh] = v;
+    }
+};
+
+// Resumable per-ray traversal state.
+struct TravState {
+    float ox, oy, oz, dx, dy, dz, tmin;
+    float idirx, idiry, idirz, oodx, oody, oodz;
+    float t, u, v;  // current hit distance (tmax until a hit) and barycentrics of the hit
+    int addr;       // float4 slot of the hit triangle, -1 = none yet
+    int node, leaf, sp;
+    uint32_t iter;
+};
+
+template <class Stack>
+__device__ __forceinline__ void trav_init(TravState &s, Stack &stack, float4 r0, float4 r1) {
+    s.ox = r0.x;
+    s.oy = r0.y;
+    s.oz = r0.z;
+    s.dx = r0.w;
+    s.dy = r1.x;
+    s.dz = r1.y;
+    s.tmin = r1.z;
+    s.t = r1.w;
+    const float ooeps = 8.27180612553027674871e-25f;  // exp2f(-80), exact
+    s.idirx = __fdiv_rn(1.0f, fabsf(s.dx) > ooeps ? s.dx : copysignf(ooeps, s.dx));
+    s.idiry = __fdiv_rn(1.0f, fabsf(s.dy) > ooeps ? s.dy : copysignf(ooeps, s.dy));
+    s.idirz = __fdiv_rn(1.0f, fabsf(s.dz) > ooeps ? s.dz : copysignf(ooeps, s.dz));
+    s.oodx = __fmul_rn(s.ox, s.idirx);
+    s.oody = __fmul_rn(s.oy, s.idiry);
+    s.oodz = __fmul_rn(s.oz, s.idirz);
+    s.u = 0.f;
+    s.v = 0.f;
+    s.addr = -1;
+    s.node = 0;
+    s.leaf = 0;
+    s.sp = 0;
+    s.iter = 0;
+    stack.set(0, kEntrypointSentinel);
+}
+
+__device__ __forceinline__ void trav_fail(TravState &s, uint32_t &err, uint32_t code, float tmax) {
+    err |= code;
+    s.addr = -1;
+    s.t = tmax;
+    s.node = kEntrypointSentinel;
+    s.leaf = kEntrypointSentinel;
+}
+
+// One inner-node visit of the reference's inner loop (IntersectKernel.cuh:112-178).
+// Returns false if the ray failed (stack / iteration bound).
+template <class Stack>
+__device__ __forceinline__ bool trav_node_step(TravState &s, Stack &stack, const BvhView &bvh, uint32_t &err,
+                                               float tmax) {
+    const float4 n0xy = ldg4(bvh.nodes + s.node);
+    const float4 n1xy = ldg4(bvh.nodes + s.node + 1);
+    const float4 nz = ldg4(bvh.nodes + s.node + 2);
+    const float4 tmp = ldg4(bvh.nodes + s.node + 3);
+    const float c0lox = slab(n0xy.x, s.idirx, s.oodx);
+    const float c0hix = slab(n0xy.y, s.idirx, s.oodx);
+    const float c0loy = slab(n0xy.z, s.idiry, s.oody);
+    const float c0hiy = slab(n0xy.w, s.idiry, s.oody);
+    const float c0loz = slab(nz.x, s.idirz, s.oodz);
+    const float c0hiz = slab(nz.y, s.idirz, s.oodz);
+    const float c1loz = slab(nz.z, s.idirz, s.oodz);
+    const float c1hiz = slab(nz.w, s.idirz, s.oodz);
+    const float c0min = span_begin(c0lox, c0hix, c0loy, c0hiy, c0loz, c0hiz, s.tmin);
+    const float c0max = span_end(c0lox, c0hix, c0loy, c0hiy, c0loz, c0hiz, s.t);
+    const float c1lox = slab(n1xy.x, s.idirx, s.oodx);
+    const float c1hix = slab(n1xy.y, s.idirx, s.oodx);
+    const float c1loy = slab(n1xy.z, s.idiry, s.oody);
+    const float c1hiy = slab(n1xy.w, s.idiry, s.oody);
+    const float c1min = span_begin(c1lox, c1hix, c1loy, c1hiy, c1loz, c1hiz, s.tmin);
+    const float c1max = span_end(c1lox, c1hix, c1loy, c1hiy, c1loz, c1hiz, s.t);
+    const bool t0 = (c0min <= c0max) && (c0min >= s.tmin) && (c0min <= 1e20f);
+    const bool t1 = (c1min <= c1max) && (c1min >= s.tmin) && (c1min <= 1e20f);
+    if (!t0 && !t1) {
+        s.node = stack.get(s.sp--);
+    } else {
+        int far_child = __float_as_int(tmp.y);
+        s.node = t0 ? __float_as_int(tmp.x) : far_child;
+        if (t0 && t1) {
+            if (c1min < c0min) {
+                const int sw = s.node;
+                s.node = far_child;
+                far_child = sw;
+            }
+            if (s.sp + 1 >= kStackSize) {
+                trav_fail(s, err, kErrStack, tmax);
+                return false;
+            }
+            stack.set(++s.sp, far_child);
+        }
+    }
+    if (s.node < 0 && s.leaf >= 0) {
+        s.leaf = s.node;
+        s.node = stack.get(s.sp--);
+    }
+    if (++s.iter > kMaxIterations) {
+        trav_fail(s, err, kErrIter, tmax);
+        return false;
+    }
+    return true;
+}
+
+// The reference's leaf loop (IntersectKernel.cuh:209-281) for a lane holding a postponed leaf:
+// that leaf, then every leaf popped right after it. Returns false if the ray failed.
+template <bool kClosest, class Stack>
+__device__ __forceinline__ bool trav_leaf_phase(TravState &s, Stack &stack, const BvhView &bvh, uint32_t &err,
+                                                float tmax) {
+    while (s.leaf < 0) {
+        for (int tri = ~s.leaf;; tri += 3) {
+            const float4 v0 = ldg4(bvh.verts + tri);
+            if (__float_as_int(v0.x) == (int)0x80000000) break;
+            const float4 v1 = ldg4(bvh.verts + tri + 1);
+            const float4 v2 = ldg4(bvh.verts + tri + 2);
+            if (++s.iter > kMaxIterations) {
+                trav_fail(s, err, kErrIter, tmax);
+                return false;
+            }
+            const float e1x = __fsub_rn(v1.x, v0.x), e1y = __fsub_rn(v1.y, v0.y), e1z = __fsub_rn(v1.z, v0.z);
+            const float e2x = __fsub_rn(v2.x, v0.x), e2y = __fsub_rn(v2.y, v0.y), e2z = __fsub_rn(v2.z, v0.z);
+            const float tvx = __fsub_rn(s.ox, v0.x), tvy = __fsub_rn(s.oy, v0.y), tvz = __fsub_rn(s.oz, v0.z);
+            const float px = cross_c(s.dy, e2z, s.dz, e2y);
+            const float py = cross_c(s.dz, e2x, s.dx, e2z);
+            const float pz = cross_c(s.dx, e2y, s.dy, e2x);
+            const float det = dot_c(e1x, e1y, e1z, px, py, pz);
+            const float inv_det = __fdiv_rn(1.0f, det);
+            const float u = __fmul_rn(dot_c(tvx, tvy, tvz, px, py, pz), inv_det);
+            const float qx = cross_c(tvy, e1z, tvz, e1y);
+            const float qy = cross_c(tvz, e1x, tvx, e1z);
+            const float qz = cross_c(tvx, e1y, tvy, e1x);
+            const float v = __fmul_rn(dot_c(s.dx, s.dy, s.dz, qx, qy, qz), inv_det);
+            const float kEps = 0.00001f;
+            if (det > kEps) {
+                if (u < 0.0f || u > 1.0f) continue;
+                if (v < 0.0f || __fadd_rn(u, v) > 1.0f) continue;
+            } else if (det < -kEps) {
+                if (u > 0.0f || u < 1.0f) continue;
+                if (v > 0.0f || __fadd_rn(u, v) < 1.0f) continue;
+            } else {
+                continue;
+            }
+            const float t = __fmul_rn(dot_c(e2x, e2y, e2z, qx, qy, qz), inv_det);
+            if (s.tmin < t && t < s.t) {
+                s.t = t;
+                s.addr = tri;
+                s.u = u;
+                s.v = v;
+                if (!kClosest) {
+                    s.node = kEntrypointSentinel;
+                    break;
+                }
+            }
+        }
+        s.leaf = s.node;
+        if (s.node < 0) s.node = stack.get(s.sp--);
+    }
+    return true;
+}
+
+// One pass of the reference's outer loop: inner nodes until a leaf is postponed and the next
+// entry is found (kSpec = false: this lane alone decides, so the result depends on nothing but
+// the ray; kSpec = true: continue speculatively until a warp vote says every active lane holds a
+// leaf, as the reference kernel does), then the pending leaves. Returns true when the ray is
+// finished. tmax is needed only to report a failed ray as a miss.
+template <bool kClosest, bool kSpec, class Stack>
+__device__ __forceinline__ bool trav_iterate(TravState &s, Stack &stack, const BvhView &bvh, uint32_t &err,
+                                             float tmax) {
+    while (s.node >= 0 && s.node != kEntrypointSentinel) {
+        if (!trav_node_step(s, stack, bvh, err, tmax)) return true;
+        if (kSpec) {
+            if (__ballot_sync(__activemask(), s.leaf >= 0) == 0u) break;
+        } else {
+            if (s.leaf < 0) break;
+        }
+    }
+    if (!trav_leaf_phase<kClosest>(s, stack, bvh, err, tmax)) return true;
+    return s.node == kEntrypointSentinel;
+}
+
 struct TraceResult {
     int addr;  // float4 slot of the hit triangle, -1 = miss
     float t;   // hit distance; tmax on a miss
     float u, v;
 };
 
-// One ray through the BVH. kClosest selects closest-hit vs any-hit.
+// One ray through the BVH, start to finish, with its whole stack in local memory.
 template <bool kClosest>
-__device__ __forceinline__ TraceResult traverse(const BvhView &bvh, float ox, float oy, float oz, float dx, float dy,
-                                                float dz, float tmin, float tmax, uint32_t &err) {
-    const float ooeps = 8.27180612553027674871e-25f;  // exp2f(-80), exact
-    const float idirx = __fdiv_rn(1.0f, fabsf(dx) > ooeps ? dx : copysignf(ooeps, dx));
-    const float idiry = __fdiv_rn(1.0f, fabsf(dy) > ooeps ? dy : copysignf(ooeps, dy));
-    const float idirz = __fdiv_rn(1.0f, fabsf(dz) > ooeps ? dz : copysignf(ooeps, dz));
-    const float oodx = __fmul_rn(ox, idirx);
-    const float oody = __fmul_rn(oy, idiry);
-    const float oodz = __fmul_rn(oz, idirz);
-
-    int stack[kStackSize];
-    int sp = 0;
-    stack[0] = kEntrypointSentinel;
-    int leaf_addr = 0;
-    int node_addr = 0;
-    TraceResult res;
-    res.addr = -1;
-    res.t = tmax;
-    res.u = 0.f;
-    res.v = 0.f;
-    uint32_t iter = 0;
-
-    while (node_addr != kEntrypointSentinel) {
-        while (node_addr >= 0 && node_addr != kEntrypointSentinel) {
-            const float4 n0xy = ldg4(bvh.nodes + node_addr);
-            const float4 n1xy = ldg4(bvh.nodes + node_addr + 1);
-            const float4 nz = ldg4(bvh.nodes + node_addr + 2);
-            const float4 tmp = ldg4(bvh.nodes + node_addr + 3);
-
-            const float c0lox = slab(n0xy.x, idirx, oodx);
-            const float c0hix = slab(n0xy.y, idirx, oodx);
-            const float c0loy = slab(n0xy.z, idiry, oody);
-            const float c0hiy = slab(n0xy.w, idiry, oody);
-            const float c0loz = slab(nz.x, idirz, oodz);
-            const float c0hiz = slab(nz.y, idirz, oodz);
-            const float c1loz = slab(nz.z, idirz, oodz);
-            const float c1hiz = slab(nz.w, idirz, oodz);
-            const float c0min = span_begin(c0lox, c0hix, c0loy, c0hiy, c0loz, c0hiz, tmin);
-            const float c0max = span_end(c0lox, c0hix, c0loy, c0hiy, c0loz, c0hiz, res.t);
-            const float c1lox = slab(n1xy.x, idirx, oodx);
-            const float c1hix = slab(n1xy.y, idirx, oodx);
-            const float c1loy = slab(n1xy.z, idiry, oody);
-            const float c1hiy = slab(n1xy.w, idiry, oody);
-            const float c1min = span_begin(c1lox, c1hix, c1loy, c1hiy, c1loz, c1hiz, tmin);
-            const float c1max = span_end(c1lox, c1hix, c1loy, c1hiy, c1loz, c1hiz, res.t);
-
-            const bool t0 = (c0min <= c0max) && (c0min >= tmin) && (c0min <= 1e20f);
-            const bool t1 = (c1min <= c1max) && (c1min >= tmin) && (c1min <= 1e20f);
-
-            if (!t0 && !t1) {
-                node_addr = stack[sp--];
-            } else {
-                int far_child = __float_as_int(tmp.y);
-                node_addr = t0 ? __float_as_int(tmp.x) : far_child;
-                if (t0 && t1) {
-                    if (c1min < c0min) {
-                        const int s = node_addr;
-                        node_addr = far_child;
-                        far_child = s;
-                    }
-                    if (sp + 1 >= kStackSize) {
-                        err |= kErrStack;
-                        res.addr = -1;
-                        res.t = tmax;
-                        return res;
-                    }
-                    stack[++sp] = far_child;
-                }
-            }
-            if (node_addr < 0 && leaf_addr >= 0) {
-                leaf_addr = node_addr;
-                node_addr = stack[sp--];
-            }
-            if (++iter > kMaxIterations) {
-                err |= kErrIter;
-                res.addr = -1;
-                res.t = tmax;
-                return res;
-            }
-            if (__ballot_sync(__activemask(), leaf_addr >= 0) == 0u) break;
-        }
-
-        while (leaf_addr < 0) {
-            for (int tri = ~leaf_addr;; tri += 3) {
-                const float4 v0 = ldg4(bvh.verts + tri);
-                if (__float_as_int(v0.x) == (int)0x80000000) break;
-                const float4 v1 = ldg4(bvh.verts + tri + 1);
-                const float4 v2 = ldg4(bvh.verts + tri + 2);
-                if (++iter > kMaxIterations) {
-                    err |= kErrIter;
-                    res.addr = -1;
-                    res.t = tmax;
-                    return res;
-                }
-
-                const float e1x = __fsub_rn(v1.x, v0.x), e1y = __fsub_rn(v1.y, v0.y), e1z = __fsub_rn(v1.z, v0.z);
-                const float e2x = __fsub_rn(v2.x, v0.x), e2y = __fsub_rn(v2.y, v0.y), e2z = __fsub_rn(v2.z, v0.z);
-                const float tvx = __fsub_rn(ox, v0.x), tvy = __fsub_rn(oy, v0.y), tvz = __fsub_rn(oz, v0.z);
-                const float px = cross_c(dy, e2z, dz, e2y);
-                const float py = cross_c(dz, e2x, dx, e2z);
-                const float pz = cross_c(dx, e2y, dy, e2x);
-                const float det = dot_c(e1x, e1y, e1z, px, py, pz);
-                const float inv_det = __fdiv_rn(1.0f, det);
-                const float u = __fmul_rn(dot_c(tvx, tvy, tvz, px, py, pz), inv_det);
-                const float qx = cross_c(tvy, e1z, tvz, e1y);
-                const float qy = cross_c(tvz, e1x, tvx, e1z);
-                const float qz = cross_c(tvx, e1y, tvy, e1x);
-                const float v = __fmul_rn(dot_c(dx, dy, dz, qx, qy, qz), inv_det);
-
-                const float kEps = 0.00001f;
-                if (det > kEps) {
-                    if (u < 0.0f || u > 1.0f) continue;
-                    if (v < 0.0f || __fadd_rn(u, v) > 1.0f) continue;
-                } else if (det < -kEps) {
-                    if (u > 0.0f || u < 1.0f) continue;
-                    if (v > 0.0f || __fadd_rn(u, v) < 1.0f) continue;
-                } else {
-                    continue;
-                }
-                const float t = __fmul_rn(dot_c(e2x, e2y, e2z, qx, qy, qz), inv_det);
-                if (tmin < t && t < res.t) {
-                    res.t = t;
-                    res.addr = tri;
-                    res.u = u;
-                    res.v = v;
-                    if (!kClosest) {
-                        node_addr = kEntrypointSentinel;
-                        break;
-                    }
-                }
-            }
-            leaf_addr = node_addr;
-            if (node_addr < 0) node_addr = stack[sp--];
-        }
+__device__ __forceinline__ TraceResult traverse(const BvhView &bvh, float4 r0, float4 r1, uint32_t &err) {
+    TravStack<0, 1> stack;
+    TravState s;
+    trav_init(s, stack, r0, r1);
+    while (!trav_iterate<kClosest, false>(s, stack, bvh, err, r1.w)) {
     }
+    TraceResult res;
+    res.addr = s.addr;
+    res.t = s.t;
+    res.u = s.u;
+    res.v = s.v;
     return res;
 }
 
