@@ -164,6 +164,29 @@ tt_status tt_trace_host(const tt_dbvh *bvh, const tt_ray *h_rays, int64_t n, tt_
  * this way are reported as misses. */
 tt_status tt_dbvh_check(const tt_dbvh *bvh, void *stream);
 
+/* Allocation-free tracing with HOST ray and hit buffers. No counterpart in the reference: it is
+ * an addition for callers that cannot allocate device memory, such as a host application whose
+ * device memory belongs to its own arena (it uploads the BVH into that memory itself and passes
+ * the arrays here), or a frame loop that must not stall on the device-wide synchronisation a
+ * cudaMalloc can cause. tt_trace_host allocates its device staging on first use and whenever a
+ * call needs more; this entry point never allocates (no cudaMalloc, cudaFree or allocating
+ * library call). Ray and hit staging, the work counter and the error word live in one fixed
+ * ~10 MiB array inside libtt.so that every GPU loading the library holds until the process
+ * exits.
+ *   d_nodes, d_vertices, d_tri_indices  the caller's device copies of the compact BVH arrays
+ *                                       (the layout of tt_bvh_arrays / bvh.cache); 16-, 16- and
+ *                                       4-byte aligned
+ *   n                                   at most TT_NOALLOC_MAX_RAYS rays per call; larger n is
+ *                                       rejected with TT_ERR_INVALID and a message
+ * Results are those of tt_trace_host with the default kernel variant. The stream is
+ * synchronised before returning. The first call on each device also looks up the device address
+ * of the staging array; make that first call before any stream capture. All calls share the one
+ * array: calls that overlap on the GPU (other host threads, other streams) race. */
+#define TT_NOALLOC_MAX_RAYS (1 << 18)
+tt_status tt_trace_host_noalloc(const void *d_nodes, const void *d_vertices, const int32_t *d_tri_indices,
+                                const tt_ray *h_rays, int64_t n, tt_hit *h_hits, int32_t closest,
+                                void *stream);
+
 #ifdef __cplusplus
 }
 #endif

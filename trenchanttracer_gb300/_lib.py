@@ -57,6 +57,7 @@ SIGNATURES = {
     "tt_trace_ext": (I32, [P, P, I64, P, I32, P]),
     "tt_trace_host": (I32, [P, P, I64, P, I32, P]),
     "tt_dbvh_check": (I32, [P, P]),
+    "tt_trace_host_noalloc": (I32, [P, P, P, P, I64, P, I32, P]),
 }
 
 _lib: C.CDLL | None = None

@@ -21,6 +21,7 @@
 
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 
 #include "tt_internal.h"
@@ -288,6 +289,48 @@ static tt_status read_error_word(const DeviceBVH &d, cudaStream_t stream) {
     return TT_OK;
 }
 
+// ---- allocation-free host-buffer tracing ----------------------------------------------------------
+// A fixed staging area for tt_trace_host_noalloc: a 256-byte header (64-bit work counter, 32-bit
+// error word) followed by room for kNoAllocMaxRays rays (32 B each) and their hits (8 B each),
+// about 10 MiB in all. Every GPU that loads this library holds it until the process exits.
+constexpr int64_t kNoAllocMaxRays = 1 << 18;
+constexpr size_t kNoAllocHeader = 256;
+constexpr size_t kNoAllocBytes = kNoAllocHeader + (size_t)kNoAllocMaxRays * (32 + 8);
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+struct NoAllocDevice {
+    unsigned char *scratch = nullptr;  // device address of g_noalloc_scratch on this device
+    int num_sms = 0;
+    int blocks_per_sm = 0;
+};
+static std::mutex g_noalloc_mu;
+static NoAllocDevice g_noalloc_dev[kNoAllocMaxDevices];
+
+// Once per device, with that device current: the device address of the staging array (host code
+// must not hand the array's host-side name to a kernel) and the launch shape.
+static tt_status noalloc_setup(NoAllocDevice &out) {
+    int dev = 0;
+    TT_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return fail(TT_ERR_INVALID, "device ordinal out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    NoAllocDevice &d = g_noalloc_dev[dev];
+    if (!d.scratch) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+        int sms = 0, bps = 0;
+        TT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        TT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kernel_for<true, false>(VARIANT_WARP_SH16),
+                                                              kTraceBlock, 0));
+        d.num_sms = sms;
+        d.blocks_per_sm = bps > 0 ? bps : 1;
+        d.scratch = static_cast<unsigned char *>(p);
+    }
+    out = d;
+    return TT_OK;
+}
+
 }  // namespace tt
 
 struct tt_dbvh {
@@ -409,6 +452,51 @@ tt_status tt_trace_host(const tt_dbvh *bvh, const tt_ray *h_rays, int64_t n, tt_
 tt_status tt_dbvh_check(const tt_dbvh *bvh, void *stream) {
     if (!bvh) return fail(TT_ERR_INVALID, "null BVH");
     return read_error_word(bvh->d, (cudaStream_t)stream);
+}
+
+// tt_trace_host for callers that must not allocate device memory: the BVH arrays are the
+// caller's own device memory, and the staging of rays and hits plus the work counter and error
+// word live in g_noalloc_scratch. Allocates nothing (no cudaMalloc, cudaFree or library
+// allocation). The first call on a device also looks up the staging array's device address.
+tt_status tt_trace_host_noalloc(const void *d_nodes, const void *d_vertices, const int32_t *d_tri_indices,
+                                const tt_ray *h_rays, int64_t n, tt_hit *h_hits, int32_t closest, void *stream) {
+    if (n < 0 || n > kNoAllocMaxRays)
+        return fail(TT_ERR_INVALID, "tt_trace_host_noalloc: " + std::to_string(n) +
+                                        " rays exceed the allocation-free staging capacity of " +
+                                        std::to_string(kNoAllocMaxRays) +
+                                        " rays per call; split the batch (or use tt_trace_host)");
+    if (n == 0) return TT_OK;
+    if (!d_nodes || !d_vertices || !d_tri_indices || !h_rays || !h_hits)
+        return fail(TT_ERR_INVALID, "tt_trace_host_noalloc: null argument");
+    if ((reinterpret_cast<uintptr_t>(d_nodes) & 15) || (reinterpret_cast<uintptr_t>(d_vertices) & 15) ||
+        (reinterpret_cast<uintptr_t>(d_tri_indices) & 3))
+        return fail(TT_ERR_INVALID, "tt_trace_host_noalloc: BVH arrays must be 16-byte (nodes, vertices) and "
+                                    "4-byte (triangle indices) aligned");
+    NoAllocDevice nd;
+    tt_status st = noalloc_setup(nd);
+    if (st != TT_OK) return st;
+    DeviceBVH d;  // a view only: nothing here is owned or freed
+    d.view.nodes = static_cast<const float4 *>(d_nodes);
+    d.view.verts = static_cast<const float4 *>(d_vertices);
+    d.view.norms = nullptr;
+    d.view.tri_idx = d_tri_indices;
+    d.view.mat_idx = nullptr;
+    d.scratch = reinterpret_cast<unsigned long long *>(nd.scratch);
+    d.num_sms = nd.num_sms;
+    d.variant = VARIANT_WARP_SH16;
+    d.blocks_per_sm[VARIANT_WARP_SH16] = nd.blocks_per_sm;
+    cudaStream_t s = (cudaStream_t)stream;
+    char *dr = reinterpret_cast<char *>(nd.scratch) + kNoAllocHeader;
+    char *dh = dr + 32 * (size_t)kNoAllocMaxRays;
+    // the header keeps the last call's contents: the error word must start at zero (the launch
+    // itself zeroes the work counter)
+    TT_CUDA(cudaMemsetAsync(nd.scratch + 8, 0, 8, s));
+    TT_CUDA(cudaMemcpyAsync(dr, h_rays, 32ull * n, cudaMemcpyHostToDevice, s));
+    st = launch_trace(d, dr, n, dh, closest != 0, false, s);
+    if (st != TT_OK) return st;
+    TT_CUDA(cudaMemcpyAsync(h_hits, dh, 8ull * n, cudaMemcpyDeviceToHost, s));
+    TT_CUDA(cudaStreamSynchronize(s));
+    return read_error_word(d, s);
 }
 
 }  // extern "C"
