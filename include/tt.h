@@ -66,7 +66,57 @@ typedef struct tt_bvh_header {
     uint32_t mat_indices; /* uint32 count, same indexing as vertices */
 } tt_bvh_header;
 
+/* CameraMeta (include/core/Camera.h:8-16), byte for byte: 60 B. */
+typedef struct tt_camera_meta {
+    int32_t width, height;
+    float position[3];
+    float view[3];
+    float up[3];
+    float fov[2];
+    float aperture;
+    float focal;
+} tt_camera_meta;
+
+/* RenderMeta (include/core/Renderer.h:24-31), byte for byte: 20 B. */
+typedef struct tt_render_meta {
+    int32_t frame_number;
+    uint32_t hashed_frame;
+    int32_t samples;
+    float pi;
+    float two_pi;
+} tt_render_meta;
+
+/* A material, flattened (the reference keeps a polymorphic MaterialUnion,
+ * include/material/MaterialUnion.h). kind: 0 Diff, 1 Metal, 2 Spec, 3 Refr, 4 Coat (the
+ * reference's MaterialType values, include/material/Material.h:11-13), 5 GGX conductor,
+ * 6 dielectric. color = diffuseColor (Diff, Coat) / color (Metal, Spec) / F0 (GGX);
+ * color2 = specularColor (Coat). 64 B. */
+typedef struct tt_material {
+    int32_t kind;
+    float emission[3];
+    float color[3];
+    float color2[3];
+    float roughness; /* GGX: alpha = roughness^2 */
+    float ior;       /* dielectric */
+    float pad[4];
+} tt_material;
+
+/* An analytic object of the scene JSON (include/geometry/{Plane,Sphere}.h). kind: 0 Sphere,
+ * 3 Plane (the reference's GeometryType values). Plane: p0, p1, p2 (a parallelogram); Sphere:
+ * radius and position in p0. 64 B. */
+typedef struct tt_geometry {
+    int32_t kind;
+    int32_t material;
+    float radius;
+    float pad;
+    float p0[3];
+    float p1[3];
+    float p2[3];
+    float pad2[3];
+} tt_geometry;
+
 typedef struct tt_scene tt_scene; /* host triangle soup + materials (core/Scene.h) */
+typedef struct tt_renderer tt_renderer; /* device materials, analytic objects, environment */
 typedef struct tt_bvh tt_bvh;     /* host compact SBVH arrays (bvh/BVHCompact.h) */
 typedef struct tt_dbvh tt_dbvh;   /* device-resident compact SBVH */
 
@@ -92,6 +142,13 @@ tt_status tt_scene_arrays(const tt_scene *scene, float *vertices, float *normals
 /* The environment map HDRLoader::load read for the scene (src/loader/HDRLoader.cpp:5-65):
  * width, height and, when rgb != NULL, w*h*3 linear floats, row 0 first. 0 x 0 = none. */
 tt_status tt_scene_env(const tt_scene *scene, int32_t *width, int32_t *height, float *rgb);
+/* Replaces the environment map (width*height*3 linear floats, row 0 first; 0 x 0 = none). */
+tt_status tt_scene_set_env(tt_scene *scene, int32_t width, int32_t height, const float *rgb);
+/* Materials and analytic objects: counts via tt_scene_counts; `out` may be NULL. */
+tt_status tt_scene_materials(const tt_scene *scene, tt_material *out);
+tt_status tt_scene_set_materials(tt_scene *scene, const tt_material *materials, int32_t count);
+tt_status tt_scene_geometries(const tt_scene *scene, tt_geometry *out);
+tt_status tt_scene_set_geometries(tt_scene *scene, const tt_geometry *geometries, int32_t count);
 void tt_scene_free(tt_scene *scene);
 
 /* ---- SBVH build and the compact layout (host) ------------------------------------ */
@@ -182,6 +239,32 @@ tt_status tt_dbvh_check(const tt_dbvh *bvh, void *stream);
  * synchronised before returning. The first call on each device also looks up the device address
  * of the staging array; make that first call before any stream capture. All calls share the one
  * array: calls that overlap on the GPU (other host threads, other streams) race. */
+/* ---- camera and frame metadata (host) ---------------------------------------------------- */
+/* Camera(config) + Camera::setFovx(fovx) + Camera::getCameraMeta() for the scene's camera block
+ * (src/core/Camera.cpp:12-44, :115-140; the reference's main uses fovx = 45). */
+tt_status tt_camera_meta_from_scene(const tt_scene *scene, float fovx, tt_camera_meta *out);
+/* RenderMeta of frame `frame_number` (1 for the first frame): hashed_frame =
+ * WangHash::encode(frame_number) (src/util/WangHash.cpp:8-15, Renderer.cpp:107) and the
+ * reference's PI = 3.14156265f and TWO_PI constants (Renderer.cpp:5-6). */
+tt_status tt_render_meta_init(int32_t frame_number, int32_t samples, tt_render_meta *out);
+uint32_t tt_wang_hash(uint32_t a);
+
+/* ---- path tracing ------------------------------------------------------------------------- */
+/* The renderer's device state: the scene's materials, analytic Plane/Sphere objects and
+ * environment map, over an uploaded BVH (which must outlive the renderer); the device half of
+ * Renderer::Renderer (src/core/Renderer.cpp:8-57) without the GL parts. */
+tt_status tt_renderer_create(const tt_dbvh *bvh, const tt_scene *scene, tt_renderer **out);
+void tt_renderer_free(tt_renderer *renderer);
+/* One frame of the reference's path tracer, Renderer::render / pathTracingKernel
+ * (src/core/RenderKernel.cu:97-233): adds sum_s L / samples of every pixel to d_accum
+ * (width*height*3 floats, row 0 = the image's bottom row, as the reference stores it). Uses
+ * curand XORWOW streams seeded as the reference does, so a frame equals the reference kernel's
+ * for the same inputs. Launch only. */
+tt_status tt_render_compat(tt_renderer *renderer, const tt_camera_meta *cam, const tt_render_meta *meta,
+                           float *d_accum, void *stream);
+/* Synchronises `stream` and reports traversal errors of the renderer's launches. */
+tt_status tt_renderer_check(tt_renderer *renderer, void *stream);
+
 #define TT_NOALLOC_MAX_RAYS (1 << 18)
 tt_status tt_trace_host_noalloc(const void *d_nodes, const void *d_vertices, const int32_t *d_tri_indices,
                                 const tt_ray *h_rays, int64_t n, tt_hit *h_hits, int32_t closest,

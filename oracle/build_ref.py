@@ -76,6 +76,21 @@ struct RenderMeta {
     float PI;
     float TWO_PI;
 };
+class HDRImage;
+class Renderer {
+public:
+    Vec3f *accumulatedBuffer;
+    Vec3f *outputBuffer;
+    CameraMeta *cameraMetaDevice;
+    RenderMeta renderMeta;
+    RenderMeta *renderMetaDevice;
+    Config *config;
+    BVHCompact *bvhCompact;
+    GeometryCompact *geometryCompact;
+    MaterialCompact *materialCompact;
+    HDRImage *hdrEnv;
+    void render();
+};
 #endif
 """
 BALLOT_LINE = '"vote.ballot.b32    %0,p;       \\n"'
@@ -151,6 +166,10 @@ def build(ref: Path = DEFAULT_REF, quiet: bool = True) -> bool:
         _run([str(cuda / "bin" / "nvcc"), "-cubin", "-gencode=arch=compute_103a,code=sm_103a", "-w",
               "-I" + str(tmp / "gpu"), "-I" + str(ref / "include"), "-I" + str(ref / "lib" / "include"),
               str(HERE / "ref" / "ref_gpu_harness.cu"), "-o", str(cubin)])
+        # the reference's pathTracingKernel (RenderKernel.cu) with struct-filling helpers
+        _run([str(cuda / "bin" / "nvcc"), "-cubin", "-gencode=arch=compute_103a,code=sm_103a", "-w",
+              "-I" + str(tmp / "gpu"), "-I" + str(ref / "include"), "-I" + str(ref / "lib" / "include"),
+              "-I" + str(ref), str(HERE / "ref" / "ref_render_harness.cu"), "-o", str(OUT / "ref_render.cubin")])
     if not quiet:
         print(f"built {OUT}/libttref_host.so and ref_intersect.cubin", file=sys.stderr)
     return True

@@ -53,6 +53,63 @@ def _load():
     return _h
 
 
+RENDER_CUBIN = HERE / "_ref" / "ref_render.cubin"
+
+
+def render_available() -> bool:
+    return RENDER_CUBIN.exists() and LIB.exists()
+
+
+def render(bvh_arrays: dict, materials: list, geometries: list, env: np.ndarray | None, cam, meta,
+           accum: np.ndarray) -> tuple[np.ndarray, float]:
+    """One frame of the reference's own pathTracingKernel. materials / geometries: the
+    tt_material / tt_geometry records of the scene; cam / meta: CameraMeta / RenderMeta;
+    accum: (W*H*3,) float32 starting contents. Returns (accumulation buffer, kernel ms)."""
+    h = _load()
+    if not hasattr(h, "_render_ready"):
+        h.ref_gpu_render.restype = C.c_int
+        h.ref_gpu_render.argtypes = [C.c_char_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p,
+                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int,
+                                     C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_uint,
+                                     C.c_int, C.c_float, C.c_float, C.c_void_p, C.c_void_p]
+        h._render_ready = True
+    a = {k: np.ascontiguousarray(bvh_arrays[k]) for k in ["nodes", "vertices", "normals", "tri_indices",
+                                                         "mat_indices"]}
+    geo = np.zeros((max(1, len(geometries)), 16), np.float32)
+    geo_mat = np.zeros(max(1, len(geometries)), np.int32)
+    for i, g in enumerate(geometries):
+        geo[i, 0] = g.kind
+        geo[i, 1:4] = list(g.p0)
+        geo[i, 4:7] = list(g.p1)
+        geo[i, 7:10] = list(g.p2)
+        geo[i, 10] = g.radius
+        geo_mat[i] = g.material
+    mat = np.zeros((max(1, len(materials)), 16), np.float32)
+    for i, m in enumerate(materials):
+        mat[i, 0] = m.kind
+        mat[i, 1:4] = list(m.emission)
+        mat[i, 4:7] = list(m.color)
+        mat[i, 7:10] = list(m.color2)
+    if env is None:
+        env_a, ew, eh = np.zeros(3, np.float32), 0, 0
+    else:
+        env_a = np.ascontiguousarray(env, dtype=np.float32)
+        eh, ew = env_a.shape[0], env_a.shape[1]
+    cam13 = np.array(list(cam.position) + list(cam.view) + list(cam.up) + list(cam.fov) + [cam.aperture, cam.focal],
+                     np.float32)
+    out = np.ascontiguousarray(accum, dtype=np.float32).copy()
+    ms = C.c_float(0.0)
+    rc = h.ref_gpu_render(str(RENDER_CUBIN).encode(), a["nodes"].ctypes.data, a["nodes"].shape[0],
+                          a["vertices"].ctypes.data, a["vertices"].shape[0], a["normals"].ctypes.data,
+                          a["tri_indices"].ctypes.data, a["mat_indices"].ctypes.data, geo.ctypes.data,
+                          geo_mat.ctypes.data, len(geometries), mat.ctypes.data, len(materials), env_a.ctypes.data,
+                          ew, eh, cam13.ctypes.data, cam.width, cam.height, meta.frame_number, meta.hashed_frame,
+                          meta.samples, meta.pi, meta.two_pi, out.ctypes.data, C.byref(ms))
+    if rc != 0:
+        raise RuntimeError("reference GPU render failed: " + h.ref_gpu_error().decode())
+    return out, float(ms.value)
+
+
 def intersect(bvh_arrays: dict, rays: np.ndarray, closest: bool, reps: int = 1) -> dict:
     rays = np.ascontiguousarray(rays, dtype=np.float32)
     n = rays.shape[0]

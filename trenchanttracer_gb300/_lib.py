@@ -29,6 +29,30 @@ class BvhHeader(C.Structure):
                 ("mat_indices", C.c_uint32)]
 
 
+class CameraMeta(C.Structure):
+    """tt_camera_meta == the reference's CameraMeta (include/core/Camera.h:8-16)."""
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("position", C.c_float * 3), ("view", C.c_float * 3),
+                ("up", C.c_float * 3), ("fov", C.c_float * 2), ("aperture", C.c_float), ("focal", C.c_float)]
+
+
+class RenderMeta(C.Structure):
+    """tt_render_meta == the reference's RenderMeta (include/core/Renderer.h:24-31)."""
+    _fields_ = [("frame_number", C.c_int32), ("hashed_frame", C.c_uint32), ("samples", C.c_int32),
+                ("pi", C.c_float), ("two_pi", C.c_float)]
+
+
+class Material(C.Structure):
+    """tt_material (include/tt.h)."""
+    _fields_ = [("kind", C.c_int32), ("emission", C.c_float * 3), ("color", C.c_float * 3), ("color2", C.c_float * 3),
+                ("roughness", C.c_float), ("ior", C.c_float), ("pad", C.c_float * 4)]
+
+
+class Geometry(C.Structure):
+    """tt_geometry (include/tt.h)."""
+    _fields_ = [("kind", C.c_int32), ("material", C.c_int32), ("radius", C.c_float), ("pad", C.c_float),
+                ("p0", C.c_float * 3), ("p1", C.c_float * 3), ("p2", C.c_float * 3), ("pad2", C.c_float * 3)]
+
+
 P = C.c_void_p
 I32 = C.c_int32
 I64 = C.c_int64
@@ -41,6 +65,11 @@ SIGNATURES = {
     "tt_scene_counts": (I32, [P, C.POINTER(I32)]),
     "tt_scene_arrays": (I32, [P, P, P, P, P, P]),
     "tt_scene_env": (I32, [P, C.POINTER(I32), C.POINTER(I32), P]),
+    "tt_scene_set_env": (I32, [P, I32, I32, P]),
+    "tt_scene_materials": (I32, [P, P]),
+    "tt_scene_set_materials": (I32, [P, P, I32]),
+    "tt_scene_geometries": (I32, [P, P]),
+    "tt_scene_set_geometries": (I32, [P, P, I32]),
     "tt_scene_free": (None, [P]),
     "tt_bvh_build": (I32, [P, F32, I32, I32, I32, C.POINTER(P)]),
     "tt_bvh_save": (I32, [P, C.c_char_p]),
@@ -58,6 +87,13 @@ SIGNATURES = {
     "tt_trace_host": (I32, [P, P, I64, P, I32, P]),
     "tt_dbvh_check": (I32, [P, P]),
     "tt_trace_host_noalloc": (I32, [P, P, P, P, I64, P, I32, P]),
+    "tt_camera_meta_from_scene": (I32, [P, F32, C.POINTER(CameraMeta)]),
+    "tt_render_meta_init": (I32, [I32, I32, C.POINTER(RenderMeta)]),
+    "tt_wang_hash": (C.c_uint32, [C.c_uint32]),
+    "tt_renderer_create": (I32, [P, P, C.POINTER(P)]),
+    "tt_renderer_free": (None, [P]),
+    "tt_render_compat": (I32, [P, C.POINTER(CameraMeta), C.POINTER(RenderMeta), P, P]),
+    "tt_renderer_check": (I32, [P, P]),
 }
 
 _lib: C.CDLL | None = None

@@ -50,7 +50,59 @@ class Scene:
 
     @classmethod
     def from_mesh(cls, mesh) -> "Scene":
-        return cls.from_arrays(mesh.vertices, mesh.normals, mesh.vidx, mesh.nidx, mesh.mat, mesh.materials)
+        sc = cls.from_arrays(mesh.vertices, mesh.normals, mesh.vidx, mesh.nidx, mesh.mat, mesh.materials)
+        if mesh.materials:
+            sc.set_materials(mesh.materials)
+        return sc
+
+    MATERIAL_KINDS = {"Diff": 0, "Metal": 1, "Spec": 2, "Refr": 3, "Coat": 4, "GGX": 5, "Dielectric": 6}
+
+    def set_materials(self, materials: list) -> None:
+        """Material-JSON style dicts ({"type": "Diff", "diffuseColor": [...], "emission": [...]}, ...)."""
+        arr = (_lib.Material * max(1, len(materials)))()
+        for m, d in zip(arr, materials):
+            m.kind = self.MATERIAL_KINDS[d["type"]]
+            m.emission[:] = [float(x) for x in d.get("emission", [0.0, 0.0, 0.0])]
+            col = d.get("diffuseColor", d.get("color", d.get("F0", [0.0, 0.0, 0.0])))
+            m.color[:] = [float(x) for x in col]
+            m.color2[:] = [float(x) for x in d.get("specularColor", [0.0, 0.0, 0.0])]
+            m.roughness = float(d.get("roughness", 0.5))
+            m.ior = float(d.get("ior", 1.4 if d["type"] == "Refr" else 1.5))
+        check(lib().tt_scene_set_materials(self._h, arr, len(materials)))
+
+    def materials_raw(self) -> list:
+        n = self.counts()["materials"]
+        arr = (_lib.Material * max(1, n))()
+        check(lib().tt_scene_materials(self._h, arr))
+        return list(arr)[:n]
+
+    def set_geometries(self, geoms: list) -> None:
+        """Dicts {"type": "Plane", "p0", "p1", "p2", "material": idx} or {"type": "Sphere", "radius",
+        "position", "material": idx}."""
+        arr = (_lib.Geometry * max(1, len(geoms)))()
+        for g, d in zip(arr, geoms):
+            g.kind = 3 if d["type"] == "Plane" else 0
+            g.material = int(d["material"])
+            if d["type"] == "Plane":
+                g.p0[:], g.p1[:], g.p2[:] = ([float(x) for x in d[k]] for k in ("p0", "p1", "p2"))
+            else:
+                g.radius = float(d["radius"])
+                g.p0[:] = [float(x) for x in d["position"]]
+        check(lib().tt_scene_set_geometries(self._h, arr, len(geoms)))
+
+    def geometries_raw(self) -> list:
+        n = self.counts()["geometries"]
+        arr = (_lib.Geometry * max(1, n))()
+        check(lib().tt_scene_geometries(self._h, arr))
+        return list(arr)[:n]
+
+    def set_env(self, rgb: np.ndarray | None) -> None:
+        """(h, w, 3) float32 linear RGB, row 0 first; None removes the environment."""
+        if rgb is None:
+            check(lib().tt_scene_set_env(self._h, 0, 0, None))
+            return
+        a = np.ascontiguousarray(rgb, dtype=np.float32)
+        check(lib().tt_scene_set_env(self._h, a.shape[1], a.shape[0], _ptr(a)))
 
     def counts(self) -> dict:
         c = (C.c_int32 * 5)()
@@ -188,6 +240,54 @@ class DeviceBVH:
     def __del__(self):
         if getattr(self, "_h", None):
             lib().tt_dbvh_free(self._h)
+            self._h = None
+
+
+def camera_meta(scene: Scene, fovx: float = 45.0) -> _lib.CameraMeta:
+    """Camera(config) + setFovx(fovx) + getCameraMeta() for a JSON scene's camera block."""
+    cm = _lib.CameraMeta()
+    check(lib().tt_camera_meta_from_scene(scene._h, fovx, C.byref(cm)))
+    return cm
+
+
+def make_camera_meta(width: int, height: int, position, view, up=(0.0, 1.0, 0.0), fov=(45.0, 45.0),
+                     aperture: float = 0.0, focal: float = 1.0) -> _lib.CameraMeta:
+    cm = _lib.CameraMeta()
+    cm.width, cm.height = int(width), int(height)
+    cm.position[:] = [float(x) for x in position]
+    cm.view[:] = [float(x) for x in view]
+    cm.up[:] = [float(x) for x in up]
+    cm.fov[:] = [float(x) for x in fov]
+    cm.aperture, cm.focal = float(aperture), float(focal)
+    return cm
+
+
+def render_meta(frame_number: int, samples: int) -> _lib.RenderMeta:
+    rm = _lib.RenderMeta()
+    check(lib().tt_render_meta_init(frame_number, samples, C.byref(rm)))
+    return rm
+
+
+class Renderer:
+    """The device half of the reference's Renderer (src/core/Renderer.cpp:8-57), without GL."""
+
+    def __init__(self, dbvh: DeviceBVH, scene: Scene):
+        h = C.c_void_p()
+        check(lib().tt_renderer_create(dbvh._h, scene._h, C.byref(h)))
+        self._h = h
+        self._keep = (dbvh, scene)
+
+    def render_compat(self, cam: _lib.CameraMeta, meta: _lib.RenderMeta, accum, stream: int = 0) -> None:
+        """One frame of the reference's path tracer into accum (CUDA tensor, W*H*3 float32)."""
+        check(lib().tt_render_compat(self._h, C.byref(cam), C.byref(meta), C.c_void_p(accum.data_ptr()),
+                                     C.c_void_p(stream)))
+
+    def check(self, stream: int = 0) -> None:
+        check(lib().tt_renderer_check(self._h, C.c_void_p(stream)))
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().tt_renderer_free(self._h)
             self._h = None
 
 

@@ -111,6 +111,56 @@ tt_status tt_scene_env(const tt_scene *scene, int32_t *width, int32_t *height, f
     return TT_OK;
 }
 
+static_assert(sizeof(tt_material) == sizeof(MaterialRec) && offsetof(tt_material, ior) == offsetof(MaterialRec, ior),
+              "tt_material must mirror MaterialRec");
+static_assert(sizeof(tt_geometry) == sizeof(GeomRec) && offsetof(tt_geometry, p2) == offsetof(GeomRec, p2),
+              "tt_geometry must mirror GeomRec");
+
+tt_status tt_scene_set_env(tt_scene *scene, int32_t width, int32_t height, const float *rgb) {
+    if (!scene || width < 0 || height < 0 || ((width > 0) != (height > 0)) || (width > 0 && !rgb))
+        return fail(TT_ERR_INVALID, "bad environment map");
+    TT_GUARD_BEGIN
+    Scene &sc = scene->s;
+    sc.env_w = width;
+    sc.env_h = height;
+    sc.env_rgb.assign(rgb, rgb + 3ll * width * height);
+    return TT_OK;
+    TT_GUARD_END
+}
+
+tt_status tt_scene_materials(const tt_scene *scene, tt_material *out) {
+    if (!scene) return fail(TT_ERR_INVALID, "null scene");
+    if (out && !scene->s.materials.empty())
+        memcpy(out, scene->s.materials.data(), sizeof(MaterialRec) * scene->s.materials.size());
+    return TT_OK;
+}
+
+tt_status tt_scene_set_materials(tt_scene *scene, const tt_material *materials, int32_t count) {
+    if (!scene || count < 0 || (count && !materials)) return fail(TT_ERR_INVALID, "bad materials");
+    TT_GUARD_BEGIN
+    Scene &sc = scene->s;
+    sc.materials.resize(count);
+    if (count) memcpy(sc.materials.data(), materials, sizeof(MaterialRec) * count);
+    sc.material_names.assign(count, std::string());
+    return TT_OK;
+    TT_GUARD_END
+}
+
+tt_status tt_scene_geometries(const tt_scene *scene, tt_geometry *out) {
+    if (!scene) return fail(TT_ERR_INVALID, "null scene");
+    if (out && !scene->s.geoms.empty()) memcpy(out, scene->s.geoms.data(), sizeof(GeomRec) * scene->s.geoms.size());
+    return TT_OK;
+}
+
+tt_status tt_scene_set_geometries(tt_scene *scene, const tt_geometry *geometries, int32_t count) {
+    if (!scene || count < 0 || (count && !geometries)) return fail(TT_ERR_INVALID, "bad geometries");
+    TT_GUARD_BEGIN
+    scene->s.geoms.resize(count);
+    if (count) memcpy(scene->s.geoms.data(), geometries, sizeof(GeomRec) * count);
+    return TT_OK;
+    TT_GUARD_END
+}
+
 void tt_scene_free(tt_scene *scene) { delete scene; }
 
 tt_status tt_bvh_build(const tt_scene *scene, float split_alpha, int32_t leaf_min, int32_t leaf_max,

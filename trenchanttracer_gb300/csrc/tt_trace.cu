@@ -49,10 +49,18 @@ struct DeviceBVH {
     int num_sms = 0;
     int blocks_per_sm[NUM_VARIANTS] = {1, 1, 1, 1, 1};
     int variant = VARIANT_WARP_SH16;
-    // device staging for the host-buffer entry point
+    // device staging, streams and events for the host-buffer entry point's copy/compute pipeline
     void *d_stage = nullptr;
     size_t d_stage_bytes = 0;
+    cudaStream_t pipe[3] = {nullptr, nullptr, nullptr};
+    cudaEvent_t pipe_done[3] = {nullptr, nullptr, nullptr};
+    cudaEvent_t pipe_start = nullptr;
 };
+
+// Scratch words (64-bit) of a DeviceBVH: [0] work counter of the caller-stream launches,
+// [1] error word shared by all launches, [2..4] work counters of the three pipeline streams.
+constexpr int kScratchErr = 1;
+constexpr int kScratchPipe = 2;
 
 struct TraceArgs {
     BvhView bvh;
@@ -222,6 +230,11 @@ static void release(DeviceBVH &d) {
     if (d.base) cudaFree(d.base);
     if (d.scratch) cudaFree(d.scratch);
     if (d.d_stage) cudaFree(d.d_stage);
+    for (int i = 0; i < 3; i++) {
+        if (d.pipe[i]) cudaStreamDestroy(d.pipe[i]);
+        if (d.pipe_done[i]) cudaEventDestroy(d.pipe_done[i]);
+    }
+    if (d.pipe_start) cudaEventDestroy(d.pipe_start);
     d = DeviceBVH();
 }
 
@@ -246,20 +259,20 @@ static void launch_variant(int variant, unsigned blocks, cudaStream_t stream, co
 }
 
 static tt_status launch_trace(const DeviceBVH &d, const void *d_rays, int64_t n, void *d_hits, bool closest,
-                              bool ext, cudaStream_t stream) {
+                              bool ext, cudaStream_t stream, int counter_slot = 0) {
     if (n < 0 || n > ((int64_t)1 << 40)) return fail(TT_ERR_INVALID, "ray count out of range");
     if (n == 0) return TT_OK;
     if (!d_rays || !d_hits) return fail(TT_ERR_INVALID, "null ray or hit buffer");
     if ((reinterpret_cast<uintptr_t>(d_rays) & 15) || (reinterpret_cast<uintptr_t>(d_hits) & 7))
         return fail(TT_ERR_INVALID, "ray buffer must be 16-byte aligned and hit buffer 8-byte aligned");
-    TT_CUDA(cudaMemsetAsync(d.scratch, 0, 8, stream));
+    TT_CUDA(cudaMemsetAsync(d.scratch + counter_slot, 0, 8, stream));
     TraceArgs a;
     a.bvh = d.view;
     a.rays = reinterpret_cast<const float4 *>(d_rays);
     a.n = n;
     a.hits = d_hits;
-    a.counter = d.scratch;
-    a.err = reinterpret_cast<unsigned int *>(d.scratch + 1);
+    a.counter = d.scratch + counter_slot;
+    a.err = reinterpret_cast<unsigned int *>(d.scratch + kScratchErr);
     const int64_t warps_needed = (n + 31) / 32;
     int64_t blocks = (int64_t)d.num_sms * d.blocks_per_sm[d.variant];
     const int64_t max_useful = (warps_needed * 32 + kTraceBlock - 1) / kTraceBlock;
@@ -338,6 +351,10 @@ struct tt_dbvh {
 };
 
 using namespace tt;
+
+namespace tt {
+BvhView dbvh_view(const tt_dbvh *bvh) { return bvh->d.view; }
+}  // namespace tt
 
 extern "C" {
 
@@ -439,13 +456,42 @@ tt_status tt_trace_host(const tt_dbvh *bvh, const tt_ray *h_rays, int64_t n, tt_
         if (e != cudaSuccess) return fail(TT_ERR_OOM, std::string("cudaMalloc staging: ") + cudaGetErrorString(e));
         d.d_stage_bytes = rb + hb;
     }
+    if (!d.pipe_start) {
+        for (int i = 0; i < 3; i++) {
+            TT_CUDA(cudaStreamCreateWithFlags(&d.pipe[i], cudaStreamNonBlocking));
+            TT_CUDA(cudaEventCreateWithFlags(&d.pipe_done[i], cudaEventDisableTiming));
+        }
+        TT_CUDA(cudaEventCreateWithFlags(&d.pipe_start, cudaEventDisableTiming));
+    }
     char *dr = static_cast<char *>(d.d_stage);
     char *dh = dr + rb;
-    TT_CUDA(cudaMemcpyAsync(dr, h_rays, rb, cudaMemcpyHostToDevice, s));
-    tt_status st = launch_trace(d, dr, n, dh, closest != 0, false, s);
-    if (st != TT_OK) return st;
-    TT_CUDA(cudaMemcpyAsync(h_hits, dh, hb, cudaMemcpyDeviceToHost, s));
+    // Chunks rotate over three streams so that the copy in of chunk i+1, the trace of chunk i and
+    // the copy out of chunk i-1 overlap; everything is ordered after prior work on `stream`.
+    const int64_t chunk = n < (int64_t)(1 << 21) ? n : (int64_t)(1 << 20);
+    TT_CUDA(cudaEventRecord(d.pipe_start, s));
+    tt_status st = TT_OK;
+    int used = 0;
+    for (int64_t off = 0, k = 0; off < n && st == TT_OK; off += chunk, k++) {
+        const int64_t m = (n - off) < chunk ? (n - off) : chunk;
+        const int p = (int)(k % 3);
+        cudaStream_t ps = d.pipe[p];
+        if (k < 3) {
+            TT_CUDA(cudaStreamWaitEvent(ps, d.pipe_start, 0));
+            used = (int)k + 1;
+        }
+        TT_CUDA(cudaMemcpyAsync(dr + 32 * off, reinterpret_cast<const char *>(h_rays) + 32 * off, 32ull * m,
+                                cudaMemcpyHostToDevice, ps));
+        st = launch_trace(d, dr + 32 * off, m, dh + 8 * off, closest != 0, false, ps, kScratchPipe + p);
+        if (st == TT_OK)
+            TT_CUDA(cudaMemcpyAsync(reinterpret_cast<char *>(h_hits) + 8 * off, dh + 8 * off, 8ull * m,
+                                    cudaMemcpyDeviceToHost, ps));
+    }
+    for (int p = 0; p < used; p++) {
+        TT_CUDA(cudaEventRecord(d.pipe_done[p], d.pipe[p]));
+        TT_CUDA(cudaStreamWaitEvent(s, d.pipe_done[p], 0));
+    }
     TT_CUDA(cudaStreamSynchronize(s));
+    if (st != TT_OK) return st;
     return read_error_word(d, s);
 }
 

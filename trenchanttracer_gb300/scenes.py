@@ -312,6 +312,55 @@ def multi_material(count: int = 400, subdiv: int = 5, seed: int = 3, world: floa
     return m
 
 
+def sky_env(width: int = 2048, height: int = 1024, sun_dir=(0.3, 0.8, 0.52), sun_radiance: float = 5e4,
+            sun_diameter_deg: float = 0.5, tint=(0.55, 0.75, 1.0)) -> np.ndarray:
+    """Equirectangular sky (h, w, 3) float32 in the reference's mapping (u = atan2(x, z) / 2pi,
+    v = acos(y) / pi, row 0 = up): radiance from 0.2 at the horizon to 1.0 at the zenith (times
+    a tint), 0.2 below the horizon, plus a sun disc of the given angular diameter and radiance."""
+    v = (np.arange(height, dtype=np.float64) + 0.5) / height
+    u = (np.arange(width, dtype=np.float64) + 0.5) / width
+    theta = v * np.pi
+    phi = u * 2.0 * np.pi
+    st, ct = np.sin(theta)[:, None], np.cos(theta)[:, None]
+    dx, dy, dz = st * np.sin(phi)[None, :], np.broadcast_to(ct, (height, width)), st * np.cos(phi)[None, :]
+    g = 0.2 + 0.8 * np.clip(dy, 0.0, 1.0)
+    img = np.stack([g * tint[0], g * tint[1], g * tint[2]], axis=-1)
+    s = np.asarray(sun_dir, np.float64)
+    s = s / np.linalg.norm(s)
+    cosang = dx * s[0] + dy * s[1] + dz * s[2]
+    disc = cosang >= np.cos(np.radians(sun_diameter_deg / 2.0))
+    if not disc.any():  # coarser maps than the disc: light the nearest texel
+        disc = cosang == cosang.max()
+    img[disc] = sun_radiance
+    return img.astype(np.float32)
+
+
+def material_showcase(subdiv: int = 3) -> tuple["Mesh", list[dict]]:
+    """Spheres of every material kind over a ground quad, for the renderer tests: Diff, Metal,
+    Spec, Refr, Coat (the reference's kinds), GGX conductor and dielectric. Also returns the
+    analytic objects (a Plane backdrop and a Sphere) the JSON scenes can carry."""
+    mats = [{"name": "ground", "type": "Diff", "diffuseColor": [0.6, 0.6, 0.6]},
+            {"name": "diff", "type": "Diff", "diffuseColor": [0.8, 0.3, 0.2]},
+            {"name": "metal", "type": "Metal", "color": [0.9, 0.8, 0.5]},
+            {"name": "spec", "type": "Spec", "color": [0.95, 0.95, 0.95]},
+            {"name": "refr", "type": "Refr"},
+            {"name": "coat", "type": "Coat", "diffuseColor": [0.2, 0.4, 0.8], "specularColor": [0.9, 0.9, 0.9]},
+            {"name": "ggx", "type": "GGX", "F0": [0.95, 0.64, 0.54], "roughness": 0.3},
+            {"name": "glass", "type": "Dielectric", "ior": 1.5},
+            {"name": "lamp", "type": "Diff", "diffuseColor": [0.0, 0.0, 0.0], "emission": [6.0, 6.0, 5.0]}]
+    parts = [(*quad([-4.0, 0.0, -4.0], [-4.0, 0.0, 4.0], [4.0, 0.0, -4.0]), 0)]
+    for k in range(1, 8):
+        x = -2.4 + 0.8 * (k - 1)
+        verts, tris, normals = displaced_icosphere(subdiv, 0.35, [x, 0.36, 0.0], 100 + k, 0.0)
+        parts.append((verts, tris, normals, k))
+    m = _concat(parts)
+    m.materials = mats
+    geoms = [{"type": "Plane", "p0": [-4.0, 0.0, -1.5], "p1": [4.0, 0.0, -1.5], "p2": [-4.0, 3.0, -1.5],
+              "material": 0},
+             {"type": "Sphere", "radius": 0.25, "position": [0.0, 1.6, 0.5], "material": 8}]
+    return m, geoms
+
+
 # ---- rays ----------------------------------------------------------------------------------
 def pinhole_rays(width: int, height: int, eye, target, tan_half_fov: float,
                  tmin: float = 0.01, tmax: float = 1e20) -> np.ndarray:
