@@ -265,6 +265,35 @@ tt_status tt_render_compat(tt_renderer *renderer, const tt_camera_meta *cam, con
 /* Synchronises `stream` and reports traversal errors of the renderer's launches. */
 tt_status tt_renderer_check(tt_renderer *renderer, void *stream);
 
+/* Parameters of the native path tracer (no counterpart in the reference, which always runs 10
+ * bounces with curand streams). */
+typedef struct tt_render_params {
+    int32_t spp;           /* samples per pixel of this call */
+    int32_t sample_offset; /* global index of the first sample (progressive rendering) */
+    int32_t max_depth;     /* bounces at most (the reference's fixed value is 10) */
+    int32_t rr_depth;      /* Russian roulette from this bounce on (>= max_depth: off) */
+    uint32_t seed;         /* PCG32 state seed; the stream of a path is its global index */
+    float env_scale;       /* environment radiance factor (the reference uses 2) */
+    float ray_eps;         /* new-ray origin offset along the normal, x max(1, |p|_inf) */
+    int32_t flags;         /* TT_RENDER_* bits */
+} tt_render_params;
+#define TT_RENDER_ACCUM_F64 1          /* d_accum holds doubles */
+#define TT_RENDER_NO_ENV_SAMPLING 2    /* BSDF sampling only (no environment light sampling / MIS) */
+/* Fills `out` with the defaults: spp 1, offset 0, max_depth 8, rr_depth 4, seed 1, env_scale 1,
+ * ray_eps 1e-4, flags 0. */
+tt_status tt_render_params_default(tt_render_params *out);
+/* Native wavefront path tracer (Lambert, GGX conductor, dielectric, environment light sampling
+ * by a 2D CDF with MIS, Russian roulette, PCG32 streams; the reference's own material kinds are
+ * sampled as documented in the design doc). Adds the sum of spp samples of every pixel to d_accum
+ * (width*height*3 floats, or doubles with TT_RENDER_ACCUM_F64; row 0 = the image's top row).
+ * Launch only; deterministic for given inputs. */
+tt_status tt_render_native(tt_renderer *renderer, const tt_camera_meta *cam, const tt_render_params *params,
+                           void *d_accum, void *stream);
+/* The environment's sampling tables built by tt_renderer_create: marginal CDF (env_h + 1 floats)
+ * and conditional CDFs (env_h * (env_w + 1) floats), copied to host buffers (either may be
+ * NULL). */
+tt_status tt_renderer_env_tables(const tt_renderer *renderer, float *marginal, float *conditional);
+
 #define TT_NOALLOC_MAX_RAYS (1 << 18)
 tt_status tt_trace_host_noalloc(const void *d_nodes, const void *d_vertices, const int32_t *d_tri_indices,
                                 const tt_ray *h_rays, int64_t n, tt_hit *h_hits, int32_t closest,

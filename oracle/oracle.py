@@ -12,7 +12,8 @@ from pathlib import Path
 import numpy as np
 
 HERE = Path(__file__).resolve().parent
-SRC = HERE / "tt_oracle.c"
+SRC = HERE / "tt_oracle_pt.c"  # includes tt_oracle.c
+SRCS = [HERE / "tt_oracle.c", SRC]
 LIB = HERE / "_build" / "liboracle.so"
 
 SLAB_FMA, CROSS_A, CROSS_B, DOT_A, DOT_B, INTERP_A, INTERP_B = 1, 2, 4, 8, 16, 32, 64
@@ -28,7 +29,7 @@ _h = None
 
 
 def build(force: bool = False) -> Path:
-    if LIB.exists() and not force and LIB.stat().st_mtime >= SRC.stat().st_mtime:
+    if LIB.exists() and not force and LIB.stat().st_mtime >= max(s.stat().st_mtime for s in SRCS):
         return LIB
     LIB.parent.mkdir(exist_ok=True)
     tmp = LIB.with_suffix(".so.tmp")
@@ -52,8 +53,50 @@ def _load():
         h.oracle_max_threads.restype = C.c_int
         h.oracle_wang_hash.restype = C.c_uint32
         h.oracle_wang_hash.argtypes = [C.c_uint32]
+        h.oracle_env_tables.restype = None
+        h.oracle_env_tables.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+        h.oracle_render_native.restype = C.c_int
+        h.oracle_render_native.argtypes = [C.c_void_p] * 5 + [C.c_void_p, C.c_int, C.c_void_p, C.c_int,
+                                                              C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                                              C.c_void_p, C.c_void_p, C.c_float, C.c_float,
+                                                              C.c_void_p, C.c_int]
         _h = h
     return _h
+
+
+def env_tables(env: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    """Marginal (h+1) and conditional (h, w+1) CDFs of an (h, w, 3) environment map."""
+    env = np.ascontiguousarray(env, dtype=np.float32)
+    h, w = env.shape[:2]
+    marg = np.empty(h + 1, np.float32)
+    cond = np.empty((h, w + 1), np.float32)
+    _load().oracle_env_tables(env.ctypes.data, w, h, marg.ctypes.data, cond.ctypes.data)
+    return marg, cond
+
+
+def render_native(bvh_arrays: dict, materials, geometries, env: np.ndarray | None, cam, params, tanx: float,
+                  tany: float, threads: int = 0) -> np.ndarray:
+    """The native path tracer restated on the CPU: returns the accumulation buffer (W*H*3 floats)
+    of params.spp samples per pixel. materials / geometries: ctypes arrays of tt_material /
+    tt_geometry; cam / params: tt_camera_meta / tt_render_params."""
+    a = [np.ascontiguousarray(bvh_arrays[k]) for k in ["nodes", "vertices", "normals", "tri_indices", "mat_indices"]]
+    if env is None:
+        env_a, ew, eh = np.zeros(3, np.float32), 0, 0
+        marg, cond = np.zeros(1, np.float32), np.zeros(1, np.float32)
+    else:
+        env_a = np.ascontiguousarray(env, dtype=np.float32)
+        eh, ew = env_a.shape[:2]
+        marg, cond = env_tables(env_a)
+    accum = np.zeros(3 * cam.width * cam.height, np.float32)
+    mats = (C.c_byte * max(1, C.sizeof(materials)))()
+    C.memmove(mats, materials, C.sizeof(materials))
+    geos = (C.c_byte * max(1, C.sizeof(geometries)))()
+    if C.sizeof(geometries):
+        C.memmove(geos, geometries, C.sizeof(geometries))
+    _load().oracle_render_native(*(x.ctypes.data for x in a), mats, len(materials), geos, len(geometries),
+                                 env_a.ctypes.data, ew, eh, marg.ctypes.data, cond.ctypes.data, C.byref(cam),
+                                 C.byref(params), tanx, tany, accum.ctypes.data, threads)
+    return accum
 
 
 def intersect(bvh_arrays: dict, rays: np.ndarray, closest: bool, arith: int = DEVICE, counters: bool = False,

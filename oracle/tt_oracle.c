@@ -100,6 +100,10 @@ typedef struct {
     const uint32_t *mat_idx;
 } Bvh;
 
+/* Raw hit of the last trace_one call on this thread: float4 slot (-1 = miss) and barycentrics. */
+static _Thread_local int g_hit_addr;
+static _Thread_local float g_hit_u, g_hit_v;
+
 /* Returns 0, or -1 when the stack would overflow. */
 static int trace_one(const Bvh *b, const float *r, int closest, int arith, int32_t *o_id, float *o_t,
                      int32_t *o_mat, float *o_n, uint32_t *cnt) {
@@ -198,6 +202,9 @@ static int trace_one(const Bvh *b, const float *r, int closest, int arith, int32
         }
     }
     *o_t = dist;
+    g_hit_addr = hit_addr;
+    g_hit_u = hu;
+    g_hit_v = hv;
     if (hit_addr >= 0) {
         *o_id = b->tri_idx[hit_addr];
         if (o_mat) *o_mat = (int32_t)b->mat_idx[hit_addr];

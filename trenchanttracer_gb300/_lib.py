@@ -53,6 +53,15 @@ class Geometry(C.Structure):
                 ("p0", C.c_float * 3), ("p1", C.c_float * 3), ("p2", C.c_float * 3), ("pad2", C.c_float * 3)]
 
 
+class RenderParams(C.Structure):
+    """tt_render_params (include/tt.h)."""
+    _fields_ = [("spp", C.c_int32), ("sample_offset", C.c_int32), ("max_depth", C.c_int32), ("rr_depth", C.c_int32),
+                ("seed", C.c_uint32), ("env_scale", C.c_float), ("ray_eps", C.c_float), ("flags", C.c_int32)]
+
+
+RENDER_ACCUM_F64 = 1
+RENDER_NO_ENV_SAMPLING = 2
+
 P = C.c_void_p
 I32 = C.c_int32
 I64 = C.c_int64
@@ -94,6 +103,9 @@ SIGNATURES = {
     "tt_renderer_free": (None, [P]),
     "tt_render_compat": (I32, [P, C.POINTER(CameraMeta), C.POINTER(RenderMeta), P, P]),
     "tt_renderer_check": (I32, [P, P]),
+    "tt_render_params_default": (I32, [C.POINTER(RenderParams)]),
+    "tt_render_native": (I32, [P, C.POINTER(CameraMeta), C.POINTER(RenderParams), P, P]),
+    "tt_renderer_env_tables": (I32, [P, P, P]),
 }
 
 _lib: C.CDLL | None = None

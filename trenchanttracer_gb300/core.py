@@ -282,6 +282,18 @@ class Renderer:
         check(lib().tt_render_compat(self._h, C.byref(cam), C.byref(meta), C.c_void_p(accum.data_ptr()),
                                      C.c_void_p(stream)))
 
+    def render_native(self, cam: _lib.CameraMeta, params: _lib.RenderParams, accum, stream: int = 0) -> None:
+        """Native wavefront path tracer: adds spp samples per pixel to accum (CUDA tensor W*H*3,
+        float32, or float64 with the RENDER_ACCUM_F64 flag; row 0 = top)."""
+        check(lib().tt_render_native(self._h, C.byref(cam), C.byref(params), C.c_void_p(accum.data_ptr()),
+                                     C.c_void_p(stream)))
+
+    def env_tables(self, env_w: int, env_h: int) -> tuple[np.ndarray, np.ndarray]:
+        marg = np.empty(env_h + 1, np.float32)
+        cond = np.empty((env_h, env_w + 1), np.float32)
+        check(lib().tt_renderer_env_tables(self._h, _ptr(marg), _ptr(cond)))
+        return marg, cond
+
     def check(self, stream: int = 0) -> None:
         check(lib().tt_renderer_check(self._h, C.c_void_p(stream)))
 
@@ -289,6 +301,15 @@ class Renderer:
         if getattr(self, "_h", None):
             lib().tt_renderer_free(self._h)
             self._h = None
+
+
+def render_params(**kw) -> _lib.RenderParams:
+    """tt_render_params with the library defaults, overridden by keyword."""
+    p = _lib.RenderParams()
+    check(lib().tt_render_params_default(C.byref(p)))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
 
 
 def hits_to_numpy(hits: np.ndarray) -> tuple[np.ndarray, np.ndarray]:

@@ -394,18 +394,7 @@ __global__ void __launch_bounds__(256) render_compat_kernel(CompatArgs a) {
 
 }  // namespace tt
 
-// ---- renderer handle ------------------------------------------------------------------------------
-struct tt_renderer {
-    tt::BvhView bvh{};
-    tt::MaterialRec *materials = nullptr;
-    int num_materials = 0;
-    tt::GeomRec *geoms = nullptr;
-    int num_geoms = 0;
-    float4 *env = nullptr;
-    int env_w = 0, env_h = 0;
-    unsigned int *err = nullptr;
-};
-
+// ---- renderer handle (struct tt_renderer: tt_device.h) ---------------------------------------------
 using namespace tt;
 
 static tt_status cuda_fail_r(cudaError_t e, const char *what) {
@@ -419,6 +408,7 @@ static tt_status cuda_fail_r(cudaError_t e, const char *what) {
 
 static void renderer_release(tt_renderer *r) {
     if (!r) return;
+    native_release(r);
     cudaFree(r->materials);
     cudaFree(r->geoms);
     cudaFree(r->env);
@@ -455,6 +445,12 @@ tt_status tt_renderer_create(const tt_dbvh *bvh, const tt_scene *scene, tt_rende
     r->num_geoms = (int)sc.geoms.size();
     r->env_w = sc.env_w;
     r->env_h = sc.env_h;
+    tt_status st = native_setup(r);
+    if (st != TT_OK) {
+        renderer_release(r);
+        delete r;
+        return st;
+    }
     *out = r;
     return TT_OK;
 }
