@@ -284,15 +284,63 @@ typedef struct tt_render_params {
 tt_status tt_render_params_default(tt_render_params *out);
 /* Native wavefront path tracer (Lambert, GGX conductor, dielectric, environment light sampling
  * by a 2D CDF with MIS, Russian roulette, PCG32 streams; the reference's own material kinds are
- * sampled as documented in the design doc). Adds the sum of spp samples of every pixel to d_accum
- * (width*height*3 floats, or doubles with TT_RENDER_ACCUM_F64; row 0 = the image's top row).
- * Launch only; deterministic for given inputs. */
+ * mapped as the header of tt_render_native.cu lists). Adds the sum of spp samples of every pixel
+ * to d_accum (width*height*3 floats, or doubles with TT_RENDER_ACCUM_F64; row 0 = the image's top
+ * row). The pixel sums are added in sample order, so the result is the same for every launch
+ * shape. Launch only; deterministic for given inputs. */
 tt_status tt_render_native(tt_renderer *renderer, const tt_camera_meta *cam, const tt_render_params *params,
                            void *d_accum, void *stream);
 /* The environment's sampling tables built by tt_renderer_create: marginal CDF (env_h + 1 floats)
  * and conditional CDFs (env_h * (env_w + 1) floats), copied to host buffers (either may be
  * NULL). */
 tt_status tt_renderer_env_tables(const tt_renderer *renderer, float *marginal, float *conditional);
+
+/* Launch shape of the native path tracer's kernels (no counterpart in the reference). */
+typedef struct tt_launch_shape {
+    int32_t block;        /* threads per block: 64, 128 or 256 */
+    int32_t stack_shared; /* traversal stack entries per thread kept in shared memory: 0, 8 or 16 */
+    int32_t wave_paths;   /* paths in flight per wave (queue capacity): 1 .. 2^24 */
+    float ms;             /* tt_batch_autotune: the trial's time; otherwise 0 */
+} tt_launch_shape;
+/* Default: 128 threads, 16 shared entries, 2^22 paths. Results do not depend on the shape. */
+tt_status tt_renderer_set_launch(tt_renderer *renderer, const tt_launch_shape *shape);
+tt_status tt_renderer_get_launch(const tt_renderer *renderer, tt_launch_shape *shape);
+/* Counters of the native path tracer since the last reset: out[0] extension rays (closest hit),
+ * out[1] shadow rays (any hit), out[2] paths. Synchronous. */
+tt_status tt_renderer_stats(tt_renderer *renderer, uint64_t *out, int32_t reset);
+
+/* Batched rendering (no counterpart in the reference): many views of any size and sample count
+ * rendered by one sequence of persistent wavefront kernels over a shared path index space, which
+ * tt_batch_render captures once as a CUDA graph and replays. Every view's image is bit-identical
+ * to tt_render_native of that view with the batch's parameters and the view's spp, sample
+ * offset and seed. */
+typedef struct tt_view {
+    tt_camera_meta cam;    /* image size and pinhole (aperture and focal are not used) */
+    int32_t spp;
+    int32_t sample_offset;
+    uint32_t seed;
+    int32_t reserved;
+} tt_view;
+typedef struct tt_batch tt_batch;
+/* params: max_depth, rr_depth, env_scale, ray_eps and flags apply to every view; its spp,
+ * sample_offset and seed are ignored. The batch keeps a pointer to the renderer. */
+tt_status tt_batch_create(tt_renderer *renderer, const tt_view *views, int32_t n, const tt_render_params *params,
+                          tt_batch **out);
+/* Paths of the whole batch, and the length of its accumulation buffer: view k's width*height*3
+ * block follows view k-1's (floats, or doubles with TT_RENDER_ACCUM_F64). */
+tt_status tt_batch_info(const tt_batch *batch, int64_t *total_paths, int64_t *accum_elems);
+/* Adds every view's samples to d_accum. use_graph = 1: the first call (and any call after the
+ * buffer, the launch shape or the renderer's path state changed) captures the kernel sequence as
+ * a CUDA graph; later calls replay it. use_graph = 0: plain launches. Launch only. */
+tt_status tt_batch_render(tt_batch *batch, void *d_accum, int32_t use_graph, void *stream);
+/* Nodes of the captured graph (0 before the first graph render). */
+tt_status tt_batch_graph_kernels(const tt_batch *batch, int32_t *kernels);
+/* Times the first sample_paths paths of the batch (0: 2^23) under every launch shape (block x
+ * stack_shared x wave_paths in {2^20, 2^21, 2^22}), keeps the fastest as the renderer's shape and
+ * writes up to max_results trials to results. Synchronous; touches no accumulation buffer. */
+tt_status tt_batch_autotune(tt_batch *batch, int64_t sample_paths, void *stream, tt_launch_shape *results,
+                            int32_t max_results, int32_t *n_results);
+tt_status tt_batch_free(tt_batch *batch);
 
 #define TT_NOALLOC_MAX_RAYS (1 << 18)
 tt_status tt_trace_host_noalloc(const void *d_nodes, const void *d_vertices, const int32_t *d_tri_indices,

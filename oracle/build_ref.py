@@ -160,7 +160,9 @@ def build(ref: Path = DEFAULT_REF, quiet: bool = True) -> bool:
             out, _ = p.communicate()
             if p.returncode != 0:
                 raise SystemExit(f"build_ref: {s} failed:\n{out[-4000:]}")
-        _run(["g++", "-shared", "-fopenmp", "-o", str(lib), *objs])
+        # -Bsymbolic: the reference's CUDA runtime calls bind to the host stub linked in here even
+        # when the process already holds the real libcudart (torch loads it into the global scope)
+        _run(["g++", "-shared", "-fopenmp", "-Wl,-Bsymbolic", "-o", str(lib), *objs])
 
         cubin = OUT / "ref_intersect.cubin"
         _run([str(cuda / "bin" / "nvcc"), "-cubin", "-gencode=arch=compute_103a,code=sm_103a", "-w",

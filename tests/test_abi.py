@@ -47,3 +47,30 @@ def test_null_arguments_are_rejected():
     assert lib.tt_bvh_build(None, 1e-5, 1, 8, 0, None) == 1
     assert lib.tt_trace(None, None, 0, None, 1, None) == 1
     assert lib.tt_bvh_upload(None, None) == 1
+
+
+STRUCTS = {"tt_camera_meta": _lib.CameraMeta, "tt_render_meta": _lib.RenderMeta, "tt_material": _lib.Material,
+           "tt_geometry": _lib.Geometry, "tt_render_params": _lib.RenderParams, "tt_bvh_header": _lib.BvhHeader,
+           "tt_launch_shape": _lib.LaunchShape, "tt_view": _lib.View}
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """Every struct of include/tt.h has the same size and field offsets in C (gcc) and in the
+    Python binding."""
+    lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{ROOT / "include" / "tt.h"}"', "int main(void) {"]
+    for cname, py in STRUCTS.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for f, _ in py._fields_:
+            lines.append(f'printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    import subprocess
+    subprocess.run(["gcc", "-std=c11", str(src), "-o", str(exe)], check=True)
+    got = dict((" ".join(l.split()[:2]), int(l.split()[2])) for l in
+               subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.splitlines())
+    for cname, py in STRUCTS.items():
+        assert got[f"{cname} size"] == C.sizeof(py), cname
+        for f, _ in py._fields_:
+            assert got[f"{cname} {f}"] == getattr(py, f).offset, (cname, f)

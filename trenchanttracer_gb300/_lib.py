@@ -62,6 +62,20 @@ class RenderParams(C.Structure):
 RENDER_ACCUM_F64 = 1
 RENDER_NO_ENV_SAMPLING = 2
 
+
+class LaunchShape(C.Structure):
+    """tt_launch_shape (include/tt.h)."""
+    _fields_ = [("block", C.c_int32), ("stack_shared", C.c_int32), ("wave_paths", C.c_int32), ("ms", C.c_float)]
+
+    def as_tuple(self) -> tuple:
+        return (self.block, self.stack_shared, self.wave_paths)
+
+
+class View(C.Structure):
+    """tt_view (include/tt.h): one view of a batched render."""
+    _fields_ = [("cam", CameraMeta), ("spp", C.c_int32), ("sample_offset", C.c_int32), ("seed", C.c_uint32),
+                ("reserved", C.c_int32)]
+
 P = C.c_void_p
 I32 = C.c_int32
 I64 = C.c_int64
@@ -106,6 +120,15 @@ SIGNATURES = {
     "tt_render_params_default": (I32, [C.POINTER(RenderParams)]),
     "tt_render_native": (I32, [P, C.POINTER(CameraMeta), C.POINTER(RenderParams), P, P]),
     "tt_renderer_env_tables": (I32, [P, P, P]),
+    "tt_renderer_set_launch": (I32, [P, C.POINTER(LaunchShape)]),
+    "tt_renderer_get_launch": (I32, [P, C.POINTER(LaunchShape)]),
+    "tt_renderer_stats": (I32, [P, P, I32]),
+    "tt_batch_create": (I32, [P, P, I32, C.POINTER(RenderParams), C.POINTER(P)]),
+    "tt_batch_info": (I32, [P, C.POINTER(I64), C.POINTER(I64)]),
+    "tt_batch_render": (I32, [P, P, I32, P]),
+    "tt_batch_graph_kernels": (I32, [P, C.POINTER(I32)]),
+    "tt_batch_autotune": (I32, [P, I64, P, P, I32, C.POINTER(I32)]),
+    "tt_batch_free": (I32, [P]),
 }
 
 _lib: C.CDLL | None = None

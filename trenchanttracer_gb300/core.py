@@ -288,6 +288,23 @@ class Renderer:
         check(lib().tt_render_native(self._h, C.byref(cam), C.byref(params), C.c_void_p(accum.data_ptr()),
                                      C.c_void_p(stream)))
 
+    def set_launch(self, block: int, stack_shared: int, wave_paths: int) -> None:
+        """Launch shape of the native kernels (include/tt.h, tt_launch_shape)."""
+        shape = _lib.LaunchShape(int(block), int(stack_shared), int(wave_paths), 0.0)
+        check(lib().tt_renderer_set_launch(self._h, C.byref(shape)))
+
+    @property
+    def launch(self) -> tuple:
+        shape = _lib.LaunchShape()
+        check(lib().tt_renderer_get_launch(self._h, C.byref(shape)))
+        return shape.as_tuple()
+
+    def stats(self, reset: bool = False) -> dict:
+        """Rays and paths the native path tracer traced since the last reset (synchronous)."""
+        out = np.zeros(3, np.uint64)
+        check(lib().tt_renderer_stats(self._h, _ptr(out), int(bool(reset))))
+        return {"extension_rays": int(out[0]), "shadow_rays": int(out[1]), "paths": int(out[2])}
+
     def env_tables(self, env_w: int, env_h: int) -> tuple[np.ndarray, np.ndarray]:
         marg = np.empty(env_h + 1, np.float32)
         cond = np.empty((env_h, env_w + 1), np.float32)
@@ -300,6 +317,57 @@ class Renderer:
     def __del__(self):
         if getattr(self, "_h", None):
             lib().tt_renderer_free(self._h)
+            self._h = None
+
+
+class Batch:
+    """Many views of any size and sample count in one graph-captured wavefront render
+    (include/tt.h, tt_batch_*). views: sequence of (CameraMeta, spp, sample_offset, seed)."""
+
+    def __init__(self, renderer: Renderer, views, params: _lib.RenderParams):
+        arr = (_lib.View * len(views))()
+        for k, (cam, spp, offset, seed) in enumerate(views):
+            arr[k].cam = cam
+            arr[k].spp, arr[k].sample_offset, arr[k].seed = int(spp), int(offset), int(seed)
+        h = C.c_void_p()
+        check(lib().tt_batch_create(renderer._h, arr, len(views), C.byref(params), C.byref(h)))
+        self._h = h
+        self._keep = renderer
+        self.sizes = [(int(v.cam.width), int(v.cam.height)) for v in arr]
+        tp, ae = C.c_int64(), C.c_int64()
+        check(lib().tt_batch_info(self._h, C.byref(tp), C.byref(ae)))
+        self.total_paths, self.accum_elems = tp.value, ae.value
+
+    def render(self, accum, use_graph: bool = True, stream: int = 0) -> None:
+        """Adds every view's samples to accum (CUDA tensor of accum_elems floats / doubles)."""
+        assert accum.numel() >= self.accum_elems
+        check(lib().tt_batch_render(self._h, C.c_void_p(accum.data_ptr()), int(bool(use_graph)), C.c_void_p(stream)))
+
+    @property
+    def graph_kernels(self) -> int:
+        n = C.c_int32()
+        check(lib().tt_batch_graph_kernels(self._h, C.byref(n)))
+        return n.value
+
+    def autotune(self, sample_paths: int = 0, stream: int = 0) -> list:
+        """Times every launch shape on the batch's first paths, keeps the fastest; returns
+        [(block, stack_shared, wave_paths, ms)]."""
+        res = (_lib.LaunchShape * 64)()
+        n = C.c_int32()
+        check(lib().tt_batch_autotune(self._h, int(sample_paths), C.c_void_p(stream), res, 64, C.byref(n)))
+        return [(r.block, r.stack_shared, r.wave_paths, r.ms) for r in res[:min(n.value, 64)]]
+
+    def split(self, accum) -> list:
+        """The per-view (H, W, 3) images of an accumulation buffer (torch tensor or numpy array)."""
+        out, off = [], 0
+        for w, h in self.sizes:
+            out.append(accum[off:off + 3 * w * h].reshape(h, w, 3))
+            off += 3 * w * h
+        return out
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().tt_batch_free(self._h)
             self._h = None
 
 

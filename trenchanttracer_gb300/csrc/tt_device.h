@@ -23,15 +23,27 @@ struct tt_renderer {
     int num_geoms = 0;
     float4 *env = nullptr;  // env_w * env_h radiance texels (w = 0: no environment)
     int env_w = 0, env_h = 0;
-    unsigned int *err = nullptr;
+    unsigned int *err = nullptr;  // 256 bytes: error word at 0, native ray counters at byte 64
     // native path tracer
     float *env_marg = nullptr;  // env_h + 1
     float *env_cond = nullptr;  // env_h * (env_w + 1)
     void *paths = nullptr;      // path state, queues and shadow rays for path_capacity paths
     size_t paths_bytes = 0;
     int path_capacity = 0;
+    unsigned long long paths_gen = 0;  // bumped whenever `paths` is reallocated
     int num_sms = 0;
+    // launch shape of the native kernels (tt_renderer_set_launch, tt_batch_autotune)
+    int launch_block = 128, launch_stack = 16, launch_wave = 1 << 22;
+    int occ_trace[3][3] = {};  // resident blocks per SM by (block shape, stack shape); 0 = unknown
+    int occ_shade[3] = {};
 };
+
+namespace tt {
+// [0] extension rays, [1] shadow rays, [2] paths traced by the native path tracer
+inline unsigned long long *renderer_stats(tt_renderer *r) {
+    return reinterpret_cast<unsigned long long *>(reinterpret_cast<char *>(r->err) + 64);
+}
+}  // namespace tt
 
 namespace tt {
 // Builds the environment's sampling tables (called by tt_renderer_create) / frees native state.

@@ -1,0 +1,155 @@
+// Device-side structures of the native wavefront path tracer, shared by the shading
+// (tt_render_native.cu) and the traversal (tt_render_extend.cu) translation units.
+//
+// Path index space. A render covers one or more camera views; view k owns the contiguous range
+// [first_k, first_k + npix_k * spp_k) of a batch-global path index space, sample-major inside
+// the view (index = sample * npix + pixel). A wave is a contiguous range of that space, so it can
+// span several views and partial samples; every kernel maps an index back to its view with a
+// binary search over the view table. A path's PCG32 stream is its view-local index
+// (sample_offset * npix + index - first), so a view renders the same bits whether it is drawn
+// alone or inside any batch.
+//
+// Queues. Queue slot q of bounce parity c holds the path index queue[c][q] and that path's next
+// ray ray[c][2q], ray[c][2q + 1] = (o.xyz, d.x), (d.y, d.z, tmin, tmax): the traversal kernels
+// read rays contiguously, in queue order. Hit records are indexed by queue slot.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "tt_device.h"
+#include "tt_ptmath.cuh"
+
+namespace tt {
+
+struct EnvView {
+    const float4 *tex;  // w*h radiance
+    const float *marg;  // h+1 marginal CDF over rows
+    const float *cond;  // h*(w+1) conditional CDFs per row
+    int w, h;
+    float scale;
+};
+
+// One camera view of a render.
+struct ViewRec {
+    long long first;      // batch-global index of the view's first path
+    long long paths;      // npix * spp
+    long long accum;      // element offset of the view's npix * 3 accumulation block
+    long long stream0;    // sample_offset * npix: PCG32 stream index of the view's first path
+    uint64_t seed_state;  // PCG32 initial state of the view's seed
+    int width, height, npix, pad;
+    float pos[3], view[3], up[3];
+    float tanx, tany, pad2;
+};
+
+struct PathSoA {
+    float *beta, *L;     // 3 per path
+    uint64_t *rng;       // PCG32 state
+    uint64_t *rng_inc;   // PCG32 stream increment
+    float *last_pdf;
+    int *depth, *flags;
+    int *queue[2];       // path index per queue slot, by bounce parity
+    float4 *ray[2];      // 2 float4 per queue slot, by bounce parity
+    float *hit_t, *hit_u, *hit_v;  // per slot of the queue being shaded
+    int *hit_prim;       // triangle slot >= 0, -(geometry+2) for analytic objects, -1 = miss
+    int *counts;         // [0] [1] queue lengths by parity, [2] shadow queue length,
+                         // [3] extend work counter, [4] shadow work counter
+    int *shadow_path;
+    float4 *shadow_ray;  // 2 float4 per shadow ray
+    float *shadow_val;   // 3 per shadow ray
+};
+
+struct NativeArgs {
+    BvhView bvh;
+    const MaterialRec *materials;
+    int num_materials;
+    const GeomRec *geoms;
+    int num_geoms;
+    EnvView env;
+    PathSoA ps;
+    tt_render_params p;
+    const ViewRec *views;  // device view table (nullptr: the single view `view0`)
+    int n_views;
+    ViewRec view0;
+    long long wave_first;  // batch-global index of the wave's first path
+    int wave_paths;
+    unsigned int *err;
+    unsigned long long *stats;  // [0] extension rays, [1] shadow rays, [2] paths
+};
+
+__device__ __forceinline__ int find_view(const NativeArgs &a, long long g) {
+    if (!a.views) return 0;
+    int lo = 0, hi = a.n_views - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(&a.views[mid].first) <= g) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ ViewRec view_of(const NativeArgs &a, int v) { return a.views ? a.views[v] : a.view0; }
+
+// Closest hit among the analytic objects (brute force over all of them, as the reference does).
+__device__ __forceinline__ void analytic_hit(const NativeArgs &a, const V3 &o, const V3 &d, float tmin,
+                                             float &t, int &prim, float &hu, float &hv) {
+    using namespace pt;
+    for (int i = 0; i < a.num_geoms; i++) {
+        const GeomRec g = a.geoms[i];
+        if (g.kind == GEOM_PLANE) {
+            const V3 p0(g.p0[0], g.p0[1], g.p0[2]);
+            const V3 e1 = sub(V3(g.p1[0], g.p1[1], g.p1[2]), p0), e2 = sub(V3(g.p2[0], g.p2[1], g.p2[2]), p0);
+            const V3 P = cross(d, e2);
+            const float det = dot(e1, P);
+            if (det > -1e-12f && det < 1e-12f) continue;
+            const float inv = PT_DIV(1.0f, det);
+            const V3 T = sub(o, p0);
+            const float u = PT_MUL(dot(T, P), inv);
+            if (u < 0.f || u > 1.f) continue;
+            const V3 Q = cross(T, e1);
+            const float v = PT_MUL(dot(d, Q), inv);
+            if (v < 0.f || v > 1.f) continue;
+            const float th = PT_MUL(dot(e2, Q), inv);
+            if (th > tmin && th < t) {
+                t = th;
+                prim = -(i + 2);
+                hu = u;
+                hv = v;
+            }
+        } else if (g.kind == GEOM_SPHERE) {
+            const V3 c(g.p0[0], g.p0[1], g.p0[2]);
+            const V3 oc = sub(c, o);
+            const float bq = dot(oc, d);
+            const float disc = PT_FMA(g.radius, g.radius, PT_FMA(bq, bq, -dot(oc, oc)));
+            if (disc < 0.0f) continue;
+            const float sq = PT_SQRT(disc);
+            float th = PT_SUB(bq, sq);
+            if (!(th > tmin)) th = PT_ADD(bq, sq);
+            if (th > tmin && th < t) {
+                t = th;
+                prim = -(i + 2);
+                hu = 0.f;
+                hv = 0.f;
+            }
+        }
+    }
+}
+
+// Kernels of one traversal launch shape (threads per block, shared-memory stack entries).
+struct TraceKernels {
+    void (*extend)(NativeArgs, int);
+    void (*shadow)(NativeArgs);
+};
+// Block sizes and shared stack depths the traversal kernels are built for.
+constexpr int kNumBlockShapes = 3;
+constexpr int kBlockShapes[kNumBlockShapes] = {64, 128, 256};
+constexpr int kNumStackShapes = 3;
+constexpr int kStackShapes[kNumStackShapes] = {0, 8, 16};
+static_assert(sizeof(tt_renderer::occ_trace) == sizeof(int) * kNumBlockShapes * kNumStackShapes &&
+                  sizeof(tt_renderer::occ_shade) == sizeof(int) * kNumBlockShapes,
+              "occupancy cache shape");
+// nullptr if (block, stack_shared) is not one of the built shapes.
+TraceKernels trace_kernels(int block, int stack_shared);
+
+}  // namespace tt

@@ -1,12 +1,16 @@
 // Native path tracer: a wavefront of compacted ray queues on one GB300.
 //
-// A frame is processed in waves of up to `wave_paths` paths (path = one sample of one pixel).
-// Per wave: raygen, then for each bounce extend (closest hit over the BVH and the analytic
-// objects) -> shade (emission, environment light sampling with MIS, BSDF sampling, Russian
-// roulette; survivors and shadow rays are appended to queues with one atomic per warp) ->
-// shadow (any hit), and finally accumulate (each pixel adds its samples in a fixed order, in
-// float or double). Every kernel reads its queue length from device memory, so a wave needs no
-// host round trip and the whole frame can be captured as a CUDA graph (tt_render_native_graph).
+// A render (one view, or a batch of views of any sizes and sample counts) is processed in waves
+// of up to `wave_paths` paths (path = one sample of one pixel of one view; index space in
+// tt_native.cuh). Per wave: raygen, then for each bounce extend (closest hit over the BVH and the
+// analytic objects, tt_render_extend.cu) -> shade (emission, environment light sampling with
+// MIS, BSDF sampling, Russian roulette; survivors and shadow rays are appended to queues with one
+// atomic per warp) -> shadow (any hit), and finally accumulate (each pixel adds its samples in
+// sample order, in float or double, so the sum does not depend on how the waves fall). Every
+// kernel is a persistent grid that reads its queue length from device memory, so a wave needs no
+// host round trip and a whole batch is captured once as a CUDA graph (tt_batch_render). The
+// launch shape (threads per block, shared-memory traversal stack depth, paths per wave) is a
+// renderer setting that tt_batch_autotune picks by timing.
 //
 // The integrator (all of it built from basic IEEE operations, tt_ptmath.cuh):
 //   camera     pinhole of the CameraMeta; pixel (x, y) with y = 0 at the top, jittered by two
@@ -25,59 +29,20 @@
 //   roulette   from rr_depth on, survival max(beta) clamped to [0.05, 1]
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <string>
 #include <vector>
 
-#include "tt_device.h"
-#include "tt_ptmath.cuh"
+#include "tt_native.cuh"
 
 namespace tt {
 
 using namespace pt;
 
-constexpr int kPtBlock = 128;
+constexpr int kShadeBlockMax = 256;
 constexpr int kFlagSpecular = 1;  // the last bounce was specular (no light sampling was done)
-
-struct EnvView {
-    const float4 *tex;  // w*h radiance
-    const float *marg;  // h+1 marginal CDF over rows
-    const float *cond;  // h*(w+1) conditional CDFs per row
-    int w, h;
-    float scale;
-};
-
-struct PathSoA {
-    float *o, *d;       // 3 per path
-    float *beta, *L;    // 3 per path
-    uint64_t *rng;      // PCG32 state (the stream increment is derived from the path index)
-    float *last_pdf;
-    int *depth, *flags;
-    float *hit_t, *hit_u, *hit_v;
-    int *hit_prim;      // triangle slot >= 0, -(geometry+2) for analytic objects, -1 = miss
-    int *queue[2];      // path indices of the active paths
-    int *counts;        // [0], [1] queue lengths by bounce parity, [2] shadow queue length
-    int *shadow_path;
-    float *shadow_ray;  // 8 per shadow ray
-    float *shadow_val;  // 3 per shadow ray
-};
-
-struct NativeArgs {
-    BvhView bvh;
-    const MaterialRec *materials;
-    int num_materials;
-    const GeomRec *geoms;
-    int num_geoms;
-    EnvView env;
-    PathSoA ps;
-    tt_camera_meta cam;
-    float tanx, tany;   // tan(fov/2)
-    tt_render_params p;
-    int npix;           // width * height
-    long long wave_first_path;  // global index of the wave's first path
-    int wave_paths;
-    unsigned int *err;
-};
 
 // ---- small helpers ------------------------------------------------------------------------------
 __device__ __forceinline__ int warp_append(int *counter, bool pred) {
@@ -96,13 +61,6 @@ __device__ __forceinline__ void st3(float *p, const V3 &v) {
     p[0] = v.x;
     p[1] = v.y;
     p[2] = v.z;
-}
-
-__device__ __forceinline__ Rng path_rng(const NativeArgs &a, long long gid, uint64_t state) {
-    Rng g;
-    g.state = state;
-    g.inc = ((uint64_t)gid << 1u) | 1u;
-    return g;
 }
 
 // ---- environment ------------------------------------------------------------------------------
@@ -338,76 +296,50 @@ __device__ __forceinline__ BsdfSample bsdf_sample(const MaterialRec &m, const V3
     return s;
 }
 
-// ---- analytic objects (brute force, as the reference does) --------------------------------------
-__device__ __forceinline__ void analytic_hit(const NativeArgs &a, const V3 &o, const V3 &d, float tmin, float &t,
-                                             int &prim, float &hu, float &hv) {
-    for (int i = 0; i < a.num_geoms; i++) {
-        const GeomRec g = a.geoms[i];
-        if (g.kind == GEOM_PLANE) {
-            const V3 p0(g.p0[0], g.p0[1], g.p0[2]);
-            const V3 e1 = sub(V3(g.p1[0], g.p1[1], g.p1[2]), p0), e2 = sub(V3(g.p2[0], g.p2[1], g.p2[2]), p0);
-            const V3 P = cross(d, e2);
-            const float det = dot(e1, P);
-            if (det > -1e-12f && det < 1e-12f) continue;
-            const float inv = PT_DIV(1.0f, det);
-            const V3 T = sub(o, p0);
-            const float u = PT_MUL(dot(T, P), inv);
-            if (u < 0.f || u > 1.f) continue;
-            const V3 Q = cross(T, e1);
-            const float v = PT_MUL(dot(d, Q), inv);
-            if (v < 0.f || v > 1.f) continue;
-            const float th = PT_MUL(dot(e2, Q), inv);
-            if (th > tmin && th < t) {
-                t = th;
-                prim = -(i + 2);
-                hu = u;
-                hv = v;
-            }
-        } else if (g.kind == GEOM_SPHERE) {
-            const V3 c(g.p0[0], g.p0[1], g.p0[2]);
-            const V3 oc = sub(c, o);
-            const float bq = dot(oc, d);
-            const float disc = PT_FMA(g.radius, g.radius, PT_FMA(bq, bq, -dot(oc, oc)));
-            if (disc < 0.0f) continue;
-            const float sq = PT_SQRT(disc);
-            float th = PT_SUB(bq, sq);
-            if (!(th > tmin)) th = PT_ADD(bq, sq);
-            if (th > tmin && th < t) {
-                t = th;
-                prim = -(i + 2);
-                hu = 0.f;
-                hv = 0.f;
-            }
-        }
-    }
+// ---- kernels ------------------------------------------------------------------------------------
+__device__ __forceinline__ void put_ray(float4 *rays, int slot, const V3 &o, const V3 &d) {
+    rays[2 * slot] = make_float4(o.x, o.y, o.z, d.x);
+    rays[2 * slot + 1] = make_float4(d.y, d.z, 0.0f, 1e20f);
 }
 
-// ---- kernels ------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(kPtBlock) k_raygen(NativeArgs a) {
+// Camera rays of the wave's paths into queue 0.
+__global__ void __launch_bounds__(kShadeBlockMax) k_raygen(NativeArgs a) {
     const int stride = gridDim.x * blockDim.x;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         a.ps.counts[0] = a.wave_paths;
         a.ps.counts[1] = 0;
         a.ps.counts[2] = 0;
+        a.ps.counts[3] = 0;
+        a.ps.counts[4] = 0;
+        atomicAdd(a.stats + 2, (unsigned long long)a.wave_paths);
     }
-    const V3 cam_pos(a.cam.position[0], a.cam.position[1], a.cam.position[2]);
-    const V3 view = normalize(V3(a.cam.view[0], a.cam.view[1], a.cam.view[2]));
-    const V3 right = normalize(cross(view, V3(a.cam.up[0], a.cam.up[1], a.cam.up[2])));
-    const V3 up = cross(right, view);
+    int cached = -1;
+    ViewRec vw;
+    V3 cam_pos, view, right, up;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.wave_paths; i += stride) {
-        const long long gid = a.wave_first_path + i;
-        const int pixel = (int)(gid % a.npix);
-        const int px = pixel % a.cam.width, py = pixel / a.cam.width;
-        Rng g = pcg32_seed((uint64_t)a.p.seed * 0x9E3779B97F4A7C15ull + 0x632BE59BD9B4E019ull, (uint64_t)gid);
-        const float jx = uniform(g), jy = uniform(g);
-        const float sx = PT_SUB(PT_MUL(2.0f, PT_DIV(PT_ADD((float)px, jx), (float)a.cam.width)), 1.0f);
-        const float sy = PT_SUB(1.0f, PT_MUL(2.0f, PT_DIV(PT_ADD((float)py, jy), (float)a.cam.height)));
-        const V3 dir = normalize(madd(up, PT_MUL(sy, a.tany), madd(right, PT_MUL(sx, a.tanx), view)));
-        st3(a.ps.o + 3ll * i, cam_pos);
-        st3(a.ps.d + 3ll * i, dir);
+        const long long g = a.wave_first + i;
+        const int v = find_view(a, g);
+        if (v != cached) {
+            vw = view_of(a, v);
+            cam_pos = V3(vw.pos[0], vw.pos[1], vw.pos[2]);
+            view = normalize(V3(vw.view[0], vw.view[1], vw.view[2]));
+            right = normalize(cross(view, V3(vw.up[0], vw.up[1], vw.up[2])));
+            up = cross(right, view);
+            cached = v;
+        }
+        const long long gid = vw.stream0 + (g - vw.first);
+        const int pixel = (int)(gid % vw.npix);
+        const int px = pixel % vw.width, py = pixel / vw.width;
+        Rng rg = pcg32_seed(vw.seed_state, (uint64_t)gid);
+        const float jx = uniform(rg), jy = uniform(rg);
+        const float sx = PT_SUB(PT_MUL(2.0f, PT_DIV(PT_ADD((float)px, jx), (float)vw.width)), 1.0f);
+        const float sy = PT_SUB(1.0f, PT_MUL(2.0f, PT_DIV(PT_ADD((float)py, jy), (float)vw.height)));
+        const V3 dir = normalize(madd(up, PT_MUL(sy, vw.tany), madd(right, PT_MUL(sx, vw.tanx), view)));
+        put_ray(a.ps.ray[0], i, cam_pos, dir);
         st3(a.ps.beta + 3ll * i, V3(1.f, 1.f, 1.f));
         st3(a.ps.L + 3ll * i, V3(0.f, 0.f, 0.f));
-        a.ps.rng[i] = g.state;
+        a.ps.rng[i] = rg.state;
+        a.ps.rng_inc[i] = rg.inc;
         a.ps.last_pdf[i] = 0.0f;
         a.ps.depth[i] = 0;
         a.ps.flags[i] = kFlagSpecular;
@@ -415,38 +347,12 @@ __global__ void __launch_bounds__(kPtBlock) k_raygen(NativeArgs a) {
     }
 }
 
-// closest hit of every queued path; `cur` = bounce parity
-__global__ void __launch_bounds__(kPtBlock) k_extend(NativeArgs a, int cur) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        a.ps.counts[cur ^ 1] = 0;
-        a.ps.counts[2] = 0;
-    }
-    const int n = a.ps.counts[cur];
-    const int stride = gridDim.x * blockDim.x;
-    uint32_t err = 0;
-    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += stride) {
-        const int i = a.ps.queue[cur][q];
-        const V3 o = ld3(a.ps.o + 3ll * i), d = ld3(a.ps.d + 3ll * i);
-        const float4 r0 = make_float4(o.x, o.y, o.z, d.x);
-        const float4 r1 = make_float4(d.y, d.z, 0.0f, 1e20f);
-        const TraceResult tr = traverse<true>(a.bvh, r0, r1, err);
-        float t = tr.t, hu = tr.u, hv = tr.v;
-        int prim = tr.addr;
-        if (a.num_geoms) analytic_hit(a, o, d, 0.0f, t, prim, hu, hv);
-        a.ps.hit_t[i] = t;
-        a.ps.hit_prim[i] = prim;
-        a.ps.hit_u[i] = hu;
-        a.ps.hit_v[i] = hv;
-    }
-    if (err) atomicOr(a.err, err);
-}
-
 __device__ __forceinline__ float ray_eps(const NativeArgs &a, const V3 &p) {
     const float m = fmaxf(fmaxf(fabsf(p.x), fabsf(p.y)), fabsf(p.z));
     return PT_MUL(a.p.ray_eps, fmaxf(1.0f, m));
 }
 
-__global__ void __launch_bounds__(kPtBlock) k_shade(NativeArgs a, int cur) {
+__global__ void __launch_bounds__(kShadeBlockMax) k_shade(NativeArgs a, int cur) {
     const int n = a.ps.counts[cur];
     const int stride = gridDim.x * blockDim.x;
     const int rounds = (n + stride - 1) / stride;
@@ -456,14 +362,16 @@ __global__ void __launch_bounds__(kPtBlock) k_shade(NativeArgs a, int cur) {
         bool alive = false;
         bool shadow = false;
         int i = 0;
-        V3 sh_o, sh_d, sh_val;
+        V3 sh_o, sh_d, sh_val, next_o, next_d;
         if (live) {
             i = a.ps.queue[cur][q];
-            const long long gid = a.wave_first_path + i;
-            Rng g = path_rng(a, gid, a.ps.rng[i]);
-            const V3 o = ld3(a.ps.o + 3ll * i), d = ld3(a.ps.d + 3ll * i);
+            Rng g;
+            g.state = a.ps.rng[i];
+            g.inc = a.ps.rng_inc[i];
+            const float4 r0 = a.ps.ray[cur][2 * q], r1 = a.ps.ray[cur][2 * q + 1];
+            const V3 o(r0.x, r0.y, r0.z), d(r0.w, r1.x, r1.y);
             V3 beta = ld3(a.ps.beta + 3ll * i), L = ld3(a.ps.L + 3ll * i);
-            const int prim = a.ps.hit_prim[i];
+            const int prim = a.ps.hit_prim[q];
             const int flags = a.ps.flags[i];
             const float last_pdf = a.ps.last_pdf[i];
             int depth = a.ps.depth[i];
@@ -479,12 +387,12 @@ __global__ void __launch_bounds__(kPtBlock) k_shade(NativeArgs a, int cur) {
                     L = madd(mul(beta, le), w, L);
                 }
             } else {
-                const float t = a.ps.hit_t[i];
+                const float t = a.ps.hit_t[q];
                 const V3 p = madd(d, t, o);
                 V3 n;
                 int mat;
                 if (prim >= 0) {
-                    hit_normal(a.bvh, prim, a.ps.hit_u[i], a.ps.hit_v[i], n.x, n.y, n.z);
+                    hit_normal(a.bvh, prim, a.ps.hit_u[q], a.ps.hit_v[q], n.x, n.y, n.z);
                     mat = (int)__ldg(a.bvh.mat_idx + prim);
                 } else {
                     const GeomRec g2 = a.geoms[-prim - 2];
@@ -544,8 +452,8 @@ __global__ void __launch_bounds__(kPtBlock) k_shade(NativeArgs a, int cur) {
                     }
                     if (alive) {
                         const V3 off = dot(bs.wi, nl) >= 0.0f ? nl : V3(-nl.x, -nl.y, -nl.z);
-                        st3(a.ps.o + 3ll * i, madd(off, eps, p));
-                        st3(a.ps.d + 3ll * i, bs.wi);
+                        next_o = madd(off, eps, p);
+                        next_d = bs.wi;
                         st3(a.ps.beta + 3ll * i, beta);
                         a.ps.last_pdf[i] = bs.pdf;
                         a.ps.flags[i] = (bs.specular || !nee) ? kFlagSpecular : 0;
@@ -557,63 +465,40 @@ __global__ void __launch_bounds__(kPtBlock) k_shade(NativeArgs a, int cur) {
             a.ps.rng[i] = g.state;
         }
         const int slot = warp_append(a.ps.counts + (cur ^ 1), alive);
-        if (alive) a.ps.queue[cur ^ 1][slot] = i;
+        if (alive) {
+            a.ps.queue[cur ^ 1][slot] = i;
+            put_ray(a.ps.ray[cur ^ 1], slot, next_o, next_d);
+        }
         const int sslot = warp_append(a.ps.counts + 2, shadow);
         if (shadow) {
             a.ps.shadow_path[sslot] = i;
-            float *r = a.ps.shadow_ray + 8ll * sslot;
-            r[0] = sh_o.x;
-            r[1] = sh_o.y;
-            r[2] = sh_o.z;
-            r[3] = sh_d.x;
-            r[4] = sh_d.y;
-            r[5] = sh_d.z;
-            r[6] = 0.0f;
-            r[7] = 1e20f;
+            put_ray(a.ps.shadow_ray, sslot, sh_o, sh_d);
             st3(a.ps.shadow_val + 3ll * sslot, sh_val);
         }
     }
 }
 
-__global__ void __launch_bounds__(kPtBlock) k_shadow(NativeArgs a) {
-    const int n = a.ps.counts[2];
-    const int stride = gridDim.x * blockDim.x;
-    uint32_t err = 0;
-    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += stride) {
-        const float4 *r = reinterpret_cast<const float4 *>(a.ps.shadow_ray + 8ll * j);
-        const float4 r0 = r[0], r1 = r[1];
-        const TraceResult tr = traverse<false>(a.bvh, r0, r1, err);
-        bool blocked = tr.addr >= 0;
-        if (!blocked && a.num_geoms) {
-            float t = r1.w, hu, hv;
-            int prim = -1;
-            analytic_hit(a, V3(r0.x, r0.y, r0.z), V3(r0.w, r1.x, r1.y), r1.z, t, prim, hu, hv);
-            blocked = prim != -1;
-        }
-        if (!blocked) {
-            const int i = a.ps.shadow_path[j];
-            st3(a.ps.L + 3ll * i, add(ld3(a.ps.L + 3ll * i), ld3(a.ps.shadow_val + 3ll * j)));
-        }
-    }
-    if (err) atomicOr(a.err, err);
-}
-
+// Adds the wave's path radiance to the views' accumulation blocks. The thread of a pixel's first
+// path in the wave adds all of that pixel's paths in the wave, in sample order.
 template <typename T>
-__global__ void __launch_bounds__(kPtBlock) k_accumulate(NativeArgs a, T *accum) {
-    // paths of the wave are laid out sample-major: path i = (wave sample k) * npix + pixel
-    const int first_pixel = (int)(a.wave_first_path % a.npix);
+__global__ void __launch_bounds__(kShadeBlockMax) k_accumulate(NativeArgs a, T *accum) {
     const int stride = gridDim.x * blockDim.x;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.npix && i < a.wave_paths; i += stride) {
-        const int pixel = (first_pixel + i) % a.npix;
-        T acc[3] = {accum[3ll * pixel], accum[3ll * pixel + 1], accum[3ll * pixel + 2]};
-        for (int k = i; k < a.wave_paths; k += a.npix) {
-            acc[0] += (T)a.ps.L[3ll * k];
-            acc[1] += (T)a.ps.L[3ll * k + 1];
-            acc[2] += (T)a.ps.L[3ll * k + 2];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.wave_paths; i += stride) {
+        const long long g = a.wave_first + i;
+        const ViewRec vw = view_of(a, find_view(a, g));
+        const long long l = g - vw.first;
+        if (l >= vw.npix && g - vw.npix >= a.wave_first) continue;  // not the pixel's first path here
+        const long long pixel = l % vw.npix;
+        T *px = accum + vw.accum + 3 * pixel;
+        T acc[3] = {px[0], px[1], px[2]};
+        for (long long k = i, lk = l; k < a.wave_paths && lk < vw.paths; k += vw.npix, lk += vw.npix) {
+            acc[0] += (T)a.ps.L[3 * k];
+            acc[1] += (T)a.ps.L[3 * k + 1];
+            acc[2] += (T)a.ps.L[3 * k + 2];
         }
-        accum[3ll * pixel] = acc[0];
-        accum[3ll * pixel + 1] = acc[1];
-        accum[3ll * pixel + 2] = acc[2];
+        px[0] = acc[0];
+        px[1] = acc[1];
+        px[2] = acc[2];
     }
 }
 
@@ -696,53 +581,222 @@ void native_release(tt_renderer *r) {
     r->path_capacity = 0;
 }
 
-// Carves the path state of `cap` paths out of one allocation.
+// Path state for `cap` paths, carved out of one allocation sized for the renderer's capacity (so
+// the pointers, which captured graphs hold, change only when the allocation does).
 static tt_status ensure_paths(tt_renderer *r, int cap, PathSoA &ps) {
     auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
-    const size_t n = (size_t)cap;
-    const size_t sizes[] = {12 * n, 12 * n, 12 * n, 12 * n, 8 * n, 4 * n, 4 * n, 4 * n, 4 * n, 4 * n, 4 * n,
-                            4 * n, 4 * n, 4 * n, 64, 4 * n, 32 * n, 12 * n};
-    size_t total = 0;
-    for (size_t s : sizes) total += al(s);
-    if (r->paths_bytes < total) {
+    auto layout = [&](size_t n, size_t *sizes) {
+        const size_t s[] = {12 * n, 12 * n, 8 * n, 8 * n, 4 * n, 4 * n, 4 * n, 4 * n, 4 * n, 32 * n, 32 * n,
+                            4 * n,  4 * n,  4 * n, 4 * n, 64,    4 * n, 32 * n, 12 * n};
+        size_t total = 0;
+        for (int i = 0; i < 19; i++) {
+            sizes[i] = s[i];
+            total += al(s[i]);
+        }
+        return total;
+    };
+    size_t sizes[19];
+    if (r->path_capacity < cap || !r->paths) {
+        const size_t total = layout((size_t)cap, sizes);
         if (r->paths) cudaFree(r->paths);
         r->paths = nullptr;
         r->paths_bytes = 0;
+        r->path_capacity = 0;
         cudaError_t e = cudaMalloc(&r->paths, total);
         if (e != cudaSuccess) return fail(TT_ERR_OOM, std::string("path state: ") + cudaGetErrorString(e));
         r->paths_bytes = total;
         r->path_capacity = cap;
+        r->paths_gen++;
     }
+    layout((size_t)r->path_capacity, sizes);
     char *p = static_cast<char *>(r->paths);
-    int k = 0;
-    auto take = [&](void *&dst) {
-        dst = p;
-        p += al(sizes[k++]);
-    };
-    void *v[18];
-    for (int i = 0; i < 18; i++) take(v[i]);
-    ps.o = (float *)v[0];
-    ps.d = (float *)v[1];
-    ps.beta = (float *)v[2];
-    ps.L = (float *)v[3];
-    ps.rng = (uint64_t *)v[4];
-    ps.last_pdf = (float *)v[5];
-    ps.depth = (int *)v[6];
-    ps.flags = (int *)v[7];
-    ps.hit_t = (float *)v[8];
-    ps.hit_u = (float *)v[9];
-    ps.hit_v = (float *)v[10];
-    ps.hit_prim = (int *)v[11];
-    ps.queue[0] = (int *)v[12];
-    ps.queue[1] = (int *)v[13];
-    ps.counts = (int *)v[14];
-    ps.shadow_path = (int *)v[15];
-    ps.shadow_ray = (float *)v[16];
-    ps.shadow_val = (float *)v[17];
+    void *v[19];
+    for (int i = 0; i < 19; i++) {
+        v[i] = p;
+        p += al(sizes[i]);
+    }
+    ps.beta = (float *)v[0];
+    ps.L = (float *)v[1];
+    ps.rng = (uint64_t *)v[2];
+    ps.rng_inc = (uint64_t *)v[3];
+    ps.last_pdf = (float *)v[4];
+    ps.depth = (int *)v[5];
+    ps.flags = (int *)v[6];
+    ps.queue[0] = (int *)v[7];
+    ps.queue[1] = (int *)v[8];
+    ps.ray[0] = (float4 *)v[9];
+    ps.ray[1] = (float4 *)v[10];
+    ps.hit_t = (float *)v[11];
+    ps.hit_u = (float *)v[12];
+    ps.hit_v = (float *)v[13];
+    ps.hit_prim = (int *)v[14];
+    ps.counts = (int *)v[15];
+    ps.shadow_path = (int *)v[16];
+    ps.shadow_ray = (float4 *)v[17];
+    ps.shadow_val = (float *)v[18];
     return TT_OK;
 }
 
-static const int kMaxWavePaths = 1 << 22;
+constexpr int kMaxWavePaths = 1 << 24;
+
+static int block_index(int block) {
+    for (int i = 0; i < kNumBlockShapes; i++)
+        if (kBlockShapes[i] == block) return i;
+    return -1;
+}
+static int stack_index(int sh) {
+    for (int i = 0; i < kNumStackShapes; i++)
+        if (kStackShapes[i] == sh) return i;
+    return -1;
+}
+
+// A launch shape resolved to kernels and persistent grid sizes.
+struct Launch {
+    TraceKernels tk;
+    int block = 0, wave = 0;
+    int grid_trace = 0, grid_shade = 0;
+};
+
+static tt_status resolve_launch(tt_renderer *r, int block, int sh, int wave, Launch &L) {
+    const int bi = block_index(block), si = stack_index(sh);
+    if (bi < 0 || si < 0 || wave < 1 || wave > kMaxWavePaths)
+        return fail(TT_ERR_INVALID, "launch shape: block must be 64/128/256, stack_shared 0/8/16, "
+                                    "wave_paths 1..16777216");
+    L.tk = trace_kernels(block, sh);
+    L.block = block;
+    L.wave = wave;
+    if (!r->occ_trace[bi][si]) {
+        int b = 0;
+        TT_CUDA_N(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, (const void *)L.tk.extend, block, 0));
+        int b2 = 0;
+        TT_CUDA_N(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, (const void *)L.tk.shadow, block, 0));
+        r->occ_trace[bi][si] = std::max(1, std::min(b, b2));
+    }
+    if (!r->occ_shade[bi]) {
+        int b = 0;
+        TT_CUDA_N(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, (const void *)k_shade, block, 0));
+        r->occ_shade[bi] = std::max(1, b);
+    }
+    L.grid_trace = r->num_sms * r->occ_trace[bi][si];
+    L.grid_shade = r->num_sms * r->occ_shade[bi];
+    return TT_OK;
+}
+
+static ViewRec make_view(const tt_camera_meta &cam, int spp, int sample_offset, uint32_t seed, long long first,
+                         long long accum) {
+    ViewRec v;
+    std::memset(&v, 0, sizeof(v));
+    v.width = cam.width;
+    v.height = cam.height;
+    v.npix = cam.width * cam.height;
+    v.first = first;
+    v.paths = (long long)v.npix * spp;
+    v.accum = accum;
+    v.stream0 = (long long)sample_offset * v.npix;
+    v.seed_state = (uint64_t)seed * 0x9E3779B97F4A7C15ull + 0x632BE59BD9B4E019ull;
+    for (int k = 0; k < 3; k++) {
+        v.pos[k] = cam.position[k];
+        v.view[k] = cam.view[k];
+        v.up[k] = cam.up[k];
+    }
+    v.tanx = (float)std::tan((double)cam.fov[0] * 0.5 * 3.14159265358979323846 / 180.0);
+    v.tany = (float)std::tan((double)cam.fov[1] * 0.5 * 3.14159265358979323846 / 180.0);
+    return v;
+}
+
+static tt_status check_view(const tt_camera_meta &cam, int spp, int sample_offset) {
+    if (cam.width <= 0 || cam.height <= 0 || spp < 1 || sample_offset < 0)
+        return fail(TT_ERR_INVALID, "bad image size, spp or sample offset");
+    if ((long long)cam.width * cam.height > (1ll << 30)) return fail(TT_ERR_INVALID, "image too large");
+    if ((long long)cam.width * cam.height * ((long long)sample_offset + spp) > (1ll << 62))
+        return fail(TT_ERR_INVALID, "sample index out of range");
+    return TT_OK;
+}
+
+static tt_status check_params(const tt_render_params &p) {
+    if (p.max_depth < 1 || p.max_depth > 1024) return fail(TT_ERR_INVALID, "max_depth must be in 1..1024");
+    return TT_OK;
+}
+
+static NativeArgs base_args(tt_renderer *r, const tt_render_params &p, const PathSoA &ps) {
+    NativeArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.bvh = r->bvh;
+    a.materials = r->materials;
+    a.num_materials = r->num_materials;
+    a.geoms = r->geoms;
+    a.num_geoms = r->num_geoms;
+    a.env.tex = r->env;
+    a.env.marg = r->env_marg;
+    a.env.cond = r->env_cond;
+    a.env.w = r->env_w;
+    a.env.h = r->env_h;
+    a.env.scale = p.env_scale;
+    a.ps = ps;
+    a.p = p;
+    a.err = r->err;
+    a.stats = renderer_stats(r);
+    return a;
+}
+
+// Issues the kernels of `total` paths (waves of L.wave) on stream s. accum = nullptr: no
+// accumulation (autotuning trials).
+static tt_status issue(NativeArgs a, long long total, const Launch &L, void *accum, cudaStream_t s) {
+    const bool f64 = (a.p.flags & TT_RENDER_ACCUM_F64) != 0;
+    for (long long done = 0; done < total; done += L.wave) {
+        a.wave_first = done;
+        a.wave_paths = (int)std::min<long long>(total - done, L.wave);
+        k_raygen<<<L.grid_shade, L.block, 0, s>>>(a);
+        for (int b = 0; b < a.p.max_depth; b++) {
+            L.tk.extend<<<L.grid_trace, L.block, 0, s>>>(a, b & 1);
+            k_shade<<<L.grid_shade, L.block, 0, s>>>(a, b & 1);
+            L.tk.shadow<<<L.grid_trace, L.block, 0, s>>>(a);
+        }
+        if (accum) {
+            if (f64) k_accumulate<double><<<L.grid_shade, L.block, 0, s>>>(a, (double *)accum);
+            else k_accumulate<float><<<L.grid_shade, L.block, 0, s>>>(a, (float *)accum);
+        }
+    }
+    TT_CUDA_N(cudaGetLastError());
+    return TT_OK;
+}
+
+}  // namespace tt
+
+// A compiled batch of views: the device view table and, once rendered, the captured graph.
+struct tt_batch {
+    tt_renderer *r = nullptr;
+    std::vector<tt::ViewRec> views;
+    tt::ViewRec *d_views = nullptr;
+    long long total_paths = 0;
+    long long accum_elems = 0;
+    tt_render_params p{};
+    cudaStream_t cap = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    void *graph_accum = nullptr;
+    int graph_block = 0, graph_stack = -1, graph_wave = 0;
+    unsigned long long graph_paths_gen = 0;
+    int graph_kernels = 0;
+};
+
+namespace tt {
+
+static void drop_graph(tt_batch *b) {
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+    b->graph_accum = nullptr;
+}
+
+static NativeArgs batch_args(tt_batch *b, const PathSoA &ps) {
+    NativeArgs a = base_args(b->r, b->p, ps);
+    a.views = b->d_views;
+    a.n_views = (int)b->views.size();
+    a.view0 = b->views[0];
+    return a;
+}
 
 }  // namespace tt
 
@@ -766,51 +820,199 @@ tt_status tt_render_params_default(tt_render_params *out) {
 tt_status tt_render_native(tt_renderer *r, const tt_camera_meta *cam, const tt_render_params *p, void *d_accum,
                            void *stream) {
     if (!r || !cam || !p || !d_accum) return fail(TT_ERR_INVALID, "null argument");
-    if (cam->width <= 0 || cam->height <= 0 || p->spp < 1 || p->max_depth < 1 || p->sample_offset < 0)
-        return fail(TT_ERR_INVALID, "bad image size or render parameters");
-    const long long npix = (long long)cam->width * cam->height;
-    if (npix > (1ll << 30)) return fail(TT_ERR_INVALID, "image too large");
-    const long long total = npix * p->spp;
-    int wave = (int)(total < kMaxWavePaths ? total : (kMaxWavePaths / npix > 0 ? (kMaxWavePaths / npix) * npix
-                                                                                : kMaxWavePaths));
-    PathSoA ps;
-    tt_status st = ensure_paths(r, wave > r->path_capacity ? wave : r->path_capacity, ps);
+    tt_status st = check_view(*cam, p->spp, p->sample_offset);
+    if (st == TT_OK) st = check_params(*p);
     if (st != TT_OK) return st;
-    NativeArgs a;
-    a.bvh = r->bvh;
-    a.materials = r->materials;
-    a.num_materials = r->num_materials;
-    a.geoms = r->geoms;
-    a.num_geoms = r->num_geoms;
-    a.env.tex = r->env;
-    a.env.marg = r->env_marg;
-    a.env.cond = r->env_cond;
-    a.env.w = r->env_w;
-    a.env.h = r->env_h;
-    a.env.scale = p->env_scale;
-    a.ps = ps;
-    a.cam = *cam;
-    a.tanx = (float)std::tan((double)cam->fov[0] * 0.5 * 3.14159265358979323846 / 180.0);
-    a.tany = (float)std::tan((double)cam->fov[1] * 0.5 * 3.14159265358979323846 / 180.0);
-    a.p = *p;
-    a.npix = (int)npix;
-    a.err = r->err;
-    cudaStream_t s = (cudaStream_t)stream;
-    const int grid = r->num_sms * 8;
-    const long long first = (long long)p->sample_offset * npix;
-    for (long long done = 0; done < total; done += wave) {
-        a.wave_first_path = first + done;
-        a.wave_paths = (int)((total - done) < wave ? (total - done) : wave);
-        k_raygen<<<grid, kPtBlock, 0, s>>>(a);
-        for (int b = 0; b < p->max_depth; b++) {
-            k_extend<<<grid, kPtBlock, 0, s>>>(a, b & 1);
-            k_shade<<<grid, kPtBlock, 0, s>>>(a, b & 1);
-            k_shadow<<<grid, kPtBlock, 0, s>>>(a);
+    const ViewRec v = make_view(*cam, p->spp, p->sample_offset, p->seed, 0, 0);
+    Launch L;
+    st = resolve_launch(r, r->launch_block, r->launch_stack, r->launch_wave, L);
+    if (st != TT_OK) return st;
+    PathSoA ps;
+    st = ensure_paths(r, (int)std::min<long long>(v.paths, L.wave), ps);
+    if (st != TT_OK) return st;
+    NativeArgs a = base_args(r, *p, ps);
+    a.views = nullptr;
+    a.n_views = 1;
+    a.view0 = v;
+    return issue(a, v.paths, L, d_accum, (cudaStream_t)stream);
+}
+
+tt_status tt_renderer_set_launch(tt_renderer *r, const tt_launch_shape *shape) {
+    if (!r || !shape) return fail(TT_ERR_INVALID, "null argument");
+    Launch L;
+    tt_status st = resolve_launch(r, shape->block, shape->stack_shared, shape->wave_paths, L);
+    if (st != TT_OK) return st;
+    r->launch_block = shape->block;
+    r->launch_stack = shape->stack_shared;
+    r->launch_wave = shape->wave_paths;
+    return TT_OK;
+}
+
+tt_status tt_renderer_get_launch(const tt_renderer *r, tt_launch_shape *shape) {
+    if (!r || !shape) return fail(TT_ERR_INVALID, "null argument");
+    shape->block = r->launch_block;
+    shape->stack_shared = r->launch_stack;
+    shape->wave_paths = r->launch_wave;
+    shape->ms = 0.0f;
+    return TT_OK;
+}
+
+tt_status tt_renderer_stats(tt_renderer *r, uint64_t *out, int reset) {
+    if (!r || !out) return fail(TT_ERR_INVALID, "null argument");
+    unsigned long long s[3];
+    TT_CUDA_N(cudaMemcpy(s, renderer_stats(r), sizeof(s), cudaMemcpyDeviceToHost));
+    for (int i = 0; i < 3; i++) out[i] = s[i];
+    if (reset) TT_CUDA_N(cudaMemset(renderer_stats(r), 0, sizeof(s)));
+    return TT_OK;
+}
+
+tt_status tt_batch_create(tt_renderer *r, const tt_view *views, int n, const tt_render_params *p, tt_batch **out) {
+    if (!r || !views || !p || !out) return fail(TT_ERR_INVALID, "null argument");
+    *out = nullptr;
+    if (n < 1) return fail(TT_ERR_INVALID, "a batch needs at least one view");
+    tt_status st = check_params(*p);
+    if (st != TT_OK) return st;
+    tt_batch *b = new tt_batch();
+    b->r = r;
+    b->p = *p;
+    b->views.reserve(n);
+    for (int k = 0; k < n; k++) {
+        st = check_view(views[k].cam, views[k].spp, views[k].sample_offset);
+        if (st != TT_OK) {
+            delete b;
+            return fail(TT_ERR_INVALID, "view " + std::to_string(k) + ": " + tt_last_error_string());
         }
-        if (p->flags & TT_RENDER_ACCUM_F64) k_accumulate<double><<<grid, kPtBlock, 0, s>>>(a, (double *)d_accum);
-        else k_accumulate<float><<<grid, kPtBlock, 0, s>>>(a, (float *)d_accum);
+        b->views.push_back(
+            make_view(views[k].cam, views[k].spp, views[k].sample_offset, views[k].seed, b->total_paths, b->accum_elems));
+        b->total_paths += b->views.back().paths;
+        b->accum_elems += 3ll * b->views.back().npix;
     }
-    TT_CUDA_N(cudaGetLastError());
+    cudaError_t e = cudaMalloc((void **)&b->d_views, sizeof(ViewRec) * n);
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_views, b->views.data(), sizeof(ViewRec) * n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        tt_batch_free(b);
+        return cuda_fail_n(e, "batch view table");
+    }
+    *out = b;
+    return TT_OK;
+}
+
+tt_status tt_batch_info(const tt_batch *b, int64_t *total_paths, int64_t *accum_elems) {
+    if (!b) return fail(TT_ERR_INVALID, "null batch");
+    if (total_paths) *total_paths = b->total_paths;
+    if (accum_elems) *accum_elems = b->accum_elems;
+    return TT_OK;
+}
+
+tt_status tt_batch_render(tt_batch *b, void *d_accum, int use_graph, void *stream) {
+    if (!b || !d_accum) return fail(TT_ERR_INVALID, "null argument");
+    tt_renderer *r = b->r;
+    Launch L;
+    tt_status st = resolve_launch(r, r->launch_block, r->launch_stack, r->launch_wave, L);
+    if (st != TT_OK) return st;
+    PathSoA ps;
+    st = ensure_paths(r, (int)std::min<long long>(b->total_paths, L.wave), ps);
+    if (st != TT_OK) return st;
+    const NativeArgs a = batch_args(b, ps);
+    if (!use_graph) return issue(a, b->total_paths, L, d_accum, (cudaStream_t)stream);
+    const bool stale = !b->exec || b->graph_accum != d_accum || b->graph_block != L.block ||
+                       b->graph_stack != r->launch_stack || b->graph_wave != L.wave ||
+                       b->graph_paths_gen != r->paths_gen;
+    if (stale) {
+        drop_graph(b);
+        TT_CUDA_N(cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal));
+        st = issue(a, b->total_paths, L, d_accum, b->cap);
+        cudaGraph_t g = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(b->cap, &g);
+        if (st != TT_OK) {
+            if (g) cudaGraphDestroy(g);
+            return st;
+        }
+        if (e != cudaSuccess) return cuda_fail_n(e, "capturing the batch");
+        b->graph = g;
+        const cudaError_t e2 = cudaGraphInstantiate(&b->exec, g, 0);
+        if (e2 != cudaSuccess) {
+            drop_graph(b);
+            return cuda_fail_n(e2, "instantiating the batch graph");
+        }
+        size_t nodes = 0;
+        cudaGraphGetNodes(g, nullptr, &nodes);
+        b->graph_kernels = (int)nodes;
+        b->graph_accum = d_accum;
+        b->graph_block = L.block;
+        b->graph_stack = r->launch_stack;
+        b->graph_wave = L.wave;
+        b->graph_paths_gen = r->paths_gen;
+    }
+    TT_CUDA_N(cudaGraphLaunch(b->exec, (cudaStream_t)stream));
+    return TT_OK;
+}
+
+tt_status tt_batch_graph_kernels(const tt_batch *b, int *kernels) {
+    if (!b || !kernels) return fail(TT_ERR_INVALID, "null argument");
+    *kernels = b->exec ? b->graph_kernels : 0;
+    return TT_OK;
+}
+
+tt_status tt_batch_autotune(tt_batch *b, int64_t sample_paths, void *stream, tt_launch_shape *results, int max_results,
+                            int *n_results) {
+    if (!b) return fail(TT_ERR_INVALID, "null batch");
+    tt_renderer *r = b->r;
+    cudaStream_t s = (cudaStream_t)stream;
+    const long long sample = std::min<long long>(b->total_paths, sample_paths > 0 ? sample_paths : (8ll << 20));
+    static const int kWaves[] = {1 << 20, 1 << 21, 1 << 22};
+    PathSoA ps;
+    tt_status st = ensure_paths(r, (int)std::min<long long>(sample, kWaves[2]), ps);
+    if (st != TT_OK) return st;
+    NativeArgs a = batch_args(b, ps);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    TT_CUDA_N(cudaEventCreate(&e0));
+    TT_CUDA_N(cudaEventCreate(&e1));
+    float best = 3.4e38f;
+    tt_launch_shape best_shape{r->launch_block, r->launch_stack, r->launch_wave, 0.0f};
+    int count = 0;
+    for (int bi = 0; bi < kNumBlockShapes; bi++)
+        for (int si = 0; si < kNumStackShapes; si++)
+            for (int wave : kWaves) {
+                if (wave > kWaves[0] && wave / 2 >= sample) continue;  // the same as a smaller wave
+                Launch L;
+                st = resolve_launch(r, kBlockShapes[bi], kStackShapes[si], wave, L);
+                if (st == TT_OK) st = issue(a, std::min<long long>(sample, 1 << 16), L, nullptr, s);  // warm-up
+                cudaError_t e = cudaEventRecord(e0, s);
+                if (st == TT_OK && e == cudaSuccess) st = issue(a, sample, L, nullptr, s);
+                if (e == cudaSuccess) e = cudaEventRecord(e1, s);
+                if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+                float ms = 0.0f;
+                if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+                if (st != TT_OK || e != cudaSuccess) {
+                    cudaEventDestroy(e0);
+                    cudaEventDestroy(e1);
+                    return st != TT_OK ? st : cuda_fail_n(e, "autotune timing");
+                }
+                const tt_launch_shape shape{kBlockShapes[bi], kStackShapes[si], wave, ms};
+                if (results && count < max_results) results[count] = shape;
+                count++;
+                if (ms < best) {
+                    best = ms;
+                    best_shape = shape;
+                }
+            }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    r->launch_block = best_shape.block;
+    r->launch_stack = best_shape.stack_shared;
+    r->launch_wave = best_shape.wave_paths;
+    if (n_results) *n_results = count;
+    return TT_OK;
+}
+
+tt_status tt_batch_free(tt_batch *b) {
+    if (!b) return TT_OK;
+    drop_graph(b);
+    if (b->d_views) cudaFree(b->d_views);
+    if (b->cap) cudaStreamDestroy(b->cap);
+    delete b;
     return TT_OK;
 }
 

@@ -277,6 +277,22 @@ struct TraceResult {
     float u, v;
 };
 
+// One ray through the BVH, start to finish, on the given stack.
+template <bool kClosest, class Stack>
+__device__ __forceinline__ TraceResult traverse_on(Stack &stack, const BvhView &bvh, float4 r0, float4 r1,
+                                                   uint32_t &err) {
+    TravState s;
+    trav_init(s, stack, r0, r1);
+    while (!trav_iterate<kClosest, false>(s, stack, bvh, err, r1.w)) {
+    }
+    TraceResult res;
+    res.addr = s.addr;
+    res.t = s.t;
+    res.u = s.u;
+    res.v = s.v;
+    return res;
+}
+
 // One ray through the BVH, start to finish, with its whole stack in local memory.
 template <bool kClosest>
 __device__ __forceinline__ TraceResult traverse(const BvhView &bvh, float4 r0, float4 r1, uint32_t &err) {

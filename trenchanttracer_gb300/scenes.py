@@ -415,6 +415,29 @@ def cosine_hemisphere(normals: np.ndarray, seed: int) -> np.ndarray:
     return _normalize(d.astype(F))
 
 
+def orbit_views(count: int = 64, seed: int = 5, scale: float = 8.0, sizes=(256, 512, 768, 1024),
+                spps=(4, 16, 64), fov: float = 60.0) -> list[tuple]:
+    """Camera views for a batched render of the terrain: orbit poses in the reference's camera
+    model (eye = centre + (sin yaw cos pitch, sin pitch, cos yaw cos pitch) * radius, looking at the
+    centre, src/core/Camera.cpp:121-140) with yaw U[0, 2pi), pitch U(0.25, 0.9) rad and radius
+    1.5 * scale; square images of a size drawn from `sizes` and a sample count drawn from `spps`.
+    Returns [(tt_camera_meta, spp, sample_offset 0, seed)]."""
+    from .core import make_camera_meta
+
+    rng = np.random.default_rng(seed)
+    views = []
+    for k in range(count):
+        yaw = float(rng.uniform(0.0, 2.0 * np.pi))
+        pitch = float(rng.uniform(0.25, 0.9))
+        res = int(rng.choice(sizes))
+        spp = int(rng.choice(spps))
+        r = 1.5 * scale
+        eye = [r * np.sin(yaw) * np.cos(pitch), r * np.sin(pitch), r * np.cos(yaw) * np.cos(pitch)]
+        cam = make_camera_meta(res, res, eye, [-eye[0], -eye[1], -eye[2]], fov=(fov, fov))
+        views.append((cam, spp, 0, 1000 + k))
+    return views
+
+
 def terrain_camera(scale: float) -> dict:
     """The recorded pose of the terrain ray-cast benchmark."""
     return {"eye": [0.0, 0.9 * scale, 1.6 * scale], "target": [0.0, 0.0, 0.1 * scale], "tan_half_fov": 0.45}
