@@ -342,6 +342,59 @@ tt_status tt_batch_autotune(tt_batch *batch, int64_t sample_paths, void *stream,
                             int32_t max_results, int32_t *n_results);
 tt_status tt_batch_free(tt_batch *batch);
 
+/* Learned radiance cache (no counterpart in the reference): an MLP (160 encoded inputs, five
+ * hidden layers of 64 with ReLU, RGB = exp(output)) with BF16 weights and FP32 accumulation on
+ * tensor cores, trained online by Adam on a relative L2 loss from radiance the path tracer
+ * itself measures. A feature record is 16 floats: position, direction towards the previous
+ * vertex, shading normal, roughness, albedo (3), material kind / 8, 2 zeros. */
+typedef struct tt_cache tt_cache;
+typedef struct tt_cache_params {
+    float lr, beta1, beta2, eps; /* Adam (defaults 1e-2, 0.9, 0.99, 1e-10) */
+    float ema;                   /* inference weights = exponential average of the weights (0.95) */
+    int32_t batch;               /* records per training step (16384) */
+    int32_t steps;               /* training steps per rendered wave (4) */
+    int32_t train_paths;         /* training paths per wave: traced to full depth, no cache (65536) */
+    float spread_c;              /* end a path (from its second vertex on) when its spread exceeds
+                                    spread_c x its pixel footprint (0.01); < 0: never */
+    uint32_t seed;               /* weight initialisation (1) */
+    int32_t use_ema;             /* render with the averaged weights (1) */
+    float bbox_lo[3], bbox_hi[3];/* scene bounds of the position encoding */
+} tt_cache_params;
+tt_status tt_cache_params_default(tt_cache_params *params);
+tt_status tt_cache_create(const tt_cache_params *params, tt_cache **out);
+tt_status tt_cache_free(tt_cache *cache);
+/* Number of FP32 weights (27136): per layer [out][in], layers 160x64, 4 x 64x64, 64x8 (rows 3..7
+ * of the last layer are padding and stay 0). */
+tt_status tt_cache_param_count(int32_t *n);
+/* which: 0 master weights, 1 averaged weights, 2 the last gradient (tt_cache_gradient). */
+tt_status tt_cache_get_weights(const tt_cache *cache, float *h_weights, int32_t which);
+/* Sets master and averaged weights (and their BF16 copies); resets the optimiser. */
+tt_status tt_cache_set_weights(tt_cache *cache, const float *h_weights);
+/* Encoded inputs of n <= batch records as n x 160 BF16 (tests). */
+tt_status tt_cache_encode(tt_cache *cache, const float *d_records, int64_t n, void *d_encoded, void *stream);
+/* Radiance (n x 3 floats) of n records. Launch only. */
+tt_status tt_cache_infer(tt_cache *cache, const float *d_records, int64_t n, float *d_rgb, int32_t use_ema,
+                         void *stream);
+/* Gradient of the mean loss over n <= batch records w.r.t. the weights (host, tt_cache_param_count
+ * floats) and the loss; no update. Synchronous. */
+tt_status tt_cache_gradient(tt_cache *cache, const float *d_records, const float *d_targets, int64_t n,
+                            float *h_gradient, float *h_loss, void *stream);
+/* `steps` Adam steps over consecutive slices of `batch` of n records (targets: n x 3 radiance);
+ * h_loss (optional) receives the mean loss. Synchronous only when h_loss is given. */
+tt_status tt_cache_train(tt_cache *cache, const float *d_records, const float *d_targets, int64_t n, int32_t steps,
+                         float *h_loss, void *stream);
+/* Adam steps taken so far. */
+tt_status tt_cache_steps(const tt_cache *cache, int32_t *steps);
+/* The native path tracer with the cache: a path that is not a training path ends at the first
+ * vertex from its second on where its spread exceeds spread_c x its pixel footprint, adding
+ * throughput x (emission + cache radiance); training paths (cache params train_paths per wave,
+ * spread evenly) are traced in full and leave a record at that vertex whose target is the
+ * radiance they measured from there on; after each wave the cache takes its training steps
+ * (train = 1). Otherwise as tt_render_native (with spread_c < 0 and train = 0 it is
+ * bit-identical to it). */
+tt_status tt_render_cached(tt_renderer *renderer, tt_cache *cache, const tt_camera_meta *cam,
+                           const tt_render_params *params, void *d_accum, int32_t train, void *stream);
+
 #define TT_NOALLOC_MAX_RAYS (1 << 18)
 tt_status tt_trace_host_noalloc(const void *d_nodes, const void *d_vertices, const int32_t *d_tri_indices,
                                 const tt_ray *h_rays, int64_t n, tt_hit *h_hits, int32_t closest,

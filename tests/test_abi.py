@@ -51,7 +51,7 @@ def test_null_arguments_are_rejected():
 
 STRUCTS = {"tt_camera_meta": _lib.CameraMeta, "tt_render_meta": _lib.RenderMeta, "tt_material": _lib.Material,
            "tt_geometry": _lib.Geometry, "tt_render_params": _lib.RenderParams, "tt_bvh_header": _lib.BvhHeader,
-           "tt_launch_shape": _lib.LaunchShape, "tt_view": _lib.View}
+           "tt_launch_shape": _lib.LaunchShape, "tt_view": _lib.View, "tt_cache_params": _lib.CacheParams}
 
 
 def test_struct_layouts_match_the_header(tmp_path):

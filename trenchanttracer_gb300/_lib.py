@@ -71,6 +71,14 @@ class LaunchShape(C.Structure):
         return (self.block, self.stack_shared, self.wave_paths)
 
 
+class CacheParams(C.Structure):
+    """tt_cache_params (include/tt.h)."""
+    _fields_ = [("lr", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float), ("eps", C.c_float),
+                ("ema", C.c_float), ("batch", C.c_int32), ("steps", C.c_int32), ("train_paths", C.c_int32),
+                ("spread_c", C.c_float), ("seed", C.c_uint32), ("use_ema", C.c_int32),
+                ("bbox_lo", C.c_float * 3), ("bbox_hi", C.c_float * 3)]
+
+
 class View(C.Structure):
     """tt_view (include/tt.h): one view of a batched render."""
     _fields_ = [("cam", CameraMeta), ("spp", C.c_int32), ("sample_offset", C.c_int32), ("seed", C.c_uint32),
@@ -129,6 +137,18 @@ SIGNATURES = {
     "tt_batch_graph_kernels": (I32, [P, C.POINTER(I32)]),
     "tt_batch_autotune": (I32, [P, I64, P, P, I32, C.POINTER(I32)]),
     "tt_batch_free": (I32, [P]),
+    "tt_cache_params_default": (I32, [C.POINTER(CacheParams)]),
+    "tt_cache_create": (I32, [C.POINTER(CacheParams), C.POINTER(P)]),
+    "tt_cache_free": (I32, [P]),
+    "tt_cache_param_count": (I32, [C.POINTER(I32)]),
+    "tt_cache_get_weights": (I32, [P, P, I32]),
+    "tt_cache_set_weights": (I32, [P, P]),
+    "tt_cache_encode": (I32, [P, P, I64, P, P]),
+    "tt_cache_infer": (I32, [P, P, I64, P, I32, P]),
+    "tt_cache_gradient": (I32, [P, P, P, I64, P, P, P]),
+    "tt_cache_train": (I32, [P, P, P, I64, I32, P, P]),
+    "tt_cache_steps": (I32, [P, C.POINTER(I32)]),
+    "tt_render_cached": (I32, [P, P, C.POINTER(CameraMeta), C.POINTER(RenderParams), P, I32, P]),
 }
 
 _lib: C.CDLL | None = None

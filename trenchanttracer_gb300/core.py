@@ -288,6 +288,12 @@ class Renderer:
         check(lib().tt_render_native(self._h, C.byref(cam), C.byref(params), C.c_void_p(accum.data_ptr()),
                                      C.c_void_p(stream)))
 
+    def render_cached(self, cache: "Cache", cam: _lib.CameraMeta, params: _lib.RenderParams, accum,
+                      train: bool = True, stream: int = 0) -> None:
+        """The native path tracer with the learned radiance cache (include/tt.h, tt_render_cached)."""
+        check(lib().tt_render_cached(self._h, cache._h, C.byref(cam), C.byref(params), C.c_void_p(accum.data_ptr()),
+                                     int(bool(train)), C.c_void_p(stream)))
+
     def set_launch(self, block: int, stack_shared: int, wave_paths: int) -> None:
         """Launch shape of the native kernels (include/tt.h, tt_launch_shape)."""
         shape = _lib.LaunchShape(int(block), int(stack_shared), int(wave_paths), 0.0)
@@ -368,6 +374,75 @@ class Batch:
     def __del__(self):
         if getattr(self, "_h", None):
             lib().tt_batch_free(self._h)
+            self._h = None
+
+
+class Cache:
+    """The learned radiance cache (include/tt.h, tt_cache_*). Tensors are CUDA torch tensors:
+    records (n, 16) float32, targets (n, 3) float32."""
+
+    def __init__(self, bbox_lo, bbox_hi, **kw):
+        p = _lib.CacheParams()
+        check(lib().tt_cache_params_default(C.byref(p)))
+        p.bbox_lo[:] = [float(x) for x in bbox_lo]
+        p.bbox_hi[:] = [float(x) for x in bbox_hi]
+        for k, v in kw.items():
+            setattr(p, k, v)
+        h = C.c_void_p()
+        check(lib().tt_cache_create(C.byref(p), C.byref(h)))
+        self._h = h
+        self.params = p
+        n = C.c_int32()
+        check(lib().tt_cache_param_count(C.byref(n)))
+        self.num_params = n.value
+
+    def weights(self, which: int = 0) -> np.ndarray:
+        """0: master weights, 1: averaged weights, 2: last gradient (compact [out][in] per layer)."""
+        w = np.empty(self.num_params, np.float32)
+        check(lib().tt_cache_get_weights(self._h, _ptr(w), int(which)))
+        return w
+
+    def set_weights(self, w: np.ndarray) -> None:
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        assert w.size == self.num_params
+        check(lib().tt_cache_set_weights(self._h, _ptr(w)))
+
+    def encode(self, rec):
+        import torch
+        out = torch.empty((rec.shape[0], 160), dtype=torch.bfloat16, device=rec.device)
+        check(lib().tt_cache_encode(self._h, C.c_void_p(rec.data_ptr()), rec.shape[0], C.c_void_p(out.data_ptr()),
+                                    None))
+        return out
+
+    def infer(self, rec, use_ema: bool = False):
+        import torch
+        out = torch.empty((rec.shape[0], 3), dtype=torch.float32, device=rec.device)
+        check(lib().tt_cache_infer(self._h, C.c_void_p(rec.data_ptr()), rec.shape[0], C.c_void_p(out.data_ptr()),
+                                   int(bool(use_ema)), None))
+        return out
+
+    def gradient(self, rec, target) -> tuple[np.ndarray, float]:
+        g = np.empty(self.num_params, np.float32)
+        loss = C.c_float()
+        check(lib().tt_cache_gradient(self._h, C.c_void_p(rec.data_ptr()), C.c_void_p(target.data_ptr()),
+                                      rec.shape[0], _ptr(g), C.byref(loss), None))
+        return g, loss.value
+
+    def train(self, rec, target, steps: int = 1) -> float:
+        loss = C.c_float()
+        check(lib().tt_cache_train(self._h, C.c_void_p(rec.data_ptr()), C.c_void_p(target.data_ptr()), rec.shape[0],
+                                   int(steps), C.byref(loss), None))
+        return loss.value
+
+    @property
+    def steps(self) -> int:
+        n = C.c_int32()
+        check(lib().tt_cache_steps(self._h, C.byref(n)))
+        return n.value
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().tt_cache_free(self._h)
             self._h = None
 
 

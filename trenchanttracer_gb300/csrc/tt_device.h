@@ -36,6 +36,10 @@ struct tt_renderer {
     int launch_block = 128, launch_stack = 16, launch_wave = 1 << 22;
     int occ_trace[3][3] = {};  // resident blocks per SM by (block shape, stack shape); 0 = unknown
     int occ_shade[3] = {};
+    // radiance-cache queries and training records of cached renders
+    void *cache_mem = nullptr;
+    size_t cache_bytes = 0;
+    long long cache_queries = 0, cache_records = 0;
 };
 
 namespace tt {

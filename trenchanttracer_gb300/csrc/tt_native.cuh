@@ -58,6 +58,28 @@ struct PathSoA {
     int *shadow_path;
     float4 *shadow_ray;  // 2 float4 per shadow ray
     float *shadow_val;   // 3 per shadow ray
+    float *a0;           // radiance cache: pixel footprint of the path at its first vertex
+    float *spread;       // radiance cache: running sum of sqrt(t^2 / (pdf cos)) over the bounces
+};
+
+// The radiance cache's side of a render (enabled = 0: the plain tracer).
+struct CacheView {
+    int enabled;
+    int train;                // training paths are selected
+    float spread_c;           // termination threshold (< 0: never)
+    unsigned train_stride;    // a path trains when (stream index + phase) % stride == 0
+    unsigned train_phase;
+    int train_cap;            // capacity of the training records
+    float *q_rec;             // queries: kRec floats per query
+    int *q_path;
+    float *q_beta;            // 3 per query: throughput arriving at the query vertex
+    float *q_rgb;             // 3 per query: the cache's radiance
+    float *t_rec;             // training records
+    int *t_path;
+    float *t_L;               // 3 per record: the path's radiance up to the record vertex
+    float *t_beta;            // 3 per record: throughput arriving at the record vertex
+    float *t_target;          // 3 per record: measured radiance leaving the vertex
+    int *counts;              // [0] queries, [1] training records
 };
 
 struct NativeArgs {
@@ -76,6 +98,7 @@ struct NativeArgs {
     int wave_paths;
     unsigned int *err;
     unsigned long long *stats;  // [0] extension rays, [1] shadow rays, [2] paths
+    CacheView cache;
 };
 
 __device__ __forceinline__ int find_view(const NativeArgs &a, long long g) {

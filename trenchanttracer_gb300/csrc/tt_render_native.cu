@@ -36,6 +36,7 @@
 #include <vector>
 
 #include "tt_native.cuh"
+#include "tt_nrc_host.h"
 
 namespace tt {
 
@@ -43,6 +44,9 @@ using namespace pt;
 
 constexpr int kShadeBlockMax = 256;
 constexpr int kFlagSpecular = 1;  // the last bounce was specular (no light sampling was done)
+constexpr int kFlagTrain = 2;     // a radiance-cache training path
+constexpr int kFlagRecorded = 4;  // the training path has left its record
+constexpr int kFlagsKept = kFlagTrain | kFlagRecorded;  // carried from bounce to bounce
 
 // ---- small helpers ------------------------------------------------------------------------------
 __device__ __forceinline__ int warp_append(int *counter, bool pred) {
@@ -297,6 +301,100 @@ __device__ __forceinline__ BsdfSample bsdf_sample(const MaterialRec &m, const V3
 }
 
 // ---- kernels ------------------------------------------------------------------------------------
+// ---- radiance cache hooks ------------------------------------------------------------------------
+// One slot of `counter` for each currently active lane (one atomic per converged group).
+__device__ __forceinline__ int append_active(int *counter) {
+    const unsigned mask = __activemask();
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(mask) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(counter, __popc(mask));
+    base = __shfl_sync(mask, base, leader);
+    return base + __popc(mask & ((1u << lane) - 1u));
+}
+
+// The feature record of a vertex (layout in tt_nrc.cuh).
+__device__ __forceinline__ void cache_record(float *r, const V3 &p, const V3 &wo, const V3 &n, const MaterialRec &m) {
+    float rough = 0.0f, a0 = 1.0f, a1 = 1.0f, a2 = 1.0f;
+    if (m.kind == MAT_DIFF || m.kind == MAT_GGX || m.kind == MAT_SPEC || m.kind == MAT_COAT) {
+        a0 = m.color[0];
+        a1 = m.color[1];
+        a2 = m.color[2];
+    }
+    if (m.kind == MAT_DIFF) rough = 1.0f;
+    else if (m.kind == MAT_GGX) rough = m.roughness;
+    else if (m.kind == MAT_COAT) rough = 0.5f;
+    float4 *r4 = reinterpret_cast<float4 *>(r);
+    r4[0] = make_float4(p.x, p.y, p.z, wo.x);
+    r4[1] = make_float4(wo.y, wo.z, n.x, n.y);
+    r4[2] = make_float4(n.z, rough, a0, a1);
+    r4[3] = make_float4(a2, (float)m.kind * 0.125f, 0.0f, 0.0f);
+}
+
+// The path-spread heuristic of Mueller et al. 2021 ("Real-time Neural Radiance Caching for Path
+// Tracing"): at its first vertex a path records its pixel footprint a0 = t^2 / (4 pi cos); at
+// vertex n >= 2 its spread is a_n = (sum over the non-specular bounces so far of
+// sqrt(t^2 / (pdf cos)))^2, the running sum kept per path. At the first vertex where
+// a_n > spread_c a0 a training path leaves a record (once) and goes on; any other path leaves a
+// query there and ends (returns true). Records and queries are appended with one atomic per
+// converged group of lanes.
+__device__ __forceinline__ bool cache_vertex(const NativeArgs &a, int i, int depth, int &flags, float last_pdf, float t,
+                                             const V3 &p, const V3 &wo, const V3 &nl, const MaterialRec &m,
+                                             const V3 &beta, const V3 &L) {
+    const float cos_o = fabsf(dot(nl, wo));
+    if (depth == 0) {
+        a.ps.a0[i] = cos_o > 0.0f ? PT_DIV(PT_MUL(t, t), PT_MUL(4.0f * kPi, cos_o)) : 3.0e38f;
+        a.ps.spread[i] = 0.0f;
+        return false;
+    }
+    if (a.cache.spread_c < 0.0f || (flags & kFlagRecorded)) return false;
+    float s_sum = a.ps.spread[i];
+    if (last_pdf > 0.0f && cos_o > 0.0f) s_sum = PT_ADD(s_sum, PT_SQRT(PT_DIV(PT_MUL(t, t), PT_MUL(last_pdf, cos_o))));
+    a.ps.spread[i] = s_sum;
+    if (!(PT_MUL(s_sum, s_sum) > PT_MUL(a.cache.spread_c, a.ps.a0[i]))) return false;
+    if (flags & kFlagTrain) {
+        flags |= kFlagRecorded;
+        const int s = append_active(a.cache.counts + 1);
+        if (s < a.cache.train_cap) {
+            cache_record(a.cache.t_rec + 16ll * s, p, wo, nl, m);
+            a.cache.t_path[s] = i;
+            st3(a.cache.t_L + 3ll * s, L);
+            st3(a.cache.t_beta + 3ll * s, beta);
+        }
+        return false;
+    }
+    const int s = append_active(a.cache.counts + 0);
+    cache_record(a.cache.q_rec + 16ll * s, p, wo, nl, m);
+    a.cache.q_path[s] = i;
+    st3(a.cache.q_beta + 3ll * s, beta);
+    return true;
+}
+
+// Adds throughput x cache radiance of every query to its path.
+__global__ void __launch_bounds__(kShadeBlockMax) k_cache_resolve(NativeArgs a) {
+    const int n = a.cache.counts[0];
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        float *L = a.ps.L + 3ll * a.cache.q_path[q];
+        const float *b = a.cache.q_beta + 3ll * q, *c = a.cache.q_rgb + 3ll * q;
+        L[0] = PT_FMA(b[0], c[0], L[0]);
+        L[1] = PT_FMA(b[1], c[1], L[1]);
+        L[2] = PT_FMA(b[2], c[2], L[2]);
+    }
+}
+
+// Training targets: the radiance each training path measured from its record vertex on.
+__global__ void __launch_bounds__(kShadeBlockMax) k_cache_targets(NativeArgs a) {
+    const int n = min(a.cache.counts[1], a.cache.train_cap);
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+        const float *L = a.ps.L + 3ll * a.cache.t_path[s];
+        for (int c = 0; c < 3; c++) {
+            const float b = a.cache.t_beta[3ll * s + c];
+            const float v = b > 0.0f ? PT_DIV(PT_SUB(L[c], a.cache.t_L[3ll * s + c]), b) : 0.0f;
+            a.cache.t_target[3ll * s + c] = v > 0.0f ? v : 0.0f;
+        }
+    }
+}
+
 __device__ __forceinline__ void put_ray(float4 *rays, int slot, const V3 &o, const V3 &d) {
     rays[2 * slot] = make_float4(o.x, o.y, o.z, d.x);
     rays[2 * slot + 1] = make_float4(d.y, d.z, 0.0f, 1e20f);
@@ -312,6 +410,10 @@ __global__ void __launch_bounds__(kShadeBlockMax) k_raygen(NativeArgs a) {
         a.ps.counts[3] = 0;
         a.ps.counts[4] = 0;
         atomicAdd(a.stats + 2, (unsigned long long)a.wave_paths);
+        if (a.cache.enabled) {
+            a.cache.counts[0] = 0;
+            a.cache.counts[1] = 0;
+        }
     }
     int cached = -1;
     ViewRec vw;
@@ -342,7 +444,8 @@ __global__ void __launch_bounds__(kShadeBlockMax) k_raygen(NativeArgs a) {
         a.ps.rng_inc[i] = rg.inc;
         a.ps.last_pdf[i] = 0.0f;
         a.ps.depth[i] = 0;
-        a.ps.flags[i] = kFlagSpecular;
+        const bool train = a.cache.train && ((unsigned long long)gid + a.cache.train_phase) % a.cache.train_stride == 0;
+        a.ps.flags[i] = kFlagSpecular | (train ? kFlagTrain : 0);
         a.ps.queue[0][i] = i;
     }
 }
@@ -372,7 +475,7 @@ __global__ void __launch_bounds__(kShadeBlockMax) k_shade(NativeArgs a, int cur)
             const V3 o(r0.x, r0.y, r0.z), d(r0.w, r1.x, r1.y);
             V3 beta = ld3(a.ps.beta + 3ll * i), L = ld3(a.ps.L + 3ll * i);
             const int prim = a.ps.hit_prim[q];
-            const int flags = a.ps.flags[i];
+            int flags = a.ps.flags[i];
             const float last_pdf = a.ps.last_pdf[i];
             int depth = a.ps.depth[i];
             if (prim == -1) {
@@ -419,7 +522,9 @@ __global__ void __launch_bounds__(kShadeBlockMax) k_shade(NativeArgs a, int cur)
                 }
                 L = V3(PT_FMA(beta.x, m.emission[0], L.x), PT_FMA(beta.y, m.emission[1], L.y),
                        PT_FMA(beta.z, m.emission[2], L.z));
-                const bool nee = use_env && !(a.p.flags & TT_RENDER_NO_ENV_SAMPLING) &&
+                bool cache_end = false;
+                if (a.cache.enabled) cache_end = cache_vertex(a, i, depth, flags, last_pdf, t, p, wo, nl, m, beta, L);
+                const bool nee = !cache_end && use_env && !(a.p.flags & TT_RENDER_NO_ENV_SAMPLING) &&
                                  (m.kind == MAT_DIFF || m.kind == MAT_GGX);
                 const float eps = ray_eps(a, p);
                 if (nee) {
@@ -438,9 +543,10 @@ __global__ void __launch_bounds__(kShadeBlockMax) k_shade(NativeArgs a, int cur)
                         }
                     }
                 }
-                const float u1 = uniform(g), u2 = uniform(g), u3 = uniform(g);
+                const float u1 = cache_end ? 0.0f : uniform(g), u2 = cache_end ? 0.0f : uniform(g),
+                            u3 = cache_end ? 0.0f : uniform(g);
                 const BsdfSample bs = bsdf_sample(m, nl, wo, entering, u1, u2, u3);
-                if (maxc(bs.weight) > 0.0f) {
+                if (!cache_end && maxc(bs.weight) > 0.0f) {
                     beta = mul(beta, bs.weight);
                     depth++;
                     alive = depth < a.p.max_depth;
@@ -456,7 +562,7 @@ __global__ void __launch_bounds__(kShadeBlockMax) k_shade(NativeArgs a, int cur)
                         next_d = bs.wi;
                         st3(a.ps.beta + 3ll * i, beta);
                         a.ps.last_pdf[i] = bs.pdf;
-                        a.ps.flags[i] = (bs.specular || !nee) ? kFlagSpecular : 0;
+                        a.ps.flags[i] = (flags & kFlagsKept) | ((bs.specular || !nee) ? kFlagSpecular : 0);
                         a.ps.depth[i] = depth;
                     }
                 }
@@ -575,27 +681,31 @@ void native_release(tt_renderer *r) {
     if (r->env_marg) cudaFree(r->env_marg);
     if (r->env_cond) cudaFree(r->env_cond);
     if (r->paths) cudaFree(r->paths);
+    if (r->cache_mem) cudaFree(r->cache_mem);
     r->env_marg = r->env_cond = nullptr;
     r->paths = nullptr;
     r->paths_bytes = 0;
     r->path_capacity = 0;
+    r->cache_mem = nullptr;
+    r->cache_bytes = 0;
 }
 
 // Path state for `cap` paths, carved out of one allocation sized for the renderer's capacity (so
 // the pointers, which captured graphs hold, change only when the allocation does).
 static tt_status ensure_paths(tt_renderer *r, int cap, PathSoA &ps) {
     auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+    constexpr int kArrays = 21;
     auto layout = [&](size_t n, size_t *sizes) {
-        const size_t s[] = {12 * n, 12 * n, 8 * n, 8 * n, 4 * n, 4 * n, 4 * n, 4 * n, 4 * n, 32 * n, 32 * n,
-                            4 * n,  4 * n,  4 * n, 4 * n, 64,    4 * n, 32 * n, 12 * n};
+        const size_t s[kArrays] = {12 * n, 12 * n, 8 * n, 8 * n,  4 * n,  4 * n, 4 * n, 4 * n, 4 * n, 32 * n, 32 * n,
+                                   4 * n,  4 * n,  4 * n, 4 * n, 64,     4 * n, 32 * n, 12 * n, 4 * n, 4 * n};
         size_t total = 0;
-        for (int i = 0; i < 19; i++) {
+        for (int i = 0; i < kArrays; i++) {
             sizes[i] = s[i];
             total += al(s[i]);
         }
         return total;
     };
-    size_t sizes[19];
+    size_t sizes[kArrays];
     if (r->path_capacity < cap || !r->paths) {
         const size_t total = layout((size_t)cap, sizes);
         if (r->paths) cudaFree(r->paths);
@@ -610,8 +720,8 @@ static tt_status ensure_paths(tt_renderer *r, int cap, PathSoA &ps) {
     }
     layout((size_t)r->path_capacity, sizes);
     char *p = static_cast<char *>(r->paths);
-    void *v[19];
-    for (int i = 0; i < 19; i++) {
+    void *v[kArrays];
+    for (int i = 0; i < kArrays; i++) {
         v[i] = p;
         p += al(sizes[i]);
     }
@@ -634,6 +744,8 @@ static tt_status ensure_paths(tt_renderer *r, int cap, PathSoA &ps) {
     ps.shadow_path = (int *)v[16];
     ps.shadow_ray = (float4 *)v[17];
     ps.shadow_val = (float *)v[18];
+    ps.a0 = (float *)v[19];
+    ps.spread = (float *)v[20];
     return TT_OK;
 }
 
@@ -740,24 +852,81 @@ static NativeArgs base_args(tt_renderer *r, const tt_render_params &p, const Pat
 }
 
 // Issues the kernels of `total` paths (waves of L.wave) on stream s. accum = nullptr: no
-// accumulation (autotuning trials).
-static tt_status issue(NativeArgs a, long long total, const Launch &L, void *accum, cudaStream_t s) {
+// accumulation (autotuning trials). cache: the radiance cache of a cached render (a.cache set up),
+// queried after the second bounce and trained after every wave when `train`.
+static tt_status issue(NativeArgs a, long long total, const Launch &L, void *accum, cudaStream_t s,
+                       tt_cache *cache = nullptr, bool train = false) {
     const bool f64 = (a.p.flags & TT_RENDER_ACCUM_F64) != 0;
     for (long long done = 0; done < total; done += L.wave) {
         a.wave_first = done;
         a.wave_paths = (int)std::min<long long>(total - done, L.wave);
+        if (cache) {
+            const long long tp = nrc::cache_params(cache).train_paths;
+            a.cache.train_stride = (unsigned)std::max<long long>(1, (a.wave_paths + tp - 1) / tp);
+            a.cache.train_phase = (unsigned)((a.view0.stream0 / std::max(1, a.view0.npix) + done) * 7 %
+                                             a.cache.train_stride);
+        }
         k_raygen<<<L.grid_shade, L.block, 0, s>>>(a);
         for (int b = 0; b < a.p.max_depth; b++) {
             L.tk.extend<<<L.grid_trace, L.block, 0, s>>>(a, b & 1);
             k_shade<<<L.grid_shade, L.block, 0, s>>>(a, b & 1);
             L.tk.shadow<<<L.grid_trace, L.block, 0, s>>>(a);
         }
+        if (cache) {  // every path queries at most once, so all queries of the wave fit
+            const tt_status st = nrc::cache_infer_device(cache, a.cache.q_rec, a.cache.counts, a.wave_paths,
+                                                         a.cache.q_rgb, nrc::cache_params(cache).use_ema, s);
+            if (st != TT_OK) return st;
+            k_cache_resolve<<<L.grid_shade, L.block, 0, s>>>(a);
+        }
+        if (cache && train) k_cache_targets<<<L.grid_shade, L.block, 0, s>>>(a);
         if (accum) {
             if (f64) k_accumulate<double><<<L.grid_shade, L.block, 0, s>>>(a, (double *)accum);
             else k_accumulate<float><<<L.grid_shade, L.block, 0, s>>>(a, (float *)accum);
         }
+        if (cache && train) {
+            const tt_status st = nrc::cache_train_device(cache, a.cache.t_rec, a.cache.t_target, a.cache.counts + 1, s);
+            if (st != TT_OK) return st;
+        }
     }
     TT_CUDA_N(cudaGetLastError());
+    return TT_OK;
+}
+
+// Query and training buffers of a cached render: `queries` query slots, `records` training slots.
+static tt_status ensure_cache_buffers(tt_renderer *r, long long queries, long long records, CacheView &cv) {
+    auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+    const size_t q = (size_t)queries, t = (size_t)records;
+    const size_t sizes[] = {64 * q, 4 * q, 12 * q, 12 * q, 64 * t, 4 * t, 12 * t, 12 * t, 12 * t, 256};
+    size_t total = 0;
+    for (size_t s : sizes) total += al(s);
+    if (r->cache_bytes < total || r->cache_queries < queries || r->cache_records < records) {
+        if (r->cache_mem) cudaFree(r->cache_mem);
+        r->cache_mem = nullptr;
+        r->cache_bytes = 0;
+        cudaError_t e = cudaMalloc(&r->cache_mem, total);
+        if (e != cudaSuccess) return fail(TT_ERR_OOM, std::string("cache buffers: ") + cudaGetErrorString(e));
+        r->cache_bytes = total;
+        r->cache_queries = queries;
+        r->cache_records = records;
+    }
+    char *p = static_cast<char *>(r->cache_mem);
+    int k = 0;
+    auto take = [&]() {
+        char *x = p;
+        p += al(sizes[k++]);
+        return x;
+    };
+    cv.q_rec = (float *)take();
+    cv.q_path = (int *)take();
+    cv.q_beta = (float *)take();
+    cv.q_rgb = (float *)take();
+    cv.t_rec = (float *)take();
+    cv.t_path = (int *)take();
+    cv.t_L = (float *)take();
+    cv.t_beta = (float *)take();
+    cv.t_target = (float *)take();
+    cv.counts = (int *)take();
+    cv.train_cap = (int)records;
     return TT_OK;
 }
 
@@ -835,6 +1004,35 @@ tt_status tt_render_native(tt_renderer *r, const tt_camera_meta *cam, const tt_r
     a.n_views = 1;
     a.view0 = v;
     return issue(a, v.paths, L, d_accum, (cudaStream_t)stream);
+}
+
+tt_status tt_render_cached(tt_renderer *r, tt_cache *c, const tt_camera_meta *cam, const tt_render_params *p,
+                           void *d_accum, int32_t train, void *stream) {
+    if (!r || !c || !cam || !p || !d_accum) return fail(TT_ERR_INVALID, "null argument");
+    tt_status st = check_view(*cam, p->spp, p->sample_offset);
+    if (st == TT_OK) st = check_params(*p);
+    if (st != TT_OK) return st;
+    const tt_cache_params &cp = nrc::cache_params(c);
+    const ViewRec v = make_view(*cam, p->spp, p->sample_offset, p->seed, 0, 0);
+    Launch L;
+    st = resolve_launch(r, r->launch_block, r->launch_stack, r->launch_wave, L);
+    if (st != TT_OK) return st;
+    const int wave = (int)std::min<long long>(v.paths, L.wave);
+    PathSoA ps;
+    st = ensure_paths(r, wave, ps);
+    if (st != TT_OK) return st;
+    NativeArgs a = base_args(r, *p, ps);
+    a.views = nullptr;
+    a.n_views = 1;
+    a.view0 = v;
+    const long long records = std::max<long long>(cp.train_paths, (long long)cp.steps * cp.batch);
+    st = ensure_cache_buffers(r, wave, records, a.cache);
+    if (st != TT_OK) return st;
+    a.cache.enabled = 1;
+    a.cache.train = train ? 1 : 0;
+    a.cache.spread_c = cp.spread_c;
+    a.cache.train_stride = 1;
+    return issue(a, v.paths, L, d_accum, (cudaStream_t)stream, c, train != 0);
 }
 
 tt_status tt_renderer_set_launch(tt_renderer *r, const tt_launch_shape *shape) {
