@@ -18,7 +18,18 @@ timed steps, outside the timed region.
   cpu_baseline  the reference's traversal restated in C (oracle/, plain float arithmetic like
             the reference's host build) under OpenMP on all host cores, on a sample of the rays
 
-Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+Other workloads (--workload; one JSON line each, same keys):
+  cornell        unit Cornell box + displaced subdivision-5 icosphere (20,492 tris), 512 x 512,
+                 16 spp, depth 8, Russian roulette from 4: Msamples/s of the native path tracer
+  multimaterial  400 displaced subdivision-5 icospheres (8,192,002 tris) with Lambert / GGX /
+                 dielectric materials under a 2048 x 1024 sky with a 0.5 degree sun of 5e4,
+                 1920 x 1080, 64 spp, depth 16: Msamples/s
+  batch          64 orbit views of the terrain (sizes 256^2..1024^2, 4/16/64 spp) as one
+                 graph-captured batch with an autotuned launch shape, against 64 sequential renders
+  cache          time to relMSE 0.01 against a 16,384-spp FP64 render, plain tracer versus the
+                 learned radiance cache (multimaterial scene; --cache-scene terrain for the terrain)
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload W]
 Multi-GPU (torchrun): every rank is an independent replica tracing its own rays (weak scaling).
 """
 from __future__ import annotations
@@ -307,21 +318,359 @@ def run_ours(args) -> None:
         dist.destroy_process_group()
 
 
+# ---- path-tracing workloads ----------------------------------------------------------------------
+RENDER_CONFIGS = {
+    "cornell": dict(desc="Cornell box (10 wall tris + 0.25 x 0.25 ceiling light 17,12,4) + subdivision-5 "
+                         "icosphere r 0.3 (seed-42 noise 0.03, Lambert 0.8), 20,492 tris; 512 x 512, 16 spp, "
+                         "depth 8, Russian roulette from 4, PCG32", width=512, height=512, spp=16, depth=8),
+    "multimaterial": dict(desc="400 displaced subdivision-5 icospheres (8,192,002 tris incl. ground), Lambert / "
+                               "GGX / dielectric 1.5; 2048 x 1024 sky with a 0.5-degree sun of 5e4, 2D-CDF light "
+                               "sampling with MIS; 1920 x 1080, 64 spp, depth 16, Russian roulette from 4",
+                          width=1920, height=1080, spp=64, depth=16),
+}
+
+
+def render_scene(name: str, width: int, height: int):
+    """(Scene, mesh, tt_camera_meta) of a path-tracing workload."""
+    import math
+    from trenchanttracer_gb300 import Scene, make_camera_meta, scenes
+    if name == "cornell":
+        mesh = scenes.cornell(5)
+        sc = Scene.from_mesh(mesh)
+        cam = make_camera_meta(width, height, [0.0, 0.0, 1.55], [0.0, 0.0, -1.0], fov=(45.0, 45.0))
+    elif name == "multimaterial":
+        mesh = scenes.multi_material(400, 5)
+        sc = Scene.from_mesh(mesh)
+        sc.set_env(scenes.sky_env(2048, 1024, sun_radiance=5e4, sun_diameter_deg=0.5))
+        fy = 2.0 * math.degrees(math.atan(math.tan(math.radians(30.0)) * height / width))
+        cam = make_camera_meta(width, height, [0.0, 14.0, 34.0], [0.0, -12.0, -34.0], fov=(60.0, fy))
+    elif name == "terrain":
+        mesh = scenes.terrain(N_CELLS, SCALE)
+        sc = Scene.from_mesh(mesh)
+        sc.set_env(scenes.sky_env(2048, 1024, sun_radiance=5e4, sun_diameter_deg=0.5))
+        c = scenes.terrain_camera(SCALE)
+        eye, tgt = np.array(c["eye"]), np.array(c["target"])
+        fx = 2.0 * math.degrees(math.atan(c["tan_half_fov"]))
+        fy = 2.0 * math.degrees(math.atan(c["tan_half_fov"] * height / width))
+        cam = make_camera_meta(width, height, list(eye), list(tgt - eye), fov=(fx, fy))
+    else:
+        raise ValueError(name)
+    return sc, mesh, cam
+
+
+def render_cpu_baseline(bvh, sc, cam, spp: int, depth: int, budget_s: float = 15.0) -> dict:
+    """The oracle's C restatement of the native path tracer (OpenMP, all host cores) on a
+    reduced-resolution image of the same view: paths per second."""
+    import ctypes as C
+    from oracle import oracle
+    from trenchanttracer_gb300 import _lib, make_camera_meta, render_params
+    mats, geos = sc.materials_raw(), sc.geometries_raw()
+    mats = (_lib.Material * len(mats))(*mats)
+    geos = (_lib.Geometry * len(geos))(*geos)
+    env = sc.env()
+    arr = bvh.arrays()
+    threads = oracle.max_threads()
+    scale, out = 16, None
+    while True:
+        w, h = max(8, cam.width // scale), max(8, cam.height // scale)
+        small = make_camera_meta(w, h, list(cam.position), list(cam.view), list(cam.up), tuple(cam.fov))
+        p = render_params(spp=spp, max_depth=depth, rr_depth=4, seed=1)
+        tx = float(np.float32(np.tan(np.radians(cam.fov[0]) / 2)))
+        ty = float(np.float32(np.tan(np.radians(cam.fov[1]) / 2)))
+        t0 = time.perf_counter()
+        oracle.render_native(arr, mats, geos, env, small, p, tx, ty, threads=threads)
+        dt = time.perf_counter() - t0
+        out = {"paths_per_s": w * h * spp / dt, "seconds": dt, "threads": threads, "sample": f"{w}x{h} x {spp} spp"}
+        if dt > budget_s / 4 or scale == 1:
+            return out
+        scale //= 2
+
+
+def run_render(args) -> None:
+    """Native path tracer on one of RENDER_CONFIGS: a step = one render of the configured image
+    and sample count."""
+    import torch
+    from trenchanttracer_gb300 import BVHCompact, DeviceBVH, Renderer, render_params
+    cfg = RENDER_CONFIGS[args.workload]
+    dev = torch.device("cuda", 0)
+    sc, mesh, cam = render_scene(args.workload, cfg["width"], cfg["height"])
+    t0 = time.perf_counter()
+    bvh = BVHCompact.build(sc, 1e-5, 1, 8)
+    build_s = time.perf_counter() - t0
+    r = Renderer(DeviceBVH(bvh), sc)
+    npx = cfg["width"] * cfg["height"] * 3
+    acc = torch.zeros(npx, dtype=torch.float32, device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    params = lambda k: render_params(spp=cfg["spp"], sample_offset=k * cfg["spp"], max_depth=cfg["depth"], rr_depth=4,
+                                     seed=1)
+    for k in range(args.warmup):
+        r.render_native(cam, params(k), acc, stream=stream.cuda_stream)
+    torch.cuda.synchronize(dev)
+    r.check()
+    r.stats(reset=True)
+    ms = []
+    with Clocks(0) as clk:
+        for k in range(args.steps):
+            flush.fill_(1)
+            e0, e1 = torch.cuda.Event(True), torch.cuda.Event(True)
+            e0.record(stream)
+            r.render_native(cam, params(args.warmup + k), acc, stream=stream.cuda_stream)
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            ms.append(e0.elapsed_time(e1))
+    r.check()
+    st = r.stats(reset=True)
+    mean_ms = float(np.mean(ms))
+    paths = cfg["width"] * cfg["height"] * cfg["spp"]
+    rays = (st["extension_rays"] + st["shadow_rays"]) / args.steps
+    # end to end: the render call plus the read of the image into page-locked host memory
+    host = torch.empty(npx, dtype=torch.float32).pin_memory()
+    e2e = []
+    for k in range(args.steps):
+        flush.fill_(1)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        r.render_native(cam, params(k), acc, stream=stream.cuda_stream)
+        host.copy_(acc, non_blocking=True)
+        torch.cuda.synchronize(dev)
+        e2e.append((time.perf_counter() - t0) * 1e3)
+    img = host.numpy()
+    assert np.isfinite(img).all()
+    cpu = render_cpu_baseline(bvh, sc, cam, cfg["spp"], cfg["depth"])
+    launches = args.steps * (1 + 3 * cfg["depth"] + 1) * -(-paths // r.launch[2])
+    line = {
+        "metric": f"Msamples/s native path tracer ({args.workload})", "value": round(paths / mean_ms / 1e3, 2),
+        "unit": "Msamples/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(mean_ms, 3), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded procedural scene)",
+        "config": {"workload": cfg["desc"], "tris": int(mesh.num_tris), "bvh_build_s": round(build_s, 2),
+                   "launch_shape": list(r.launch), "l2": "L2 flushed (256 MB write) between steps, untimed"},
+        "mrays_per_s": round(rays / mean_ms / 1e3, 1),
+        "rays_per_step": {"extension": st["extension_rays"] // args.steps, "shadow": st["shadow_rays"] // args.steps},
+        "e2e": {"value": round(paths / float(np.mean(e2e)) / 1e3, 2), "unit": "Msamples/s",
+                "h2d_bytes_per_step": 0, "d2h_bytes_per_step": int(npx * 4)},
+        "cpu_baseline": {"value": round(cpu["paths_per_s"] / 1e6, 4), "unit": "Msamples/s", "cores": cpu["threads"],
+                         "kind": "port", "sample": cpu["sample"] + f", {cpu['seconds']:.1f} s (same view)"},
+        "clocks": clk.summary(),
+        "gpu_launches": int(launches),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_batch(args) -> None:
+    """64 uneven orbit views of the terrain: one graph-captured batch versus 64 sequential renders."""
+    import torch
+    from trenchanttracer_gb300 import Batch, BVHCompact, DeviceBVH, Renderer, render_params, scenes
+    dev = torch.device("cuda", 0)
+    sc, mesh, _ = render_scene("terrain", 64, 64)
+    r = Renderer(DeviceBVH(BVHCompact.build(sc, 1e-5, 1, 8)), sc)
+    views = scenes.orbit_views(64)
+    P = dict(max_depth=8, rr_depth=4)
+    b = Batch(r, views, render_params(**P))
+    t0 = time.perf_counter()
+    trials = b.autotune()
+    tune_s = time.perf_counter() - t0
+    acc = torch.zeros(b.accum_elems, dtype=torch.float32, device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(args.warmup):
+        b.render(acc, stream=stream.cuda_stream)
+    torch.cuda.synchronize(dev)
+    r.check()
+    r.stats(reset=True)
+    ms = []
+    with Clocks(0) as clk:
+        for _ in range(args.steps):
+            flush.fill_(1)
+            e0, e1 = torch.cuda.Event(True), torch.cuda.Event(True)
+            e0.record(stream)
+            b.render(acc, stream=stream.cuda_stream)
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            ms.append(e0.elapsed_time(e1))
+    r.check()
+    st = r.stats(reset=True)
+    accs = [torch.zeros(c.width * c.height * 3, dtype=torch.float32, device=dev) for c, *_ in views]
+    seq = []
+    for k in range(max(1, args.steps // 2)):
+        flush.fill_(1)
+        e0, e1 = torch.cuda.Event(True), torch.cuda.Event(True)
+        e0.record(stream)
+        for (cam, spp, off, seed), a in zip(views, accs):
+            r.render_native(cam, render_params(spp=spp, sample_offset=off, seed=seed, **P), a,
+                            stream=stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        seq.append(e0.elapsed_time(e1))
+    host = torch.empty(b.accum_elems, dtype=torch.float32).pin_memory()
+    e2e = []
+    for _ in range(args.steps):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        b.render(acc, stream=stream.cuda_stream)
+        host.copy_(acc, non_blocking=True)
+        torch.cuda.synchronize(dev)
+        e2e.append((time.perf_counter() - t0) * 1e3)
+    mean_ms = float(np.mean(ms))
+    rays = (st["extension_rays"] + st["shadow_rays"]) / args.steps
+    line = {
+        "metric": "Msamples/s batched uneven renders (64 views, one graph launch)",
+        "value": round(b.total_paths / mean_ms / 1e3, 2), "unit": "Msamples/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(mean_ms, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded terrain and orbit poses)",
+        "config": {"workload": "64 orbit views of the terrain (2,097,152 tris, sky + sun), sizes from "
+                               "{256,512,768,1024}^2, spp from {4,16,64}, depth 8, RR from 4",
+                   "paths_per_step": b.total_paths, "graph_kernels": b.graph_kernels,
+                   "launch_shape": list(r.launch), "autotune_s": round(tune_s, 2), "autotune_trials": len(trials),
+                   "l2": "L2 flushed (256 MB write) between steps, untimed"},
+        "sequential": {"value": round(b.total_paths / float(np.mean(seq)) / 1e3, 2), "unit": "Msamples/s",
+                       "ms_per_step": round(float(np.mean(seq)), 3), "how": "64 tt_render_native calls"},
+        "mrays_per_s": round(rays / mean_ms / 1e3, 1),
+        "e2e": {"value": round(b.total_paths / float(np.mean(e2e)) / 1e3, 2), "unit": "Msamples/s",
+                "h2d_bytes_per_step": 0, "d2h_bytes_per_step": int(b.accum_elems * 4)},
+        "clocks": clk.summary(),
+        "gpu_launches": args.steps * b.graph_kernels,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_cache(args) -> None:
+    """Time to relMSE 0.01 against an FP64 reference of args.ref_spp samples (rendered as two
+    independent halves, whose disagreement measures the reference's own error), plain native
+    tracer versus the tracer with the learned radiance cache, both at 1 spp per frame, time from
+    CUDA events around each frame (training included), error evaluated between frames."""
+    import torch
+    from trenchanttracer_gb300 import BVHCompact, Cache, DeviceBVH, Renderer, render_params
+    dev = torch.device("cuda", 0)
+    W, H = args.width, args.height
+    sc, mesh, cam = render_scene(args.cache_scene, W, H)
+    r = Renderer(DeviceBVH(BVHCompact.build(sc, 1e-5, 1, 8)), sc)
+    npx = W * H * 3
+    D = dict(max_depth=16, rr_depth=4)
+    half = args.ref_spp // 2
+    t0 = time.perf_counter()
+    halves = []
+    for hlf in range(2):
+        a = torch.zeros(npx, dtype=torch.float64, device=dev)
+        for k in range(0, half, 256):
+            n = min(256, half - k)
+            r.render_native(cam, render_params(spp=n, sample_offset=hlf * half + k, seed=777, flags=1, **D), a)
+        halves.append(a.view(-1, 3) / half)
+    torch.cuda.synchronize(dev)
+    r.check()
+    ref_s = time.perf_counter() - t0
+    ref = (halves[0] + halves[1]) / 2
+    den = ref * ref + 1e-2
+
+    def relmse(x):
+        return float((((x - ref) ** 2) / den).sum(1).mean().item())
+
+    a_, b_ = halves
+    floor = float((((a_ - b_) ** 2) / (0.5 * (a_ * a_ + b_ * b_) + 1e-2)).sum(1).mean().item()) / 4.0
+    evals = sorted({1, 2, 4, 8, 16, 32, 64, 96, 128, 192, 256, 384, 512, 768, 1024, 1536, 2048, 3072, 4096})
+
+    def run(step_fn):
+        acc = torch.zeros(npx, dtype=torch.float32, device=dev)
+        total, curve, hit = 0.0, [], None
+        for f in range(args.max_frames):
+            e0, e1 = torch.cuda.Event(True), torch.cuda.Event(True)
+            e0.record()
+            step_fn(f, acc)
+            e1.record()
+            e1.synchronize()
+            total += e0.elapsed_time(e1) / 1e3
+            if f + 1 in evals or f + 1 == args.max_frames:
+                v = relmse(acc.view(-1, 3).double() / (f + 1))
+                curve.append([f + 1, round(total, 4), round(v, 5)])
+                if hit is None and v <= 0.01:
+                    hit = [f + 1, round(total, 4)]
+            if total > args.max_seconds:
+                v = relmse(acc.view(-1, 3).double() / (f + 1))
+                curve.append([f + 1, round(total, 4), round(v, 5)])
+                break
+        r.check()
+        return hit, curve
+
+    with Clocks(0) as clk:
+        plain = run(lambda f, acc: r.render_native(cam, render_params(spp=1, sample_offset=f, seed=1, **D), acc))
+        lo, hi = mesh.vertices.min(0) - 0.5, mesh.vertices.max(0) + 0.5
+        cache = Cache(lo, hi)
+        cached = run(lambda f, acc: r.render_cached(cache, cam, render_params(spp=1, sample_offset=f, seed=1, **D),
+                                                    acc, train=True))
+
+    def time_to(curve, level):
+        """Time after which the error stays at or below `level`: the last crossing from above,
+        interpolated linearly in log error (None if the curve ends above it)."""
+        above = [i for i, c in enumerate(curve) if c[2] > level]
+        if not above:
+            return curve[0][1]
+        i = above[-1]
+        if i == len(curve) - 1:
+            return None
+        (_, t0_, e0), (_, t1, e1) = curve[i], curve[i + 1]
+        return t0_ + (t1 - t0_) * (np.log(e0) - np.log(level)) / (np.log(e0) - np.log(e1))
+
+    t_plain, t_cached = time_to(plain[1], 0.01), time_to(cached[1], 0.01)
+    final_plain = plain[1][-1]
+    t_equal = time_to(cached[1], final_plain[2])
+    line = {
+        "metric": "time to relMSE 0.01, cached vs plain tracer", "value": None if t_cached is None else round(t_cached, 3),
+        "unit": "s", "n_gpus": 1, "steps": len(cached[1]), "warmup": 0, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (MLP bf16, fp32 accumulation)",
+        "data": "synthetic (seeded procedural scene)",
+        "config": {"workload": f"{args.cache_scene} {W}x{H}, depth 16, RR from 4, 1 spp per frame; cache MLP "
+                               "160-64x5-3, 65,536 training paths per frame, 4 Adam steps of 16,384, lr 1e-2",
+                   "relmse": "mean over pixels of sum_c (x - r)^2 / (r^2 + 0.01)",
+                   "reference": f"{args.ref_spp} spp FP64 accumulation ({ref_s:.1f} s)"},
+        "plain": {"time_to_0.01_s": None if t_plain is None else round(t_plain, 3), "curve": plain[1]},
+        "cached": {"time_to_0.01_s": None if t_cached is None else round(t_cached, 3), "curve": cached[1],
+                   "adam_steps": cache.steps},
+        "time_ratio_cached_over_plain": None if (t_plain is None or t_cached is None) else round(t_cached / t_plain, 3),
+        "reference_error": {"relmse_vs_truth_estimate": round(floor, 5),
+                            "how": "relMSE between the two independent halves / 4"},
+        "equal_error": {"plain_error": final_plain[2], "plain_s": final_plain[1],
+                        "cached_s_to_same_error": None if t_equal is None else round(float(t_equal), 3),
+                        "ratio": None if t_equal is None else round(float(t_equal) / final_plain[1], 3)},
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["terrain", "cornell", "multimaterial", "batch", "cache"], default="terrain")
+    ap.add_argument("--cache-scene", choices=["multimaterial", "terrain"], default="multimaterial")
+    ap.add_argument("--width", type=int, default=1920)
+    ap.add_argument("--height", type=int, default=1080)
+    ap.add_argument("--ref-spp", type=int, default=16384)
+    ap.add_argument("--max-frames", type=int, default=4096)
+    ap.add_argument("--max-seconds", type=float, default=60.0)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     from trenchanttracer_gb300 import build
     build.build()
     if args.impl == "reference":
+        if args.workload != "terrain":
+            if int(os.environ.get("RANK", "0")) == 0:
+                print(json.dumps({"impl": "reference", "unavailable": "the reference arm is defined for the terrain "
+                                  "ray-cast workload; the path-tracing workloads report the oracle port as "
+                                  "cpu_baseline"}), flush=True)
+            return
         run_reference(args)
-    else:
+    elif args.workload == "terrain":
         run_ours(args)
+    elif args.workload in RENDER_CONFIGS:
+        run_render(args)
+    elif args.workload == "batch":
+        run_batch(args)
+    else:
+        run_cache(args)
 
 
 if __name__ == "__main__":
