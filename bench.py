@@ -28,6 +28,8 @@ Other workloads (--workload; one JSON line each, same keys):
                  graph-captured batch with an autotuned launch shape, against 64 sequential renders
   cache          time to relMSE 0.01 against a 16,384-spp FP64 render, plain tracer versus the
                  learned radiance cache (multimaterial scene; --cache-scene terrain for the terrain)
+  mlp            the radiance cache's BF16 tensor-core kernels alone (inference on 2^21 records,
+                 one frame's training): TFLOP/s against the measured BF16 peak
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload W]
 Multi-GPU (torchrun): every rank is an independent replica tracing its own rays (weak scaling).
@@ -54,6 +56,10 @@ WIDTH = 2048
 METRIC = "Mrays/s closest-hit; time to relMSE 0.01, cached vs plain tracer, 1 GB300"
 UNIT = "Mrays/s"
 L2_FLUSH_BYTES = 256 << 20
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one trace launch of this workload,
+# the mean of the four launches ncu captured of `bench.py --steps 2 --warmup 3` on a GB300
+# (incoherent 0.935 GB, primary 0.292 GB per launch); bench.py cannot run ncu itself.
+TRACE_DRAM_BYTES_PER_LAUNCH = 613_200_000
 
 
 def load_peaks() -> dict:
@@ -303,7 +309,9 @@ def run_ours(args) -> None:
         "e2e": {"value": round(e2e_val, 2), "unit": UNIT, "h2d_bytes_per_step": int(n_rays * 32),
                 "d2h_bytes_per_step": int(n_rays * 8)},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                     "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": None,
+                     "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": TRACE_DRAM_BYTES_PER_LAUNCH,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per trace launch of this "
+                                       "workload (mean of the primary and incoherent launches)",
                      "peak_source": f"{peaks['source']} hbm_gbs (MEASURED_PEAKS.json)" if peaks["source"] == "measured"
                      else "fallback 6.8 TB/s", "bytes_per_ray": round(bpr, 1),
                      "kernel": "trace_kernel<closest> (avg launch)", "avg_launch_ms": round(float(kernel_ms), 4)},
@@ -637,13 +645,70 @@ def run_cache(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+MLP_MACS = 160 * 64 + 4 * 64 * 64 + 64 * 8  # multiply-adds per row of one forward pass (padded output)
+
+
+def run_mlp(args) -> None:
+    """The radiance cache's tensor-core kernels alone: inference on 2^21 records and one frame's
+    training (steps x batch rows; forward, backward and weight gradients = 3 forward's worth of
+    multiply-adds) on random records, in TFLOP/s against the measured dense BF16 peak."""
+    import torch
+    from trenchanttracer_gb300 import Cache
+    dev = torch.device("cuda", 0)
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = float(peaks.get("bf16_tflops", 1900.0))
+    g = torch.Generator(device=dev).manual_seed(5)
+    n = 1 << 21
+    rec = torch.rand((n, 16), generator=g, device=dev) * 2 - 1
+    rec[:, 9:13] = rec[:, 9:13].abs()
+    tgt = torch.rand((n, 3), generator=g, device=dev) + 0.1
+    cache = Cache([-1.0] * 3, [1.0] * 3)
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(args.warmup):
+        cache.infer(rec)
+        cache.train(rec[:65536], tgt[:65536], steps=4)
+    torch.cuda.synchronize(dev)
+    inf_ms, tr_ms = [], []
+    with Clocks(0) as clk:
+        for _ in range(args.steps):
+            e0, e1, e2 = (torch.cuda.Event(True) for _ in range(3))
+            e0.record(stream)
+            out = cache.infer(rec)
+            e1.record(stream)
+            cache.train(rec[:65536], tgt[:65536], steps=4)
+            e2.record(stream)
+            torch.cuda.synchronize(dev)
+            inf_ms.append(e0.elapsed_time(e1))
+            tr_ms.append(e1.elapsed_time(e2))
+    assert torch.isfinite(out).all()
+    inf = float(np.median(inf_ms))
+    tr = float(np.median(tr_ms))
+    inf_tf = 2.0 * MLP_MACS * n / (inf * 1e-3) / 1e12
+    tr_tf = 3 * 2.0 * MLP_MACS * 65536 / (tr * 1e-3) / 1e12
+    line = {
+        "metric": "radiance-cache MLP inference TFLOP/s (BF16 tensor cores, FP32 accumulation)",
+        "value": round(inf_tf, 2), "unit": "TFLOP/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(inf, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "bf16 (fp32 accumulation)", "data": "synthetic (random feature records)",
+        "config": {"workload": f"MLP 160-64x5-3 (padded to 8 outputs), inference on {n} records incl. encoding; "
+                               "training = 4 Adam steps of 16,384 rows", "macs_per_row": MLP_MACS},
+        "training": {"ms_per_frame": round(tr, 4), "tflops": round(tr_tf, 2)},
+        "roofline": {"bound": "tensor", "achieved": round(inf_tf, 2), "peak": peak, "unit": "TFLOP/s",
+                     "frac": round(inf_tf / peak, 4), "traffic": None,
+                     "peak_source": "measured bf16_tflops (MEASURED_PEAKS.json)" if peaks else "fallback"},
+        "clocks": clk.summary(),
+        "gpu_launches": args.steps * (1 + 4 * 5),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["terrain", "cornell", "multimaterial", "batch", "cache"], default="terrain")
+    ap.add_argument("--workload", choices=["terrain", "cornell", "multimaterial", "batch", "cache", "mlp"], default="terrain")
     ap.add_argument("--cache-scene", choices=["multimaterial", "terrain"], default="multimaterial")
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--height", type=int, default=1080)
@@ -669,6 +734,8 @@ def main() -> None:
         run_render(args)
     elif args.workload == "batch":
         run_batch(args)
+    elif args.workload == "mlp":
+        run_mlp(args)
     else:
         run_cache(args)
 
