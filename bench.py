@@ -56,10 +56,12 @@ WIDTH = 2048
 METRIC = "Mrays/s closest-hit; time to relMSE 0.01, cached vs plain tracer, 1 GB300"
 UNIT = "Mrays/s"
 L2_FLUSH_BYTES = 256 << 20
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one trace launch of this workload,
-# the mean of the four launches ncu captured of `bench.py --steps 2 --warmup 3` on a GB300
-# (incoherent 0.935 GB, primary 0.292 GB per launch); bench.py cannot run ncu itself.
-TRACE_DRAM_BYTES_PER_LAUNCH = 613_200_000
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of the trace kernel of
+# this workload (the default, ray-ordered variant), the mean of the primary (309.4 MB) and
+# incoherent (1,243.9 MB) launches ncu captured of `bench.py --steps 2 --warmup 3` on a GB300;
+# the ordering kernels before them add 140 MB (primary) and 187 MB (incoherent). bench.py cannot
+# run ncu itself.
+TRACE_DRAM_BYTES_PER_LAUNCH = 776_600_000
 
 
 def load_peaks() -> dict:
@@ -314,7 +316,7 @@ def run_ours(args) -> None:
                                        "workload (mean of the primary and incoherent launches)",
                      "peak_source": f"{peaks['source']} hbm_gbs (MEASURED_PEAKS.json)" if peaks["source"] == "measured"
                      else "fallback 6.8 TB/s", "bytes_per_ray": round(bpr, 1),
-                     "kernel": "trace_kernel<closest> (avg launch)", "avg_launch_ms": round(float(kernel_ms), 4)},
+                     "kernel": "tt_trace: ray ordering + trace_warp_kernel<closest> (avg per ray set)", "avg_launch_ms": round(float(kernel_ms), 4)},
         "cpu_baseline": {"value": round(cpu["mrays"], 3), "unit": UNIT, "cores": cpu["threads"], "kind": "port",
                          "sample": f"{cpu['rays']} rays (every {n_rays // cpu['rays']}th of both sets), "
                                    f"{cpu['seconds']:.1f} s"},

@@ -178,11 +178,15 @@ void tt_dbvh_free(tt_dbvh *dbvh);
 /* Kernel shape used by the traversal calls on `bvh` (a tuning knob; the reference launches one
  * ray per thread, src/core/RenderKernel.cu:221-231):
  *   0 TT_VARIANT_WARP       each warp traces 32 consecutive rays, stack in local memory
- *   1 TT_VARIANT_WARP_SH16  (default) as 0, the lowest 16 stack entries in shared memory
+ *   1 TT_VARIANT_WARP_SH16  as 0, the lowest 16 stack entries in shared memory
  *   2 TT_VARIANT_WARP_SH32  as 0, the lowest 32 stack entries in shared memory
  *   3 TT_VARIANT_DYNAMIC    every lane claims a new ray as soon as it finishes one
  *   4 TT_VARIANT_WARP_VOTE  as 0, with the reference's warp-vote leaf postponement
  *                           (IntersectKernel.cuh:180-203)
+ *   5 TT_VARIANT_SORTED     (default) as 1, over the rays in the order of a counting sort by direction
+ *                           octant and origin cell (device scratch of ~17 MB + 8 B per ray)
+ *   6 TT_VARIANT_SH16_OCC   as 1, compiled for 12 resident blocks per SM (fewer registers)
+ *   7 TT_VARIANT_SORTED_OCC as 5, compiled for 12 resident blocks per SM
  * All variants but 4 return the per-ray result of the reference's algorithm and are identical;
  * variant 4 can differ from them in float corner cases, as the reference's own kernel does. */
 #define TT_VARIANT_WARP 0
@@ -190,7 +194,10 @@ void tt_dbvh_free(tt_dbvh *dbvh);
 #define TT_VARIANT_WARP_SH32 2
 #define TT_VARIANT_DYNAMIC 3
 #define TT_VARIANT_WARP_VOTE 4
-#define TT_NUM_VARIANTS 5
+#define TT_VARIANT_SORTED 5
+#define TT_VARIANT_SH16_OCC 6
+#define TT_VARIANT_SORTED_OCC 7
+#define TT_NUM_VARIANTS 8
 tt_status tt_dbvh_set_variant(tt_dbvh *bvh, int32_t variant);
 tt_status tt_dbvh_get_variant(const tt_dbvh *bvh, int32_t *variant);
 /* Autotuner: traces the n device rays with every variant (the warp-vote one only when

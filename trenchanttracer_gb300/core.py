@@ -213,8 +213,9 @@ class DeviceBVH:
                                   C.c_void_p(stream)))
 
     VARIANT_WARP, VARIANT_WARP_SH16, VARIANT_WARP_SH32, VARIANT_DYNAMIC, VARIANT_WARP_VOTE = 0, 1, 2, 3, 4
-    NUM_VARIANTS = 5
-    DETERMINISTIC_VARIANTS = (0, 1, 2, 3)
+    VARIANT_SORTED, VARIANT_SH16_OCC, VARIANT_SORTED_OCC = 5, 6, 7
+    NUM_VARIANTS = 8
+    DETERMINISTIC_VARIANTS = (0, 1, 2, 3, 5, 6, 7)
 
     def set_variant(self, variant: int) -> None:
         """Kernel shape of the traversal calls (include/tt.h, tt_dbvh_set_variant)."""

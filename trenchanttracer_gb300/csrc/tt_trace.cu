@@ -16,15 +16,23 @@
 //                         active at the vote depends on how the warp re-converges, so in float
 //                         corner cases (a leaf box whose entry rounds above a nearly equal hit
 //                         distance) the result can depend on the other rays of the warp.
+//   TT_VARIANT_SORTED     WARP_SH16 over the rays in the order of a counting sort by direction
+//                         octant and origin cell (tt_reorder.cu); each hit still goes to its
+//                         own ray's slot.
+//   TT_VARIANT_SH16_OCC,  WARP_SH16 and SORTED compiled for 12 resident blocks per SM (40
+//   TT_VARIANT_SORTED_OCC registers and a few spilled values instead of 54 registers), trading
+//                         spills for more warps to hide the node-fetch latency.
 // All but WARP_VOTE return the per-ray result of the reference's algorithm, bit for bit.
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
 #include <string>
 
 #include "tt_internal.h"
+#include "tt_reorder.h"
 #include "tt_traverse.cuh"
 
 namespace tt {
@@ -36,8 +44,12 @@ enum TraceVariant : int {
     VARIANT_WARP_SH32 = 2,
     VARIANT_DYNAMIC = 3,
     VARIANT_WARP_VOTE = 4,
-    NUM_VARIANTS = 5
+    VARIANT_SORTED = 5,
+    VARIANT_SH16_OCC = 6,
+    VARIANT_SORTED_OCC = 7,
+    NUM_VARIANTS = 8
 };
+constexpr int kOccBlocks = 12;  // resident blocks per SM the *_OCC variants are compiled for
 
 struct DeviceBVH {
     BvhView view;
@@ -47,8 +59,12 @@ struct DeviceBVH {
     unsigned long long *scratch = nullptr;  // [0] work counter, [1] error word (low 32 bits)
     int device = 0;
     int num_sms = 0;
-    int blocks_per_sm[NUM_VARIANTS] = {1, 1, 1, 1, 1};
-    int variant = VARIANT_WARP_SH16;
+    int blocks_per_sm[NUM_VARIANTS] = {1, 1, 1, 1, 1, 1, 1, 1};
+    int variant = VARIANT_SORTED;
+    float lo[3] = {-1.f, -1.f, -1.f}, hi[3] = {1.f, 1.f, 1.f};  // scene bounds (root boxes)
+    // ray-ordering scratch per work-counter slot (caller stream, three pipeline streams)
+    void *order[4] = {nullptr, nullptr, nullptr, nullptr};
+    size_t order_bytes[4] = {0, 0, 0, 0};
     // device staging, streams and events for the host-buffer entry point's copy/compute pipeline
     void *d_stage = nullptr;
     size_t d_stage_bytes = 0;
@@ -69,6 +85,7 @@ struct TraceArgs {
     void *hits;
     unsigned long long *counter;
     unsigned int *err;
+    const int *perm;  // TT_VARIANT_SORTED: ray index of each slot
 };
 
 template <bool kExt>
@@ -94,9 +111,10 @@ __device__ __forceinline__ void store_hit(const TraceArgs &a, int64_t i, const T
     }
 }
 
-// Warp-batched: each warp claims 32 consecutive rays. kSh stack entries live in shared memory.
-template <bool kClosest, bool kExt, bool kSpec, int kSh>
-__global__ void __launch_bounds__(kTraceBlock) trace_warp_kernel(TraceArgs a) {
+// Warp-batched: each warp claims 32 consecutive rays (kPerm: 32 consecutive slots of the ray
+// permutation). kSh stack entries live in shared memory.
+template <bool kClosest, bool kExt, bool kSpec, int kSh, bool kPerm = false, int kMinBlocks = 1>
+__global__ void __launch_bounds__(kTraceBlock, kMinBlocks) trace_warp_kernel(TraceArgs a) {
     __shared__ int sh_stack[(kSh > 0 ? kSh : 1) * kTraceBlock];
     const int lane = threadIdx.x & 31;
     uint32_t err = 0;
@@ -107,8 +125,9 @@ __global__ void __launch_bounds__(kTraceBlock) trace_warp_kernel(TraceArgs a) {
         if (lane == 0) base = atomicAdd(a.counter, 32ull);
         base = __shfl_sync(0xffffffffu, base, 0);
         if ((int64_t)base >= a.n) break;
-        const int64_t i = (int64_t)base + lane;
-        if (i < a.n) {
+        const int64_t slot = (int64_t)base + lane;
+        if (slot < a.n) {
+            const int64_t i = kPerm ? (int64_t)a.perm[slot] : slot;
             TravState s;
             const float4 r0 = __ldg(a.rays + 2 * i), r1 = __ldg(a.rays + 2 * i + 1);
             trav_init(s, stack, r0, r1);
@@ -173,6 +192,9 @@ static const void *kernel_for(int variant) {
         case VARIANT_WARP_SH16: return (const void *)trace_warp_kernel<kClosest, kExt, false, 16>;
         case VARIANT_WARP_SH32: return (const void *)trace_warp_kernel<kClosest, kExt, false, 32>;
         case VARIANT_DYNAMIC: return (const void *)trace_dynamic_kernel<kClosest, kExt, 16>;
+        case VARIANT_SORTED: return (const void *)trace_warp_kernel<kClosest, kExt, false, 16, true>;
+        case VARIANT_SH16_OCC: return (const void *)trace_warp_kernel<kClosest, kExt, false, 16, false, kOccBlocks>;
+        case VARIANT_SORTED_OCC: return (const void *)trace_warp_kernel<kClosest, kExt, false, 16, true, kOccBlocks>;
         default: return (const void *)trace_warp_kernel<kClosest, kExt, true, 0>;
     }
 }
@@ -220,6 +242,20 @@ static tt_status upload(const CompactBVH &b, DeviceBVH &d) {
     TT_CUDA(cudaMemcpy(p, b.mat_idx.data(), ab, cudaMemcpyHostToDevice));
     d.num_nodes = (uint32_t)b.nodes.size();
     d.num_verts = (uint32_t)b.vertices.size();
+    // scene bounds from the root's two child boxes (float4 0: c0 x/y, 1: c1 x/y, 2: z of both),
+    // for the ray-ordering grid; an axis without a finite, non-empty extent keeps [-1, 1]
+    if (b.nodes.size() >= 3) {
+        const float *n0 = reinterpret_cast<const float *>(&b.nodes[0]);
+        const float *n1 = reinterpret_cast<const float *>(&b.nodes[1]);
+        const float *nz = reinterpret_cast<const float *>(&b.nodes[2]);
+        const float lo[3] = {std::fmin(n0[0], n1[0]), std::fmin(n0[2], n1[2]), std::fmin(nz[0], nz[2])};
+        const float hi[3] = {std::fmax(n0[1], n1[1]), std::fmax(n0[3], n1[3]), std::fmax(nz[1], nz[3])};
+        for (int k = 0; k < 3; k++)
+            if (std::isfinite(lo[k]) && std::isfinite(hi[k]) && hi[k] > lo[k]) {
+                d.lo[k] = lo[k];
+                d.hi[k] = hi[k];
+            }
+    }
     e = cudaMalloc(&d.scratch, 256);
     if (e != cudaSuccess) return fail(TT_ERR_OOM, std::string("cudaMalloc scratch: ") + cudaGetErrorString(e));
     TT_CUDA(cudaMemset(d.scratch, 0, 256));
@@ -230,6 +266,8 @@ static void release(DeviceBVH &d) {
     if (d.base) cudaFree(d.base);
     if (d.scratch) cudaFree(d.scratch);
     if (d.d_stage) cudaFree(d.d_stage);
+    for (int i = 0; i < 4; i++)
+        if (d.order[i]) cudaFree(d.order[i]);
     for (int i = 0; i < 3; i++) {
         if (d.pipe[i]) cudaStreamDestroy(d.pipe[i]);
         if (d.pipe_done[i]) cudaEventDestroy(d.pipe_done[i]);
@@ -253,6 +291,15 @@ static void launch_variant(int variant, unsigned blocks, cudaStream_t stream, co
         case VARIANT_DYNAMIC:
             trace_dynamic_kernel<kClosest, kExt, 16><<<blocks, kTraceBlock, 0, stream>>>(a);
             break;
+        case VARIANT_SORTED:
+            trace_warp_kernel<kClosest, kExt, false, 16, true><<<blocks, kTraceBlock, 0, stream>>>(a);
+            break;
+        case VARIANT_SH16_OCC:
+            trace_warp_kernel<kClosest, kExt, false, 16, false, kOccBlocks><<<blocks, kTraceBlock, 0, stream>>>(a);
+            break;
+        case VARIANT_SORTED_OCC:
+            trace_warp_kernel<kClosest, kExt, false, 16, true, kOccBlocks><<<blocks, kTraceBlock, 0, stream>>>(a);
+            break;
         default:
             trace_warp_kernel<kClosest, kExt, true, 0><<<blocks, kTraceBlock, 0, stream>>>(a);
     }
@@ -273,17 +320,37 @@ static tt_status launch_trace(const DeviceBVH &d, const void *d_rays, int64_t n,
     a.hits = d_hits;
     a.counter = d.scratch + counter_slot;
     a.err = reinterpret_cast<unsigned int *>(d.scratch + kScratchErr);
+    a.perm = nullptr;
+    int variant = d.variant;
+    const bool sorted = variant == VARIANT_SORTED || variant == VARIANT_SORTED_OCC;
+    if (sorted && n >= ((int64_t)1 << 31)) variant = VARIANT_WARP_SH16;  // the permutation is int
+    if (variant == VARIANT_SORTED || variant == VARIANT_SORTED_OCC) {
+        // one scratch per work-counter slot, so the pipeline streams never share one
+        const int k = counter_slot == 0 ? 0 : 1 + (counter_slot - kScratchPipe) % 3;
+        const size_t need = reorder_scratch_bytes(n);
+        DeviceBVH &dm = const_cast<DeviceBVH &>(d);
+        if (dm.order_bytes[k] < need) {
+            if (dm.order[k]) cudaFree(dm.order[k]);
+            dm.order[k] = nullptr;
+            dm.order_bytes[k] = 0;
+            cudaError_t e = cudaMalloc(&dm.order[k], need);
+            if (e != cudaSuccess) return fail(TT_ERR_OOM, std::string("ray ordering scratch: ") + cudaGetErrorString(e));
+            dm.order_bytes[k] = need;
+        }
+        const tt_status st = reorder_rays(a.rays, n, d.lo, d.hi, dm.order[k], d.num_sms, stream, &a.perm);
+        if (st != TT_OK) return st;
+    }
     const int64_t warps_needed = (n + 31) / 32;
-    int64_t blocks = (int64_t)d.num_sms * d.blocks_per_sm[d.variant];
+    int64_t blocks = (int64_t)d.num_sms * d.blocks_per_sm[variant];
     const int64_t max_useful = (warps_needed * 32 + kTraceBlock - 1) / kTraceBlock;
     if (blocks > max_useful) blocks = max_useful;
     if (blocks < 1) blocks = 1;
     if (closest) {
-        if (ext) launch_variant<true, true>(d.variant, (unsigned)blocks, stream, a);
-        else launch_variant<true, false>(d.variant, (unsigned)blocks, stream, a);
+        if (ext) launch_variant<true, true>(variant, (unsigned)blocks, stream, a);
+        else launch_variant<true, false>(variant, (unsigned)blocks, stream, a);
     } else {
-        if (ext) launch_variant<false, true>(d.variant, (unsigned)blocks, stream, a);
-        else launch_variant<false, false>(d.variant, (unsigned)blocks, stream, a);
+        if (ext) launch_variant<false, true>(variant, (unsigned)blocks, stream, a);
+        else launch_variant<false, false>(variant, (unsigned)blocks, stream, a);
     }
     TT_CUDA(cudaGetLastError());
     return TT_OK;
