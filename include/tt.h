@@ -366,6 +366,7 @@ typedef struct tt_cache_params {
     uint32_t seed;               /* weight initialisation (1) */
     int32_t use_ema;             /* render with the averaged weights (1) */
     float bbox_lo[3], bbox_hi[3];/* scene bounds of the position encoding */
+    int32_t mma_kind;            /* inference kernel: 0 tcgen05 + TMEM (default), 1 mma.sync */
 } tt_cache_params;
 tt_status tt_cache_params_default(tt_cache_params *params);
 tt_status tt_cache_create(const tt_cache_params *params, tt_cache **out);
@@ -392,6 +393,8 @@ tt_status tt_cache_train(tt_cache *cache, const float *d_records, const float *d
                          float *h_loss, void *stream);
 /* Adam steps taken so far. */
 tt_status tt_cache_steps(const tt_cache *cache, int32_t *steps);
+/* The tensor-core kernels' error word (a bounded wait that ran out); synchronises `stream`. */
+tt_status tt_cache_check(tt_cache *cache, void *stream);
 /* The native path tracer with the cache: a path that is not a training path ends at the first
  * vertex from its second on where its spread exceeds spread_c x its pixel footprint, adding
  * throughput x (emission + cache radiance); training paths (cache params train_paths per wave,

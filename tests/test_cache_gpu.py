@@ -66,6 +66,26 @@ def test_inference_matches_oracle():
     assert torch.equal(cache.infer(rec_t, use_ema=True), cache.infer(rec_t))
 
 
+@pytest.mark.parametrize("n", [1, 127, 128, 129, 3000])
+def test_tcgen05_inference_matches_mma_sync_and_oracle(n):
+    """The tcgen05 / TMEM inference kernel (mma_kind 0) against the mma.sync one (mma_kind 1) and
+    the oracle, with the same BF16 weights, including partial 128-row tiles."""
+    w = nrc.init_weights(21)
+    tc = Cache(LO, HI, batch=4096, mma_kind=0)
+    ms = Cache(LO, HI, batch=4096, mma_kind=1)
+    tc.set_weights(w)
+    ms.set_weights(w)
+    rec_t = torch.from_numpy(_records(n, 7)).cuda()
+    a = tc.infer(rec_t).cpu().numpy()
+    b = ms.infer(rec_t).cpu().numpy()
+    tc.check()
+    ref = nrc.radiance(_enc_np(ms, rec_t), w)
+    for got in (a, b):
+        rel = np.abs(got - ref) / np.abs(ref)
+        assert np.median(rel) < 1e-3 and rel.max() < 5e-2, (np.median(rel), rel.max())
+    assert np.median(np.abs(a - b) / np.abs(b)) < 1e-3
+
+
 def test_gradient_matches_oracle():
     cache = Cache(LO, HI, batch=4096)
     w = nrc.init_weights(12)

@@ -76,7 +76,7 @@ class CacheParams(C.Structure):
     _fields_ = [("lr", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float), ("eps", C.c_float),
                 ("ema", C.c_float), ("batch", C.c_int32), ("steps", C.c_int32), ("train_paths", C.c_int32),
                 ("spread_c", C.c_float), ("seed", C.c_uint32), ("use_ema", C.c_int32),
-                ("bbox_lo", C.c_float * 3), ("bbox_hi", C.c_float * 3)]
+                ("bbox_lo", C.c_float * 3), ("bbox_hi", C.c_float * 3), ("mma_kind", C.c_int32)]
 
 
 class View(C.Structure):
@@ -148,6 +148,7 @@ SIGNATURES = {
     "tt_cache_gradient": (I32, [P, P, P, I64, P, P, P]),
     "tt_cache_train": (I32, [P, P, P, I64, I32, P, P]),
     "tt_cache_steps": (I32, [P, C.POINTER(I32)]),
+    "tt_cache_check": (I32, [P, P]),
     "tt_render_cached": (I32, [P, P, C.POINTER(CameraMeta), C.POINTER(RenderParams), P, I32, P]),
 }
 

@@ -441,6 +441,9 @@ class Cache:
         check(lib().tt_cache_steps(self._h, C.byref(n)))
         return n.value
 
+    def check(self, stream: int = 0) -> None:
+        check(lib().tt_cache_check(self._h, C.c_void_p(stream)))
+
     def __del__(self):
         if getattr(self, "_h", None):
             lib().tt_cache_free(self._h)

@@ -17,6 +17,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdint>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -24,6 +25,7 @@
 #include "tt_internal.h"
 #include "tt_nrc.cuh"
 #include "tt_nrc_host.h"
+#include "tt_nrc_tc.h"
 
 namespace tt {
 namespace nrc {
@@ -508,6 +510,8 @@ struct tt_cache {
     int num_sms = 0;
     float *master = nullptr, *m = nullptr, *v = nullptr, *ema = nullptr, *grad = nullptr;
     uint16_t *w_train = nullptr, *w_ema = nullptr;
+    uint16_t *w_tc_train = nullptr, *w_tc_ema = nullptr;  // the same in the tcgen05 operand layout
+    unsigned *err = nullptr;                                // error word of the tcgen05 kernel
     int *step = nullptr;
     float *loss = nullptr;
     // training scratch for `p.batch` rows
@@ -587,6 +591,9 @@ tt_status upload_weights(tt_cache *c, const std::vector<float> &w) {
     TT_CUDA_C(cudaMemcpy(c->w_train, pad.data(), 2 * kPadded, cudaMemcpyHostToDevice));
     TT_CUDA_C(cudaMemcpy(c->w_ema, pad.data(), 2 * kPadded, cudaMemcpyHostToDevice));
     TT_CUDA_C(cudaMemset(c->step, 0, sizeof(int)));
+    tc_relayout(c->master, c->w_tc_train, nullptr);
+    tc_relayout(c->ema, c->w_tc_ema, nullptr);
+    TT_CUDA_C(cudaDeviceSynchronize());
     return TT_OK;
 }
 
@@ -656,7 +663,11 @@ tt_status train_pass(tt_cache *c, const float *rec, const float *target, long lo
     ad.ema_f = c->p.ema;
     ad.update = update;
     k_adam<<<(kParams + 255) / 256, 256, 0, s>>>(ad);
-    if (update) k_adam_step<<<1, 1, 0, s>>>(c->step, n_dev, n_dev ? off : 0);
+    if (update) {
+        k_adam_step<<<1, 1, 0, s>>>(c->step, n_dev, n_dev ? off : 0);
+        tc_relayout(c->master, c->w_tc_train, s);
+        tc_relayout(c->ema, c->w_tc_ema, s);
+    }
     TT_CUDA_C(cudaGetLastError());
     return TT_OK;
 }
@@ -668,6 +679,11 @@ namespace nrc {
 
 tt_status cache_infer_device(tt_cache *c, const float *rec, const int *n_dev, long long cap, float *rgb, int use_ema,
                              cudaStream_t s) {
+    if (c->p.mma_kind == 0) {
+        const Encoding e = encoding_of(c->p);
+        return tc_infer(use_ema ? c->w_tc_ema : c->w_tc_train, rec, 0, n_dev, cap, e.lo, e.inv_ext, rgb, c->err,
+                        c->num_sms, s);
+    }
     MlpArgs a;
     std::memset(&a, 0, sizeof(a));
     a.w = use_ema ? c->w_ema : c->w_train;
@@ -710,6 +726,7 @@ tt_status tt_cache_params_default(tt_cache_params *p) {
     p->spread_c = 0.01f;
     p->seed = 1;
     p->use_ema = 1;
+    p->mma_kind = 0;
     for (int i = 0; i < 3; i++) {
         p->bbox_lo[i] = -1.0f;
         p->bbox_hi[i] = 1.0f;
@@ -720,6 +737,7 @@ tt_status tt_cache_params_default(tt_cache_params *p) {
 tt_status tt_cache_create(const tt_cache_params *p, tt_cache **out) {
     if (!p || !out) return fail(TT_ERR_INVALID, "null argument");
     *out = nullptr;
+    if (p->mma_kind < 0 || p->mma_kind > 1) return fail(TT_ERR_INVALID, "cache: mma_kind must be 0 or 1");
     if (p->batch < 16 || p->batch > (1 << 22) || p->steps < 1 || p->train_paths < 1 || p->train_paths > (1 << 24))
         return fail(TT_ERR_INVALID, "cache: batch must be in 16..2^22, steps >= 1, train_paths in 1..2^24");
     if (!(p->lr > 0.0f) || !(p->beta1 >= 0.0f && p->beta1 < 1.0f) || !(p->beta2 >= 0.0f && p->beta2 < 1.0f) ||
@@ -740,6 +758,10 @@ tt_status tt_cache_create(const tt_cache_params *p, tt_cache **out) {
         delete c;
         return cuda_fail_c(e, "cache setup");
     }
+    if (tc_setup() != TT_OK) {
+        delete c;
+        return TT_ERR_CUDA;
+    }
     const size_t B = (size_t)p->batch;
     c->chunks = (int)((B + kChunkRows - 1) / kChunkRows);
     auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
@@ -750,6 +772,9 @@ tt_status tt_cache_create(const tt_cache_params *p, tt_cache **out) {
     sizes.push_back(2 * B * kOutPad);                                       // dY
     sizes.push_back(4 * B * 3);                                             // y
     sizes.push_back(4 * (size_t)c->chunks * kParams);                       // partials
+    sizes.push_back(2 * tc_weight_elems());                                 // operand-layout weights
+    sizes.push_back(2 * tc_weight_elems());
+    sizes.push_back(256);                                                   // error word
     size_t total = 0;
     for (size_t s : sizes) total += al(s);
     e = cudaMalloc(&c->block, total);
@@ -778,6 +803,9 @@ tt_status tt_cache_create(const tt_cache_params *p, tt_cache **out) {
     for (int l = 0; l < kLayers; l++) c->dz[l] = (uint16_t *)take();
     c->y = (float *)take();
     c->partial = (float *)take();
+    c->w_tc_train = (uint16_t *)take();
+    c->w_tc_ema = (uint16_t *)take();
+    c->err = (unsigned *)take();
     std::vector<float> w;
     init_weights(p->seed, w);
     const tt_status st = upload_weights(c, w);
@@ -833,6 +861,13 @@ tt_status tt_cache_infer(tt_cache *c, const float *d_records, int64_t n, float *
                          void *stream) {
     if (!c || (n > 0 && (!d_records || !d_rgb))) return fail(TT_ERR_INVALID, "null argument");
     if (n <= 0) return n == 0 ? TT_OK : fail(TT_ERR_INVALID, "negative count");
+    if (c->p.mma_kind == 0) {
+        if (reinterpret_cast<uintptr_t>(d_records) & 15)
+            return fail(TT_ERR_INVALID, "cache: records must be 16-byte aligned");
+        const Encoding e = encoding_of(c->p);
+        return tc_infer(use_ema ? c->w_tc_ema : c->w_tc_train, d_records, n, nullptr, 0, e.lo, e.inv_ext, d_rgb,
+                        c->err, c->num_sms, (cudaStream_t)stream);
+    }
     MlpArgs a;
     std::memset(&a, 0, sizeof(a));
     a.w = use_ema ? c->w_ema : c->w_train;
@@ -842,6 +877,18 @@ tt_status tt_cache_infer(tt_cache *c, const float *d_records, int64_t n, float *
     a.rgb = d_rgb;
     k_mlp_forward<false><<<fwd_grid(c, n), kThreads, kFwdSmem, (cudaStream_t)stream>>>(a);
     TT_CUDA_C(cudaGetLastError());
+    return TT_OK;
+}
+
+tt_status tt_cache_check(tt_cache *c, void *stream) {
+    if (!c) return fail(TT_ERR_INVALID, "null cache");
+    unsigned w = 0;
+    TT_CUDA_C(cudaMemcpyAsync(&w, c->err, sizeof(w), cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+    TT_CUDA_C(cudaStreamSynchronize((cudaStream_t)stream));
+    if (w) {
+        TT_CUDA_C(cudaMemset(c->err, 0, sizeof(w)));
+        return fail(TT_ERR_TIMEOUT, "cache: a tensor-core wait ran out");
+    }
     return TT_OK;
 }
 

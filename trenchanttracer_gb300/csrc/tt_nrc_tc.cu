@@ -1,0 +1,389 @@
+// The radiance cache's inference on 5th-generation tensor cores: tcgen05.mma with the FP32
+// accumulator in tensor memory (TMEM), operands in shared memory, weights and feature records
+// brought in by bulk asynchronous copies (cp.async.bulk) that signal an mbarrier.
+//
+// One CTA of 128 threads owns a tile of 128 rows at a time (row r = thread r = TMEM lane r):
+//   records  cp.async.bulk of the tile's 128 x 64 B into shared memory
+//   encode   each thread builds its row's 160 BF16 inputs in the A buffer
+//   layers   one thread issues the layer's tcgen05.mma (M = 128, N = 64 or 16, K = 16 each) and a
+//            tcgen05.commit to an mbarrier; after the wait every warp reads its 32 TMEM lanes
+//            (tcgen05.ld 32x32b), applies ReLU, rounds to BF16 and writes the next layer's A
+//   output   exp of the first three columns of the last layer
+// The network's weights (55.3 KB, in the operand layout below) are loaded once per CTA.
+//
+// Operand layout: no swizzle, K-major, 8 x 16-byte core matrices. A (128 x K): core (m8, k8) at
+// byte (k8 * 16 + m8) * 128, so the stride between 8-row groups (SBO) is 128 and between the two
+// K halves of one instruction (LBO) 2048. Weights W_l (N x K): core (n8, k8) at (k8 * N/8 + n8) *
+// 128 from the layer's base: SBO 128, LBO N/8 * 128. Shared memory holds A first, then the
+// weights, the records and the barriers, so that every operand address the descriptors can form
+// (with either of the two byte offsets applied along either dimension) lies inside the CTA's
+// own allocation.
+//
+// Every wait is bounded (a clock budget of about a second): one thread waits, the outcome goes
+// to all threads through shared memory and a block barrier, so a failure is uniform; it is
+// reported in the error word, and the TMEM columns are freed on every path.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "tt_nrc.cuh"
+#include "tt_nrc_tc.h"
+
+namespace tt {
+namespace nrc {
+
+constexpr int kTcRows = 128;
+constexpr int kTcThreads = 128;
+constexpr int kTmemCols = 64;
+constexpr int kABytes = kTcRows * kIn * 2;           // 40960
+constexpr int kRecBytes = kTcRows * kRec * 4;        // 8192
+constexpr long long kWaitCycles = 2000000000ll;      // ~1 s at 2 GHz
+constexpr unsigned kErrMlpWait = 8u;                 // error word bit: a tensor-core wait ran out
+
+__host__ __device__ constexpr int tc_out(int l) { return l == kLayers - 1 ? 16 : kHidden; }
+__host__ __device__ constexpr int tc_offset(int l) { return l == 0 ? 0 : tc_offset(l - 1) + layer_in(l - 1) * tc_out(l - 1); }
+constexpr int kTcWeights = tc_offset(kLayers);        // 27648 bf16
+constexpr int kTcWeightBytes = kTcWeights * 2;        // 55296
+constexpr int kTcSmem = kTcWeightBytes + kABytes + kRecBytes + 64;
+static_assert(kTcWeightBytes % 16 == 0 && kABytes % 16 == 0 && kRecBytes % 16 == 0, "bulk copy sizes");
+
+__host__ __device__ inline int tc_index(int l, int n, int k) {
+    const int ng = tc_out(l) / 8;
+    return tc_offset(l) + ((k / 8) * ng + n / 8) * 64 + (n % 8) * 8 + (k % 8);
+}
+
+// ---- PTX helpers ------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t saddr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(saddr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(saddr(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(saddr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait for the phase of the given parity
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+    const long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity))
+        if (clock64() - t0 > kWaitCycles) return false;
+    return true;
+}
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     saddr(dst)),
+                 "l"(src), "r"(bytes), "r"(saddr(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_alloc(uint32_t *slot, uint32_t cols) {  // whole warp
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(saddr(slot)), "r"(cols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_free(uint32_t taddr, uint32_t cols) {  // whole warp
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(cols) : "memory");
+}
+
+// shared-memory matrix descriptor: no swizzle, version 1 (bits 46-47), LBO / SBO in bytes
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | ((uint64_t)1 << 46);
+}
+// instruction descriptor, kind::f16: D = F32 (bits 4-5), A = B = BF16 (bits 7-9, 10-12),
+// both K-major, N >> 3 at bit 17, M >> 4 at bit 24
+__host__ __device__ constexpr uint32_t idesc_bf16(int m, int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+__device__ __forceinline__ void umma(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+            dtmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc)
+        : "memory");
+}
+__device__ __forceinline__ void umma_commit(uint64_t *bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(saddr(bar))
+                 : "memory");
+}
+// 16 consecutive 32-bit TMEM columns of this thread's lane
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float v[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr)
+        : "memory");
+#pragma unroll
+    for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// ---- the A operand ----------------------------------------------------------------------------
+__device__ __forceinline__ int a_offset(int r, int k) {  // bf16 element index in the A buffer
+    return ((k >> 3) * 16 + (r >> 3)) * 64 + (r & 7) * 8 + (k & 7);
+}
+
+struct TcEncoding {
+    float lo[3], inv_ext[3];
+};
+
+// the encoding of tt_nrc.cuh, one row, straight into the A operand
+__device__ __forceinline__ void encode_row(const float *rec, const TcEncoding &e, __nv_bfloat16 *A, int r) {
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        float f = (rec[i] - e.lo[i]) * e.inv_ext[i];
+        for (int k = 0; k < kPosFreq; k++) {
+            float s, c;
+            sincospif(f, &s, &c);
+            A[a_offset(r, 24 * i + 2 * k)] = __float2bfloat16_rn(s);
+            A[a_offset(r, 24 * i + 2 * k + 1)] = __float2bfloat16_rn(c);
+            f *= 2.0f;
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        float fd = (rec[3 + i] + 1.0f) * 0.5f, fn = (rec[6 + i] + 1.0f) * 0.5f;
+        for (int k = 0; k < kDirFreq; k++) {
+            float s, c;
+            sincospif(fd, &s, &c);
+            A[a_offset(r, 72 + 12 * i + 2 * k)] = __float2bfloat16_rn(s);
+            A[a_offset(r, 72 + 12 * i + 2 * k + 1)] = __float2bfloat16_rn(c);
+            sincospif(fn, &s, &c);
+            A[a_offset(r, 108 + 12 * i + 2 * k)] = __float2bfloat16_rn(s);
+            A[a_offset(r, 108 + 12 * i + 2 * k + 1)] = __float2bfloat16_rn(c);
+            fd *= 2.0f;
+            fn *= 2.0f;
+        }
+    }
+    float tail[16];
+    tail[0] = rec[9];
+    tail[1] = rec[10];
+    tail[2] = rec[11];
+    tail[3] = rec[12];
+    tail[4] = 1.0f;
+    for (int i = 0; i < 3; i++) {
+        tail[5 + i] = rec[3 + i];
+        tail[8 + i] = rec[6 + i];
+        tail[11 + i] = (rec[i] - e.lo[i]) * e.inv_ext[i];
+    }
+    tail[14] = rec[13];
+    tail[15] = 0.0f;
+    uint32_t w[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+        const __nv_bfloat162 b = __floats2bfloat162_rn(tail[2 * j], tail[2 * j + 1]);
+        w[j] = *reinterpret_cast<const uint32_t *>(&b);
+    }
+    *reinterpret_cast<uint4 *>(A + a_offset(r, 144)) = make_uint4(w[0], w[1], w[2], w[3]);
+    *reinterpret_cast<uint4 *>(A + a_offset(r, 152)) = make_uint4(w[4], w[5], w[6], w[7]);
+}
+
+struct TcArgs {
+    const uint16_t *w;  // weights in the operand layout (kTcWeights bf16)
+    const float *rec;
+    long long n_host;
+    const int *n_dev;   // rows = min(*n_dev, cap) when set
+    long long cap;
+    TcEncoding enc;
+    float *rgb;
+    unsigned *err;
+};
+
+__global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(TcArgs a) {
+    extern __shared__ __align__(128) uint8_t smem[];
+    __nv_bfloat16 *A = reinterpret_cast<__nv_bfloat16 *>(smem);
+    uint16_t *W = reinterpret_cast<uint16_t *>(smem + kABytes);
+    float *R = reinterpret_cast<float *>(smem + kABytes + kTcWeightBytes);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kABytes + kTcWeightBytes + kRecBytes);  // [0] w [1] rec [2] mma
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 3);
+    int *ok = reinterpret_cast<int *>(bars + 4);
+    int *failed = ok + 1;  // the barrier (0..2) and parity of a wait that ran out
+    const int tid = threadIdx.x, warp = tid >> 5;
+
+    long long n = a.n_host;
+    if (a.n_dev) {
+        n = *a.n_dev;
+        n = n < 0 ? 0 : (n > a.cap ? a.cap : n);
+    }
+    const long long ntiles = (n + kTcRows - 1) / kTcRows;
+    if ((long long)blockIdx.x >= ntiles) return;  // uniform per block: nothing allocated yet
+
+    if (tid == 0) {
+        mbar_init(bars + 0, 1);
+        mbar_init(bars + 1, 1);
+        mbar_init(bars + 2, 1);
+        *ok = 1;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (warp == 0) tmem_alloc(tmem_slot, kTmemCols);
+    if (tid == 0) {
+        mbar_expect_tx(bars + 0, kTcWeightBytes);
+        bulk_load(W, a.w, kTcWeightBytes, bars + 0);
+        if (!mbar_wait(bars + 0, 0)) {
+            *ok = 0;
+            *failed = 0;
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    uint32_t ph_rec = 0, ph_mma = 0;
+    for (long long tile = blockIdx.x; tile < ntiles && *ok; tile += gridDim.x) {
+        const long long r0 = tile * kTcRows;
+        const int rows = (int)((n - r0) < kTcRows ? (n - r0) : kTcRows);
+        if (tid == 0) {
+            mbar_expect_tx(bars + 1, (uint32_t)rows * kRec * 4);
+            bulk_load(R, a.rec + r0 * kRec, (uint32_t)rows * kRec * 4, bars + 1);
+            if (!mbar_wait(bars + 1, ph_rec)) {
+                *ok = 0;
+                *failed = 2 + (int)ph_rec;
+            }
+        }
+        ph_rec ^= 1;
+        __syncthreads();
+        if (!*ok) break;
+        if (tid < rows) {
+            encode_row(R + tid * kRec, a.enc, A, tid);
+        } else {
+            for (int k = 0; k < kIn; k += 8)
+                *reinterpret_cast<uint4 *>(A + a_offset(tid, k)) = make_uint4(0u, 0u, 0u, 0u);
+        }
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        for (int l = 0; l < kLayers; l++) {
+            const int K = layer_in(l), N = tc_out(l);
+            if (tid == 0) {
+                const uint32_t a0 = saddr(A), b0 = saddr(W + tc_offset(l));
+                const uint32_t idesc = idesc_bf16(kTcRows, N);
+                for (int s = 0; s < K / 16; s++)
+                    umma(tmem, sdesc(a0 + s * 2 * 2048, 2048, 128), sdesc(b0 + s * 2 * (N / 8) * 128, (N / 8) * 128, 128),
+                         idesc, s > 0 ? 1u : 0u);
+                umma_commit(bars + 2);
+                if (!mbar_wait(bars + 2, ph_mma)) {
+                    *ok = 0;
+                    *failed = 4 + (int)ph_mma;
+                }
+            }
+            ph_mma ^= 1;
+            __syncthreads();
+            tc_fence_after();
+            if (!*ok) break;
+            const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
+            if (l < kLayers - 1) {
+#pragma unroll
+                for (int c = 0; c < kHidden; c += 16) {
+                    float v[16];
+                    tmem_ld16(lane_addr + c, v);
+                    tmem_wait_ld();
+                    uint32_t w[8];
+#pragma unroll
+                    for (int j = 0; j < 8; j++) {
+                        const __nv_bfloat162 b = __floats2bfloat162_rn(fmaxf(v[2 * j], 0.f), fmaxf(v[2 * j + 1], 0.f));
+                        w[j] = *reinterpret_cast<const uint32_t *>(&b);
+                    }
+                    *reinterpret_cast<uint4 *>(A + a_offset(tid, c)) = make_uint4(w[0], w[1], w[2], w[3]);
+                    *reinterpret_cast<uint4 *>(A + a_offset(tid, c + 8)) = make_uint4(w[4], w[5], w[6], w[7]);
+                }
+                fence_async_smem();
+            } else {
+                float v[16];
+                tmem_ld16(lane_addr, v);
+                tmem_wait_ld();
+                if (tid < rows) {
+                    float *o = a.rgb + (r0 + tid) * 3;
+                    o[0] = expf(fminf(v[0], 20.0f));
+                    o[1] = expf(fminf(v[1], 20.0f));
+                    o[2] = expf(fminf(v[2], 20.0f));
+                }
+            }
+            tc_fence_before();
+            __syncthreads();
+            tc_fence_after();
+        }
+    }
+    if (tid == 0 && !*ok) {
+        atomicOr(a.err, kErrMlpWait);
+        // let the copy or the products still in flight land (bounded again) before TMEM is freed
+        const int f = *failed;
+        mbar_wait(bars + (f == 0 ? 0 : (f < 4 ? 1 : 2)), f == 0 ? 0u : (uint32_t)(f & 1));
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) tmem_free(tmem, kTmemCols);
+}
+
+__global__ void k_tc_layout(const float *w, uint16_t *out) {
+    // compact [out][in] FP32 weights -> operand layout BF16 (rows beyond the layer's outputs: 0)
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kTcWeights) return;
+    int l = 0;
+    while (l + 1 < kLayers && i >= tc_offset(l + 1)) l++;
+    const int local = i - tc_offset(l);
+    const int ng = tc_out(l) / 8;
+    const int core = local / 64, within = local % 64;
+    const int k8 = core / ng, n8 = core % ng;
+    const int n = n8 * 8 + within / 8, k = k8 * 8 + within % 8;
+    const float v = n < layer_out(l) ? w[w_offset(l) + n * layer_in(l) + k] : 0.0f;
+    const __nv_bfloat16 b = __float2bfloat16_rn(v);
+    out[i] = *reinterpret_cast<const uint16_t *>(&b);
+}
+
+tt_status tc_setup() {
+    const cudaError_t e =
+        cudaFuncSetAttribute(k_mlp_forward_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
+    if (e != cudaSuccess) return fail(TT_ERR_CUDA, std::string("tensor-core MLP setup: ") + cudaGetErrorString(e));
+    return TT_OK;
+}
+
+size_t tc_weight_elems() { return kTcWeights; }
+
+void tc_relayout(const float *w_f32, uint16_t *w_tc, cudaStream_t s) {
+    k_tc_layout<<<(kTcWeights + 255) / 256, 256, 0, s>>>(w_f32, w_tc);
+}
+
+tt_status tc_infer(const uint16_t *w_tc, const float *rec, long long n_host, const int *n_dev, long long cap,
+                   const float lo[3], const float inv_ext[3], float *rgb, unsigned *err, int num_sms,
+                   cudaStream_t s) {
+    TcArgs a;
+    a.w = w_tc;
+    a.rec = rec;
+    a.n_host = n_host;
+    a.n_dev = n_dev;
+    a.cap = cap;
+    for (int i = 0; i < 3; i++) {
+        a.enc.lo[i] = lo[i];
+        a.enc.inv_ext[i] = inv_ext[i];
+    }
+    a.rgb = rgb;
+    a.err = err;
+    const long long rows = n_dev ? cap : n_host;
+    const long long tiles = (rows + kTcRows - 1) / kTcRows;
+    const long long cap_blocks = 2ll * num_sms;
+    const int grid = (int)(tiles < 1 ? 1 : (tiles < cap_blocks ? tiles : cap_blocks));
+    k_mlp_forward_tc<<<grid, kTcThreads, kTcSmem, s>>>(a);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(TT_ERR_CUDA, std::string("tensor-core MLP: ") + cudaGetErrorString(e));
+    return TT_OK;
+}
+
+}  // namespace nrc
+}  // namespace tt
