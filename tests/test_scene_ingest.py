@@ -1,0 +1,123 @@
+"""Scene ingest beyond the golden scenes: the chunked parallel OBJ parser gives the same arrays as
+the reference's loader and as itself on any number of threads (chunk boundaries fall inside
+lines, groups and material switches); OBJs without normals or with fewer normals than vertices
+load (the reference rejects or misreads them)."""
+import hashlib
+import json
+import os
+import subprocess
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import refhost
+from trenchanttracer_gb300 import Scene, TTError
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def _tricky_obj(d: Path, with_normals: bool = True, short_normals: bool = False) -> Path:
+    rng = np.random.default_rng(5)
+    v = rng.uniform(-3, 3, (240, 3)).astype(np.float32)
+    n = rng.normal(size=(240, 3))
+    n = (n / np.linalg.norm(n, axis=1, keepdims=True)).astype(np.float32)
+    if short_normals:
+        n = n[:100]
+    lines = ["# tricky obj\r", "mtllib m.mtl\r"]
+    for i, p in enumerate(v):
+        sep = "\t" if i % 7 == 0 else " "
+        lines.append(f"v{sep}{float(p[0])!r} {float(p[1])!r}  {float(p[2])!r}" + ("\r" if i % 3 == 0 else ""))
+    if with_normals:
+        for q in n:
+            lines.append(f"vn {float(q[0])!r} {float(q[1])!r} {float(q[2])!r}")
+    mats = ["a", "b", "c"]
+    k = 0
+    for gi in range(9):
+        lines.append(f"g grp{gi}")
+        lines.append(f"usemtl {mats[gi % 3]}")
+        for _ in range(int(rng.integers(3, 12))):
+            deg = int(rng.integers(3, 6))
+            idx = rng.choice(240, deg, replace=False)
+            if with_normals:
+                ni = rng.integers(0, len(n), deg)
+                lines.append("f " + " ".join(f"{a + 1}/{(a % 5) + 1}/{b + 1}" for a, b in zip(idx, ni)))
+            else:
+                lines.append("f " + " ".join(f"{a + 1}" for a in idx))
+            k += 1
+        if gi == 4:
+            lines.append("usemtl c")  # a material switch inside a group
+    (d / "m.obj").write_text("\n".join(lines) + "\n")
+    (d / "m.mtl").write_text(json.dumps({"a": {"type": "Diff", "diffuseColor": [0.5, 0.5, 0.5]},
+                                         "b": {"type": "Spec", "color": [0.9, 0.9, 0.9]},
+                                         "c": {"type": "Diff", "diffuseColor": [0.2, 0.7, 0.2]}}))
+    cfg = {"work-dir": str(d), "samples": 1, "material-file": str(d / "m.mtl"), "hdr-file-name": "",
+           "bvh-reload": True, "material-reload": True,
+           "camera": {"width": 8, "height": 8, "position": [0.0, 0.0, 0.0], "yaw": 0.0, "pitch": 0.0,
+                      "focal": 1.0, "aperture": 0.0},
+           "objects": [{"type": "Mesh", "file": str(d / "m.obj"),
+                        "transform": {"scale": [2, 3, 4], "orientation": [10, 20, 30], "translate": [1, 2, 3]}}]}
+    (d / "s.json").write_text(json.dumps(cfg))
+    return d / "s.json"
+
+
+def _digest(arrays: dict) -> str:
+    h = hashlib.sha256()
+    for k in ["vertices", "normals", "vidx", "nidx", "mat"]:
+        h.update(np.ascontiguousarray(arrays[k]).tobytes())
+    return h.hexdigest()
+
+
+@pytest.mark.skipif(not refhost.available(), reason="the reference's loader is not built on this host")
+def test_tricky_obj_matches_reference_loader(tmp_path):
+    cfg = _tricky_obj(tmp_path)
+    mine = Scene.load_json(cfg).arrays()
+    ref = refhost.scene_arrays(str(cfg))
+    for k in ["vertices", "normals", "vidx", "nidx", "mat"]:
+        assert np.array_equal(np.asarray(mine[k]).view(np.uint32) if mine[k].dtype == np.float32 else mine[k],
+                              np.asarray(ref[k]).view(np.uint32) if ref[k].dtype == np.float32 else ref[k]), k
+
+
+def test_parse_is_independent_of_thread_count(tmp_path):
+    cfg = _tricky_obj(tmp_path)
+    code = ("import sys, hashlib, numpy as np; sys.path.insert(0, %r); from trenchanttracer_gb300 import Scene; "
+            "a = Scene.load_json(%r).arrays(); h = hashlib.sha256(); "
+            "[h.update(np.ascontiguousarray(a[k]).tobytes()) for k in ['vertices','normals','vidx','nidx','mat']]; "
+            "print(h.hexdigest())") % (str(ROOT), str(cfg))
+    digests = set()
+    for threads in ("1", "3", "7", "16"):
+        env = dict(os.environ, OMP_NUM_THREADS=threads)
+        out = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, check=True)
+        digests.add(out.stdout.strip().splitlines()[-1])
+    assert len(digests) == 1
+    assert digests == {_digest(Scene.load_json(cfg).arrays())}
+
+
+def test_obj_without_normals_gets_vertex_normals(tmp_path):
+    cfg = _tricky_obj(tmp_path, with_normals=False)
+    a = Scene.load_json(cfg).arrays()
+    assert a["normals"].shape == a["vertices"].shape
+    assert np.array_equal(a["nidx"], a["vidx"])
+    length = np.linalg.norm(a["normals"], axis=1)
+    assert np.allclose(length, 1.0, atol=1e-5)
+
+
+def test_obj_with_fewer_normals_than_vertices(tmp_path):
+    cfg = _tricky_obj(tmp_path, short_normals=True)
+    a = Scene.load_json(cfg).arrays()
+    assert a["normals"].shape[0] == 100 and a["vertices"].shape[0] == 240
+    assert np.allclose(np.linalg.norm(a["normals"], axis=1), 1.0, atol=1e-5)  # all transformed and normalised
+    assert a["nidx"].max() < 100
+
+
+def test_malformed_obj_reports_the_first_error(tmp_path):
+    cfg = _tricky_obj(tmp_path)
+    obj = tmp_path / "m.obj"
+    text = obj.read_text().splitlines()
+    text.insert(50, "v 1.0 2.0")  # a short vertex line, early in the file
+    text.insert(len(text) - 3, "usemtl nosuch")
+    obj.write_text("\n".join(text) + "\n")
+    with pytest.raises(TTError) as e:
+        Scene.load_json(cfg)
+    assert "short v line" in str(e.value)

@@ -19,6 +19,10 @@
 #include <map>
 #include <sstream>
 
+#include <omp.h>
+
+#include <algorithm>
+
 #include "tt_internal.h"
 
 namespace tt {
@@ -342,96 +346,206 @@ static bool next_float(const char *&p, float &out) {
     return true;
 }
 
-// OBJLoader::load + Object::postProcess + Object::apply + Scene::add(Object*).
-static tt_status load_obj(const std::string &file, const M4 &xf, Scene &sc) {
-    std::ifstream ifs(file);
-    if (!ifs.good()) return fail(TT_ERR_IO, "cannot read OBJ " + file);
-    std::vector<V3> verts, norms;
-    std::vector<ObjGroup> groups;
-    std::map<std::string, int32_t> pool;
-    bool have_pool = false;
-    std::string line;
-    while (std::getline(ifs, line)) {
-        const char *p = line.c_str();
+// One line-aligned chunk of an OBJ file, parsed on its own: vertices, normals, triangles (fan
+// triangulation, 0-based indices) and the group / material statements in file order, each with
+// the number of this chunk's triangles that precede it.
+struct ObjEvent {
+    int kind;        // 0 "g", 1 "usemtl", 2 "mtllib"
+    size_t tri;
+    std::string name;
+};
+struct ObjChunk {
+    std::vector<V3> v, vn;
+    std::vector<int32_t> fv, fn;  // 3 per triangle
+    std::vector<ObjEvent> ev;
+    std::string error;  // the first malformed line of the chunk (parsing stopped there)
+};
+
+// Parses the NUL-separated lines in [b, e); every line ends in '\0' or at e, and *e == '\0'.
+static void parse_obj_chunk(char *b, char *e, const std::string &file, ObjChunk &c) {
+    for (char *line = b; line < e;) {
+        char *nl = static_cast<char *>(memchr(line, '\n', (size_t)(e - line)));
+        char *stop = nl ? nl : e;
+        *stop = '\0';
+        const char *p = line;
+        line = stop + 1;
         while (*p == ' ' || *p == '\t') p++;
         const char *k = p;
         while (*p && *p != ' ' && *p != '\t' && *p != '\r') p++;
-        std::string key(k, p);
+        const size_t klen = (size_t)(p - k);
         while (*p == ' ' || *p == '\t') p++;
-        std::string rest(p);
-        while (!rest.empty() && (rest.back() == '\r' || rest.back() == ' ')) rest.pop_back();
-        if (key == "g") {
-            groups.emplace_back();
-        } else if (key == "mtllib") {
-            std::string prefix;
-            size_t slash = file.find_last_of('/');
-            if (slash != std::string::npos) prefix = file.substr(0, slash + 1);
-            std::string name = rest.substr(0, rest.find_first_of(" \t"));
-            tt_status st = load_material_pool(prefix + name, sc, pool);
-            if (st != TT_OK) return st;
-            have_pool = true;
-        } else if (key == "usemtl") {
-            std::string name = rest.substr(0, rest.find_first_of(" \t"));
-            if (!have_pool) return fail(TT_ERR_FORMAT, file + ": usemtl before mtllib");
-            auto it = pool.find(name);
-            if (it == pool.end()) return fail(TT_ERR_FORMAT, "Material " + name + " not found");
-            if (groups.empty()) groups.emplace_back();
-            groups.back().mat = it->second;
-        } else if (key == "v" || key == "vn") {
-            const char *q = rest.c_str();
+        auto key_is = [&](const char *w) { return strlen(w) == klen && strncmp(k, w, klen) == 0; };
+        auto first_word = [&]() {
+            const char *q = p;
+            while (*q && *q != ' ' && *q != '\t' && *q != '\r') q++;
+            return std::string(p, q);
+        };
+        if (key_is("g")) {
+            c.ev.push_back({0, c.fv.size() / 3, std::string()});
+        } else if (key_is("mtllib")) {
+            c.ev.push_back({2, c.fv.size() / 3, first_word()});
+        } else if (key_is("usemtl")) {
+            c.ev.push_back({1, c.fv.size() / 3, first_word()});
+        } else if (key_is("v") || key_is("vn")) {
+            std::vector<V3> &dst = klen == 1 ? c.v : c.vn;
+            const char *q = p;
             float x, y, z;
             while (next_float(q, x)) {
-                if (!next_float(q, y) || !next_float(q, z)) return fail(TT_ERR_FORMAT, file + ": short " + key + " line");
-                (key == "v" ? verts : norms).push_back(V3(x, y, z));
+                if (!next_float(q, y) || !next_float(q, z)) {
+                    c.error = file + ": short " + std::string(k, klen) + " line";
+                    return;
+                }
+                dst.push_back(V3(x, y, z));
             }
-        } else if (key == "f") {
-            if (groups.empty()) groups.emplace_back();
-            std::vector<int> fv, fn;
+        } else if (key_is("f")) {
+            int fv[64], fn[64], cnt = 0;
             int v = 1, n = 1;
-            const char *q = rest.c_str();
-            while (*q) {
-                char *end = nullptr;
-                long a = strtol(q, &end, 10);
-                if (end == q) break;
+            const char *q = p;
+            while (*q && cnt < 64) {
+                char *endp = nullptr;
+                long a = strtol(q, &endp, 10);
+                if (endp == q) break;
                 v = (int)a;
-                q = end;
+                q = endp;
                 if (*q == '/') {
                     q++;
                     if (*q == '/') {
                         q++;
-                        n = (int)strtol(q, &end, 10);
-                        q = end;
+                        n = (int)strtol(q, &endp, 10);
+                        q = endp;
                     } else {
-                        strtol(q, &end, 10);  // texture index: unused
-                        q = end;
+                        strtol(q, &endp, 10);  // texture index: unused
+                        q = endp;
                         if (*q == '/') {
                             q++;
-                            n = (int)strtol(q, &end, 10);
-                            q = end;
+                            n = (int)strtol(q, &endp, 10);
+                            q = endp;
                         }
                     }
                 }
-                fv.push_back(v - 1);
-                fn.push_back(n - 1);
+                fv[cnt] = v - 1;
+                fn[cnt] = n - 1;
+                cnt++;
                 while (*q == ' ' || *q == '\t' || *q == '\r') q++;
             }
-            for (int i = 0; i + 2 < (int)fv.size(); i++) {
-                ObjGroup &g = groups.back();
-                g.v.insert(g.v.end(), {fv[0], fv[i + 1], fv[i + 2]});
-                g.n.insert(g.n.end(), {fn[0], fn[i + 1], fn[i + 2]});
+            if (*q && cnt == 64) {
+                c.error = file + ": face with more than 64 vertices";
+                return;
+            }
+            for (int i = 0; i + 2 < cnt; i++) {
+                c.fv.insert(c.fv.end(), {fv[0], fv[i + 1], fv[i + 2]});
+                c.fn.insert(c.fn.end(), {fn[0], fn[i + 1], fn[i + 2]});
             }
         }
+    }
+}
+
+// OBJLoader::load + Object::postProcess + Object::apply + Scene::add(Object*), the file parsed in
+// line-aligned chunks on all host threads and the chunks' statements replayed in file order, so
+// the result is that of one sequential pass. Beyond the reference: an OBJ without `vn` lines gets
+// area-weighted vertex normals, and when the normal and vertex counts differ both arrays are
+// transformed in full (the reference indexes normals with the vertex loop, reading past the end
+// of a shorter normal array and leaving the extra normals of a longer one untransformed).
+static tt_status load_obj(const std::string &file, const M4 &xf, Scene &sc) {
+    std::vector<char> buf;
+    {
+        FILE *f = fopen(file.c_str(), "rb");
+        if (!f) return fail(TT_ERR_IO, "cannot read OBJ " + file);
+        std::fseek(f, 0, SEEK_END);
+        const long size = std::ftell(f);
+        std::fseek(f, 0, SEEK_SET);
+        if (size < 0) {
+            fclose(f);
+            return fail(TT_ERR_IO, "cannot read OBJ " + file);
+        }
+        buf.resize((size_t)size + 1);
+        const size_t got = size ? fread(buf.data(), 1, (size_t)size, f) : 0;
+        fclose(f);
+        if (got != (size_t)size) return fail(TT_ERR_IO, "short read of OBJ " + file);
+        buf[(size_t)size] = '\0';
+    }
+    const size_t size = buf.size() - 1;
+    const int nchunks = std::max(1, omp_get_max_threads());
+    std::vector<size_t> cut(nchunks + 1, size);
+    cut[0] = 0;
+    for (int i = 1; i < nchunks; i++) {
+        size_t c = std::max(cut[i - 1], size / nchunks * i);
+        while (c < size && c > 0 && buf[c - 1] != '\n') c++;  // start each chunk at a line start
+        cut[i] = c;
+    }
+    std::vector<ObjChunk> chunks(nchunks);
+#pragma omp parallel for schedule(static, 1)
+    for (int i = 0; i < nchunks; i++) {
+        if (cut[i] < cut[i + 1]) {
+            char *b = buf.data() + cut[i], *e = buf.data() + cut[i + 1];
+            // the chunk's last byte is its last line's '\n' (or the file ends there): that line ends
+            // at a terminator the chunk owns, and the splitter writes only inside [b, e]
+            const char saved = *(e - 1);
+            if (saved == '\n') *(e - 1) = '\0';
+            parse_obj_chunk(b, saved == '\n' ? e - 1 : e, file, chunks[i]);
+        }
+    }
+    std::vector<V3> verts, norms;
+    std::vector<ObjGroup> groups;
+    std::map<std::string, int32_t> pool;
+    bool have_pool = false;
+    auto add_tris = [&](const ObjChunk &c, size_t t0, size_t t1) {
+        if (t1 <= t0) return;
+        if (groups.empty()) groups.emplace_back();
+        ObjGroup &g = groups.back();
+        g.v.insert(g.v.end(), c.fv.begin() + 3 * t0, c.fv.begin() + 3 * t1);
+        g.n.insert(g.n.end(), c.fn.begin() + 3 * t0, c.fn.begin() + 3 * t1);
+    };
+    for (const ObjChunk &c : chunks) {
+        size_t t = 0;
+        for (const ObjEvent &ev : c.ev) {
+            add_tris(c, t, ev.tri);
+            t = ev.tri;
+            if (ev.kind == 0) {
+                groups.emplace_back();
+            } else if (ev.kind == 2) {
+                std::string prefix;
+                size_t slash = file.find_last_of('/');
+                if (slash != std::string::npos) prefix = file.substr(0, slash + 1);
+                tt_status st = load_material_pool(prefix + ev.name, sc, pool);
+                if (st != TT_OK) return st;
+                have_pool = true;
+            } else {
+                if (!have_pool) return fail(TT_ERR_FORMAT, file + ": usemtl before mtllib");
+                auto it = pool.find(ev.name);
+                if (it == pool.end()) return fail(TT_ERR_FORMAT, "Material " + ev.name + " not found");
+                if (groups.empty()) groups.emplace_back();
+                groups.back().mat = it->second;
+            }
+        }
+        add_tris(c, t, c.fv.size() / 3);
+        verts.insert(verts.end(), c.v.begin(), c.v.end());
+        norms.insert(norms.end(), c.vn.begin(), c.vn.end());
+        if (!c.error.empty()) return fail(TT_ERR_FORMAT, c.error);
     }
     if (!have_pool) return fail(TT_ERR_FORMAT, file + ": OBJ has no mtllib (the scene needs its material pool)");
     for (const ObjGroup &g : groups) {
         if (!g.v.empty() && g.mat < 0) return fail(TT_ERR_FORMAT, file + ": group without usemtl");
         for (int32_t i : g.v)
             if (i < 0 || (size_t)i >= verts.size()) return fail(TT_ERR_FORMAT, file + ": face vertex out of range");
+    }
+    if (norms.empty()) {
+        // no normals in the file: area-weighted vertex normals, indexed like the vertices
+        norms.assign(verts.size(), V3(0.0f, 0.0f, 0.0f));
+        for (ObjGroup &g : groups) {
+            for (size_t t = 0; t + 2 < g.v.size(); t += 3) {
+                const V3 &a0 = verts[g.v[t]], &a1 = verts[g.v[t + 1]], &a2 = verts[g.v[t + 2]];
+                const V3 fnrm = cross3(a1 - a0, a2 - a0);
+                for (int k = 0; k < 3; k++) norms[g.v[t + k]] = norms[g.v[t + k]] + fnrm;
+            }
+            g.n = g.v;
+        }
+        for (V3 &n : norms)
+            if (!(dot3(n, n) > 0.0f)) n = V3(0.0f, 1.0f, 0.0f);
+    }
+    for (const ObjGroup &g : groups)
         for (int32_t i : g.n)
             if (i < 0 || (size_t)i >= norms.size()) return fail(TT_ERR_FORMAT, file + ": face normal out of range");
-    }
-    if (norms.size() < verts.size())
-        return fail(TT_ERR_FORMAT, file + ": fewer vn than v lines (the transform needs one normal per vertex)");
 
     // Object::postProcess: centre the face-referenced bounds at the origin, scale into [-1,1].
     V3 minp(FLT_MAX, FLT_MAX, FLT_MAX), maxp(-FLT_MAX, -FLT_MAX, -FLT_MAX);
@@ -450,14 +564,22 @@ static tt_status load_obj(const std::string &file, const M4 &xf, Scene &sc) {
         v = v - c;
         v = v * scale;
     }
-    // Object::apply(Transform): vertices with w = 1, normals with w = 0 then normalised.
-    for (size_t i = 0; i < verts.size(); i++) {
-        float in[4] = {verts[i].x, verts[i].y, verts[i].z, 1.0f}, out[4];
-        xf.apply(in, out);
-        verts[i] = V3(out[0], out[1], out[2]);
-        float nin[4] = {norms[i].x, norms[i].y, norms[i].z, 0.0f};
-        xf.apply(nin, out);
-        norms[i] = normalized(V3(out[0], out[1], out[2]));
+    // Object::apply(Transform): vertices with w = 1, normals with w = 0 then normalised (the
+    // reference's loop over the vertex count when the counts agree, each array in full otherwise)
+    const size_t nn = norms.size() == verts.size() ? verts.size() : norms.size();
+#pragma omp parallel for schedule(static)
+    for (long long i = 0; i < (long long)std::max(verts.size(), nn); i++) {
+        float out[4];
+        if ((size_t)i < verts.size()) {
+            float in[4] = {verts[i].x, verts[i].y, verts[i].z, 1.0f};
+            xf.apply(in, out);
+            verts[i] = V3(out[0], out[1], out[2]);
+        }
+        if ((size_t)i < nn) {
+            float nin[4] = {norms[i].x, norms[i].y, norms[i].z, 0.0f};
+            xf.apply(nin, out);
+            norms[i] = normalized(V3(out[0], out[1], out[2]));
+        }
     }
     // Scene::add(Object*)
     const int32_t vbase = (int32_t)sc.vertices.size(), nbase = (int32_t)sc.normals.size();
