@@ -291,7 +291,8 @@ typedef struct tt_render_params {
 tt_status tt_render_params_default(tt_render_params *out);
 /* Native wavefront path tracer (Lambert, GGX conductor, dielectric, environment light sampling
  * by a 2D CDF with MIS, Russian roulette, PCG32 streams; the reference's own material kinds are
- * mapped as the header of tt_render_native.cu lists). Adds the sum of spp samples of every pixel
+ * mapped as the header of tt_render_native.cu lists; a camera with aperture > 1e-5 is a thin
+ * lens focused at `focal` along the view direction). Adds the sum of spp samples of every pixel
  * to d_accum (width*height*3 floats, or doubles with TT_RENDER_ACCUM_F64; row 0 = the image's top
  * row). The pixel sums are added in sample order, so the result is the same for every launch
  * shape. Launch only; deterministic for given inputs. */
@@ -322,7 +323,8 @@ tt_status tt_renderer_stats(tt_renderer *renderer, uint64_t *out, int32_t reset)
  * to tt_render_native of that view with the batch's parameters and the view's spp, sample
  * offset and seed. */
 typedef struct tt_view {
-    tt_camera_meta cam;    /* image size and pinhole (aperture and focal are not used) */
+    tt_camera_meta cam;    /* image size, pinhole and thin lens (aperture > 1e-5: lens radius, focal:
+                              distance of the focal plane along the view direction) */
     int32_t spp;
     int32_t sample_offset;
     uint32_t seed;

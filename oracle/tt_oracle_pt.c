@@ -399,8 +399,19 @@ static V3 o_path(const World *w, const Cam *cam, float tanx, float tany, const P
     const float jx = o_unif(&g), jy = o_unif(&g);
     const float sx = (2.0f * (((float)px + jx) / (float)cam->width)) - 1.0f;
     const float sy = 1.0f - 2.0f * (((float)py + jy) / (float)cam->height);
-    V3 o = cpos;
-    V3 d = norm3(madd3(up, sy * tany, madd3(right, sx * tanx, view)));
+    const V3 dp = madd3(up, sy * tany, madd3(right, sx * tanx, view));
+    V3 o = cpos, d;
+    if (cam->aperture > 1e-5f) { /* thin lens, as the device raygen */
+        const V3 focus = madd3(dp, cam->focal, cpos);
+        const float u1 = o_unif(&g), u2 = o_unif(&g);
+        const float r = cam->aperture * sqrtf(u1);
+        float sp, cp;
+        o_sincos(KTWOPI * u2, &sp, &cp);
+        o = madd3(up, r * sp, madd3(right, r * cp, cpos));
+        d = norm3(sub3(focus, o));
+    } else {
+        d = norm3(dp);
+    }
     V3 beta = v3(1, 1, 1), L = v3(0, 0, 0);
     int specular = 1;
     float last_pdf = 0.0f;

@@ -40,7 +40,8 @@ struct ViewRec {
     uint64_t seed_state;  // PCG32 initial state of the view's seed
     int width, height, npix, pad;
     float pos[3], view[3], up[3];
-    float tanx, tany, pad2;
+    float tanx, tany;
+    float aperture, focal;  // thin lens (aperture <= 1e-5: pinhole)
 };
 
 struct PathSoA {

@@ -14,7 +14,10 @@
 //
 // The integrator (all of it built from basic IEEE operations, tt_ptmath.cuh):
 //   camera     pinhole of the CameraMeta; pixel (x, y) with y = 0 at the top, jittered by two
-//              PCG32 draws; tan(fov/2) evaluated on the host
+//              PCG32 draws; tan(fov/2) evaluated on the host; with aperture > 1e-5 a thin lens
+//              (two more draws: a point of the lens disc aimed at the pinhole ray's point on the
+//              focal plane, which lies `focal` along the view direction, as in the reference's
+//              camera, src/core/RenderKernel.cu:168-184)
 //   rng        PCG32, stream = global path index (sample * pixels + pixel), state = frame seed
 //   Lambert    cosine sampling (pdf cos/pi), f = albedo/pi
 //   GGX        conductor: alpha = roughness^2, Trowbridge-Reitz D, separable Smith G, Schlick F
@@ -436,8 +439,21 @@ __global__ void __launch_bounds__(kShadeBlockMax) k_raygen(NativeArgs a) {
         const float jx = uniform(rg), jy = uniform(rg);
         const float sx = PT_SUB(PT_MUL(2.0f, PT_DIV(PT_ADD((float)px, jx), (float)vw.width)), 1.0f);
         const float sy = PT_SUB(1.0f, PT_MUL(2.0f, PT_DIV(PT_ADD((float)py, jy), (float)vw.height)));
-        const V3 dir = normalize(madd(up, PT_MUL(sy, vw.tany), madd(right, PT_MUL(sx, vw.tanx), view)));
-        put_ray(a.ps.ray[0], i, cam_pos, dir);
+        const V3 dp = madd(up, PT_MUL(sy, vw.tany), madd(right, PT_MUL(sx, vw.tanx), view));
+        V3 org = cam_pos, dir;
+        if (vw.aperture > 1e-5f) {
+            // thin lens: aim at the pinhole ray's point on the focal plane from a point of the lens disc
+            const V3 focus = madd(dp, vw.focal, cam_pos);
+            const float u1 = uniform(rg), u2 = uniform(rg);
+            const float r = PT_MUL(vw.aperture, PT_SQRT(u1));
+            float sp, cp;
+            sincos(PT_MUL(kTwoPi, u2), sp, cp);
+            org = madd(up, PT_MUL(r, sp), madd(right, PT_MUL(r, cp), cam_pos));
+            dir = normalize(sub(focus, org));
+        } else {
+            dir = normalize(dp);
+        }
+        put_ray(a.ps.ray[0], i, org, dir);
         st3(a.ps.beta + 3ll * i, V3(1.f, 1.f, 1.f));
         st3(a.ps.L + 3ll * i, V3(0.f, 0.f, 0.f));
         a.ps.rng[i] = rg.state;
@@ -813,6 +829,8 @@ static ViewRec make_view(const tt_camera_meta &cam, int spp, int sample_offset, 
     }
     v.tanx = (float)std::tan((double)cam.fov[0] * 0.5 * 3.14159265358979323846 / 180.0);
     v.tany = (float)std::tan((double)cam.fov[1] * 0.5 * 3.14159265358979323846 / 180.0);
+    v.aperture = cam.aperture;
+    v.focal = cam.focal;
     return v;
 }
 
