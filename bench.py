@@ -151,10 +151,34 @@ def cpu_baseline(bvh_arrays: dict, rays: np.ndarray, sample: int, want_counters:
             "counters": o.get("counters")}
 
 
+def rank_info() -> tuple[int, int, int]:
+    """(world size, rank, local rank) from the torchrun environment (1, 0, 0 without it)."""
+    return (int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def max_over_ranks(ms: float, world: int, device) -> float:
+    """The slowest rank's time: every rank times its own replica; the job takes as long as the
+    slowest one (all_reduce MAX over the default process group when world > 1)."""
+    if world <= 1:
+        return float(ms)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank: float, ms: float, world: int) -> float:
+    """The whole job's throughput in millions of units per second when each of `world`
+    replicas processes `units_per_rank` units in `ms` milliseconds."""
+    return world * units_per_rank / ms / 1e3
+
+
 def run_reference(args) -> None:
     """--impl reference: the reference's traversal on the host cores (the oracle port with the
     reference's plain float arithmetic, OpenMP), on this arm's workload and metric."""
-    rank = int(os.environ.get("RANK", "0"))
+    _, rank, _ = rank_info()
     if rank != 0:
         return
     from trenchanttracer_gb300 import scenes
@@ -192,9 +216,7 @@ def run_ours(args) -> None:
     import torch
     import torch.distributed as dist
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+    world, rank, local = rank_info()
     if world > 1:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     torch.cuda.set_device(local)
@@ -253,12 +275,8 @@ def run_ours(args) -> None:
             dist.barrier()
     dbvh.check(s)
     clocks = clk.summary()
-    ms = float(np.sum(step_ms)) / args.steps
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * n_rays / ms / 1e3  # whole-job Mrays/s
+    ms = max_over_ranks(float(np.sum(step_ms)) / args.steps, world, dev)
+    value = whole_job_rate(n_rays, ms, world)  # whole-job Mrays/s
 
     # end to end through the host-buffer entry point (pinned host memory)
     h_sets = [torch.from_numpy(primary).pin_memory(), torch.from_numpy(secondary).pin_memory()]
@@ -280,7 +298,7 @@ def run_ours(args) -> None:
         t0 = time.perf_counter()
         e2e_step()
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
-    e2e_val = world * n_rays / (float(np.mean(e2e_ms))) / 1e3
+    e2e_val = whole_job_rate(n_rays, max_over_ranks(float(np.mean(e2e_ms)), world, dev), world)
     # device and host paths agree bit for bit
     ids_d, t_d = hits_to_numpy(hits[1].cpu().numpy())
     ids_h, t_h = hits_to_numpy(h_hits[1].numpy())

@@ -55,14 +55,25 @@ def sources() -> list[Path]:
 
 
 def build(force: bool = False, verbose: bool = False) -> Path:
-    """Compile and link libtt.so if any source is newer than the library."""
+    """Compile and link libtt.so if any source is newer than the library. Concurrent callers
+    (several ranks starting at once) serialise on a lock file, and only the first compiles."""
+    import fcntl
+    BUILD.mkdir(exist_ok=True)
+    with open(BUILD / ".lock", "w") as lock:
+        fcntl.flock(lock, fcntl.LOCK_EX)
+        try:
+            return _build_locked(force, verbose)
+        finally:
+            fcntl.flock(lock, fcntl.LOCK_UN)
+
+
+def _build_locked(force: bool, verbose: bool) -> Path:
     cuda = _cuda_home()
     srcs = sources()
     headers = [*CSRC.glob("*.h"), *CSRC.glob("*.cuh"), *(REPO / "include").glob("*.h")]
     newest = max(p.stat().st_mtime for p in [*srcs, *headers, Path(__file__)])
     if LIB.exists() and not force and LIB.stat().st_mtime >= newest:
         return LIB
-    BUILD.mkdir(exist_ok=True)
     jobs = min(len(srcs), os.cpu_count() or 4)
     with cf.ThreadPoolExecutor(jobs) as ex:
         futs = [ex.submit(_compile, s, BUILD / (s.name + ".o"), cuda) for s in srcs]
