@@ -678,11 +678,11 @@ namespace tt {
 namespace nrc {
 
 tt_status cache_infer_device(tt_cache *c, const float *rec, const int *n_dev, long long cap, float *rgb, int use_ema,
-                             cudaStream_t s) {
+                             unsigned *err, cudaStream_t s) {
     if (c->p.mma_kind == 0) {
         const Encoding e = encoding_of(c->p);
-        return tc_infer(use_ema ? c->w_tc_ema : c->w_tc_train, rec, 0, n_dev, cap, e.lo, e.inv_ext, rgb, c->err,
-                        c->num_sms, s);
+        return tc_infer(use_ema ? c->w_tc_ema : c->w_tc_train, rec, 0, n_dev, cap, e.lo, e.inv_ext, rgb,
+                        err ? err : c->err, c->num_sms, s);
     }
     MlpArgs a;
     std::memset(&a, 0, sizeof(a));

@@ -493,7 +493,8 @@ tt_status tt_renderer_check(tt_renderer *r, void *stream) {
     if (w) {
         TT_CUDA_R(cudaMemset(r->err, 0, 4));
         if (w & kErrStack) return fail(TT_ERR_BOUNDS, "traversal stack overflow during rendering");
-        return fail(TT_ERR_TIMEOUT, "traversal iteration cap reached during rendering");
+        if (w & kErrIter) return fail(TT_ERR_TIMEOUT, "traversal iteration cap reached during rendering");
+        return fail(TT_ERR_TIMEOUT, "a radiance-cache tensor-core wait ran out during rendering");
     }
     return TT_OK;
 }

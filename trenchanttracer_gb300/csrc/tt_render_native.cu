@@ -892,7 +892,7 @@ static tt_status issue(NativeArgs a, long long total, const Launch &L, void *acc
         }
         if (cache) {  // every path queries at most once, so all queries of the wave fit
             const tt_status st = nrc::cache_infer_device(cache, a.cache.q_rec, a.cache.counts, a.wave_paths,
-                                                         a.cache.q_rgb, nrc::cache_params(cache).use_ema, s);
+                                                         a.cache.q_rgb, nrc::cache_params(cache).use_ema, a.err, s);
             if (st != TT_OK) return st;
             k_cache_resolve<<<L.grid_shade, L.block, 0, s>>>(a);
         }
