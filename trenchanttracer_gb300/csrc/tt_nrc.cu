@@ -59,52 +59,17 @@ struct Encoding {
     float lo[3], inv_ext[3];
 };
 
-// Values of record `rec` into one encoding row: part 0 = the position block [0, 72), part 1 =
-// everything else [72, 160).
+// Values of record `rec` into one encoding row (16-byte aligned): part 0 = chunks 0..8 (the
+// position block [0, 72)), part 1 = chunks 9..19 (everything else).
 __device__ __forceinline__ void encode_part(const float *rec, const Encoding &e, __nv_bfloat16 *dst, int part) {
+    const EncInputs in = enc_inputs(rec, e.lo, e.inv_ext);
+    uint4 *d4 = reinterpret_cast<uint4 *>(dst);
     if (part == 0) {
 #pragma unroll
-        for (int i = 0; i < 3; i++) {
-            float f = (rec[i] - e.lo[i]) * e.inv_ext[i];
-            for (int k = 0; k < kPosFreq; k++) {
-                float s, c;
-                sincospif(f, &s, &c);
-                dst[24 * i + 2 * k] = __float2bfloat16_rn(s);
-                dst[24 * i + 2 * k + 1] = __float2bfloat16_rn(c);
-                f *= 2.0f;
-            }
-        }
+        for (int c = 0; c < 9; c++) d4[c] = enc_chunk(in, rec, c);
     } else {
 #pragma unroll
-        for (int i = 0; i < 3; i++) {
-            float fd = (rec[3 + i] + 1.0f) * 0.5f, fn = (rec[6 + i] + 1.0f) * 0.5f;
-            for (int k = 0; k < kDirFreq; k++) {
-                float s, c;
-                sincospif(fd, &s, &c);
-                dst[72 + 12 * i + 2 * k] = __float2bfloat16_rn(s);
-                dst[72 + 12 * i + 2 * k + 1] = __float2bfloat16_rn(c);
-                sincospif(fn, &s, &c);
-                dst[108 + 12 * i + 2 * k] = __float2bfloat16_rn(s);
-                dst[108 + 12 * i + 2 * k + 1] = __float2bfloat16_rn(c);
-                fd *= 2.0f;
-                fn *= 2.0f;
-            }
-        }
-        float tail[16];
-        tail[0] = rec[9];
-        tail[1] = rec[10];
-        tail[2] = rec[11];
-        tail[3] = rec[12];
-        tail[4] = 1.0f;
-        for (int i = 0; i < 3; i++) {
-            tail[5 + i] = rec[3 + i];
-            tail[8 + i] = rec[6 + i];
-            tail[11 + i] = (rec[i] - e.lo[i]) * e.inv_ext[i];
-        }
-        tail[14] = rec[13];
-        tail[15] = 0.0f;
-#pragma unroll
-        for (int i = 0; i < 16; i++) dst[144 + i] = __float2bfloat16_rn(tail[i]);
+        for (int c = 9; c < 20; c++) d4[c] = enc_chunk(in, rec, c);
     }
 }
 

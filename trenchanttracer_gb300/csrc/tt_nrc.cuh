@@ -12,6 +12,10 @@
 
 #include <cstdint>
 
+#ifdef __CUDACC__
+#include <cuda_bf16.h>
+#endif
+
 namespace tt {
 namespace nrc {
 
@@ -46,6 +50,75 @@ __host__ __device__ constexpr int p_offset(int l) {
 constexpr int kParams = w_offset(kLayers);     // 27136
 constexpr int kPadded = p_offset(kLayers);     // 29760 bf16 = 59520 bytes
 static_assert(kParams == 160 * 64 + 4 * 64 * 64 + 8 * 64, "parameter count");
+
+#ifdef __CUDACC__
+// sin(pi x) and cos(pi x): the argument reduced exactly to r = x - 2 rint(x / 2) in [-1, 1],
+// then the hardware approximations of sin and cos of pi r (absolute error ~4e-7, far below the
+// BF16 step of the encoding).
+__device__ __forceinline__ void sincospi_fast(float x, float &s, float &c) {
+    const float r = x - 2.0f * rintf(0.5f * x);
+    __sincosf(r * 3.14159265358979f, &s, &c);
+}
+
+// The per-record inputs of the encoding: normalised position, (wo + 1) / 2, (n + 1) / 2.
+struct EncInputs {
+    float ph[3], xd[3], xn[3];
+};
+
+__device__ __forceinline__ EncInputs enc_inputs(const float *rec, const float lo[3], const float inv_ext[3]) {
+    EncInputs in;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        in.ph[i] = (rec[i] - lo[i]) * inv_ext[i];
+        in.xd[i] = (rec[3 + i] + 1.0f) * 0.5f;
+        in.xn[i] = (rec[6 + i] + 1.0f) * 0.5f;
+    }
+    return in;
+}
+
+__device__ __forceinline__ uint32_t enc_pack(float lo, float hi) {
+    const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<const uint32_t *>(&v);
+}
+
+// Encoding values [8 c, 8 c + 8) as four packed BF16 pairs (c = 0..19; with c a compile-time
+// constant after unrolling, the index arithmetic folds away).
+__device__ __forceinline__ uint4 enc_chunk(const EncInputs &in, const float *rec, int c) {
+    uint32_t w[4];
+    if (c < 18) {
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const int idx = 8 * c + 2 * j;
+            float src;
+            int k;
+            if (idx < 72) {
+                src = in.ph[idx / 24];
+                k = (idx % 24) / 2;
+            } else if (idx < 108) {
+                src = in.xd[(idx - 72) / 12];
+                k = ((idx - 72) % 12) / 2;
+            } else {
+                src = in.xn[(idx - 108) / 12];
+                k = ((idx - 108) % 12) / 2;
+            }
+            float sv, cv;
+            sincospi_fast(src * (float)(1 << k), sv, cv);
+            w[j] = enc_pack(sv, cv);
+        }
+    } else if (c == 18) {  // roughness, albedo, 1, wo
+        w[0] = enc_pack(rec[9], rec[10]);
+        w[1] = enc_pack(rec[11], rec[12]);
+        w[2] = enc_pack(1.0f, rec[3]);
+        w[3] = enc_pack(rec[4], rec[5]);
+    } else {  // normal, p_hat, kind, 0
+        w[0] = enc_pack(rec[6], rec[7]);
+        w[1] = enc_pack(rec[8], in.ph[0]);
+        w[2] = enc_pack(in.ph[1], in.ph[2]);
+        w[3] = enc_pack(rec[13], 0.0f);
+    }
+    return make_uint4(w[0], w[1], w[2], w[3]);
+}
+#endif
 
 }  // namespace nrc
 }  // namespace tt

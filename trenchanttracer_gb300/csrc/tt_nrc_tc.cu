@@ -141,55 +141,12 @@ struct TcEncoding {
     float lo[3], inv_ext[3];
 };
 
-// the encoding of tt_nrc.cuh, one row, straight into the A operand
+// the encoding of tt_nrc.cuh, one row, straight into the A operand: 20 chunks of 8 BF16 values,
+// each one 16-byte store (the 32 rows of a warp write 512 contiguous bytes per chunk)
 __device__ __forceinline__ void encode_row(const float *rec, const TcEncoding &e, __nv_bfloat16 *A, int r) {
+    const EncInputs in = enc_inputs(rec, e.lo, e.inv_ext);
 #pragma unroll
-    for (int i = 0; i < 3; i++) {
-        float f = (rec[i] - e.lo[i]) * e.inv_ext[i];
-        for (int k = 0; k < kPosFreq; k++) {
-            float s, c;
-            sincospif(f, &s, &c);
-            A[a_offset(r, 24 * i + 2 * k)] = __float2bfloat16_rn(s);
-            A[a_offset(r, 24 * i + 2 * k + 1)] = __float2bfloat16_rn(c);
-            f *= 2.0f;
-        }
-    }
-#pragma unroll
-    for (int i = 0; i < 3; i++) {
-        float fd = (rec[3 + i] + 1.0f) * 0.5f, fn = (rec[6 + i] + 1.0f) * 0.5f;
-        for (int k = 0; k < kDirFreq; k++) {
-            float s, c;
-            sincospif(fd, &s, &c);
-            A[a_offset(r, 72 + 12 * i + 2 * k)] = __float2bfloat16_rn(s);
-            A[a_offset(r, 72 + 12 * i + 2 * k + 1)] = __float2bfloat16_rn(c);
-            sincospif(fn, &s, &c);
-            A[a_offset(r, 108 + 12 * i + 2 * k)] = __float2bfloat16_rn(s);
-            A[a_offset(r, 108 + 12 * i + 2 * k + 1)] = __float2bfloat16_rn(c);
-            fd *= 2.0f;
-            fn *= 2.0f;
-        }
-    }
-    float tail[16];
-    tail[0] = rec[9];
-    tail[1] = rec[10];
-    tail[2] = rec[11];
-    tail[3] = rec[12];
-    tail[4] = 1.0f;
-    for (int i = 0; i < 3; i++) {
-        tail[5 + i] = rec[3 + i];
-        tail[8 + i] = rec[6 + i];
-        tail[11 + i] = (rec[i] - e.lo[i]) * e.inv_ext[i];
-    }
-    tail[14] = rec[13];
-    tail[15] = 0.0f;
-    uint32_t w[8];
-#pragma unroll
-    for (int j = 0; j < 8; j++) {
-        const __nv_bfloat162 b = __floats2bfloat162_rn(tail[2 * j], tail[2 * j + 1]);
-        w[j] = *reinterpret_cast<const uint32_t *>(&b);
-    }
-    *reinterpret_cast<uint4 *>(A + a_offset(r, 144)) = make_uint4(w[0], w[1], w[2], w[3]);
-    *reinterpret_cast<uint4 *>(A + a_offset(r, 152)) = make_uint4(w[4], w[5], w[6], w[7]);
+    for (int c = 0; c < 20; c++) *reinterpret_cast<uint4 *>(A + a_offset(r, 8 * c)) = enc_chunk(in, rec, c);
 }
 
 struct TcArgs {
