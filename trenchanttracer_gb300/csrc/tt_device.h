@@ -21,6 +21,10 @@ struct tt_renderer {
     int num_materials = 0;
     tt::GeomRec *geoms = nullptr;
     int num_geoms = 0;
+    // the native tracer's bounding-box hierarchy over the analytic objects (more than a few):
+    // num_geom_nodes GeomNode records followed by num_geoms object indices, one allocation
+    void *geom_tree = nullptr;
+    int num_geom_nodes = 0;
     float4 *env = nullptr;  // env_w * env_h radiance texels (w = 0: no environment)
     int env_w = 0, env_h = 0;
     unsigned int *err = nullptr;  // 256 bytes: error word at 0, native ray counters at byte 64
@@ -50,7 +54,8 @@ inline unsigned long long *renderer_stats(tt_renderer *r) {
 }  // namespace tt
 
 namespace tt {
-// Builds the environment's sampling tables (called by tt_renderer_create) / frees native state.
-tt_status native_setup(tt_renderer *r);
+// Builds the environment's sampling tables and the analytic objects' box hierarchy (called by
+// tt_renderer_create with the scene's objects) / frees native state.
+tt_status native_setup(tt_renderer *r, const std::vector<GeomRec> &geoms);
 void native_release(tt_renderer *r);
 }  // namespace tt

@@ -100,6 +100,8 @@ struct NativeArgs {
     unsigned int *err;
     unsigned long long *stats;  // [0] extension rays, [1] shadow rays, [2] paths
     CacheView cache;
+    const struct GeomNode *gnodes;  // box hierarchy over the analytic objects, or nullptr
+    const int *gidx;
 };
 
 __device__ __forceinline__ int find_view(const NativeArgs &a, long long g) {
@@ -115,47 +117,92 @@ __device__ __forceinline__ int find_view(const NativeArgs &a, long long g) {
 
 __device__ __forceinline__ ViewRec view_of(const NativeArgs &a, int v) { return a.views ? a.views[v] : a.view0; }
 
-// Closest hit among the analytic objects (brute force over all of them, as the reference does).
-__device__ __forceinline__ void analytic_hit(const NativeArgs &a, const V3 &o, const V3 &d, float tmin,
+// A node of the box hierarchy over the analytic objects: an inner node (count == 0) has its
+// children at `first` and `first + 1`; a leaf holds objects gidx[first .. first + count).
+struct GeomNode {
+    float lo[3];
+    int first;
+    float hi[3];
+    int count;
+};
+static_assert(sizeof(GeomNode) == 32, "GeomNode must stay 32 B");
+constexpr int kGeomStack = 64;
+
+// The exact test of analytic object i (the reference's Plane / Sphere tests); a hit nearer than
+// t replaces the current one, and an equally near one replaces it only when it is an analytic
+// object of higher index, so any visiting order gives the result of the reference's loop over
+// the objects in index order.
+__device__ __forceinline__ void analytic_one(const NativeArgs &a, int i, const V3 &o, const V3 &d, float tmin,
                                              float &t, int &prim, float &hu, float &hv) {
     using namespace pt;
-    for (int i = 0; i < a.num_geoms; i++) {
-        const GeomRec g = a.geoms[i];
-        if (g.kind == GEOM_PLANE) {
-            const V3 p0(g.p0[0], g.p0[1], g.p0[2]);
-            const V3 e1 = sub(V3(g.p1[0], g.p1[1], g.p1[2]), p0), e2 = sub(V3(g.p2[0], g.p2[1], g.p2[2]), p0);
-            const V3 P = cross(d, e2);
-            const float det = dot(e1, P);
-            if (det > -1e-12f && det < 1e-12f) continue;
-            const float inv = PT_DIV(1.0f, det);
-            const V3 T = sub(o, p0);
-            const float u = PT_MUL(dot(T, P), inv);
-            if (u < 0.f || u > 1.f) continue;
-            const V3 Q = cross(T, e1);
-            const float v = PT_MUL(dot(d, Q), inv);
-            if (v < 0.f || v > 1.f) continue;
-            const float th = PT_MUL(dot(e2, Q), inv);
-            if (th > tmin && th < t) {
-                t = th;
-                prim = -(i + 2);
-                hu = u;
-                hv = v;
-            }
-        } else if (g.kind == GEOM_SPHERE) {
-            const V3 c(g.p0[0], g.p0[1], g.p0[2]);
-            const V3 oc = sub(c, o);
-            const float bq = dot(oc, d);
-            const float disc = PT_FMA(g.radius, g.radius, PT_FMA(bq, bq, -dot(oc, oc)));
-            if (disc < 0.0f) continue;
-            const float sq = PT_SQRT(disc);
-            float th = PT_SUB(bq, sq);
-            if (!(th > tmin)) th = PT_ADD(bq, sq);
-            if (th > tmin && th < t) {
-                t = th;
-                prim = -(i + 2);
-                hu = 0.f;
-                hv = 0.f;
-            }
+    const GeomRec g = a.geoms[i];
+    float th, u = 0.f, v = 0.f;
+    if (g.kind == GEOM_PLANE) {
+        const V3 p0(g.p0[0], g.p0[1], g.p0[2]);
+        const V3 e1 = sub(V3(g.p1[0], g.p1[1], g.p1[2]), p0), e2 = sub(V3(g.p2[0], g.p2[1], g.p2[2]), p0);
+        const V3 P = cross(d, e2);
+        const float det = dot(e1, P);
+        if (det > -1e-12f && det < 1e-12f) return;
+        const float inv = PT_DIV(1.0f, det);
+        const V3 T = sub(o, p0);
+        u = PT_MUL(dot(T, P), inv);
+        if (u < 0.f || u > 1.f) return;
+        const V3 Q = cross(T, e1);
+        v = PT_MUL(dot(d, Q), inv);
+        if (v < 0.f || v > 1.f) return;
+        th = PT_MUL(dot(e2, Q), inv);
+    } else if (g.kind == GEOM_SPHERE) {
+        const V3 c(g.p0[0], g.p0[1], g.p0[2]);
+        const V3 oc = sub(c, o);
+        const float bq = dot(oc, d);
+        const float disc = PT_FMA(g.radius, g.radius, PT_FMA(bq, bq, -dot(oc, oc)));
+        if (disc < 0.0f) return;
+        const float sq = PT_SQRT(disc);
+        th = PT_SUB(bq, sq);
+        if (!(th > tmin)) th = PT_ADD(bq, sq);
+    } else {
+        return;
+    }
+    if (th > tmin && (th < t || (th == t && prim <= -2 && i < -prim - 2))) {
+        t = th;
+        prim = -(i + 2);
+        hu = u;
+        hv = v;
+    }
+}
+
+// Closest hit among the analytic objects: the reference's loop over all of them, or, when the
+// renderer holds a box hierarchy over them, its traversal (boxes padded on the host so that no
+// hit the exact tests accept is culled; a stack that would overflow falls back to the loop).
+__device__ __forceinline__ void analytic_hit(const NativeArgs &a, const V3 &o, const V3 &d, float tmin,
+                                             float &t, int &prim, float &hu, float &hv) {
+    if (!a.gnodes) {
+        for (int i = 0; i < a.num_geoms; i++) analytic_one(a, i, o, d, tmin, t, prim, hu, hv);
+        return;
+    }
+    const float ix = 1.0f / (fabsf(d.x) > 1e-20f ? d.x : copysignf(1e-20f, d.x));
+    const float iy = 1.0f / (fabsf(d.y) > 1e-20f ? d.y : copysignf(1e-20f, d.y));
+    const float iz = 1.0f / (fabsf(d.z) > 1e-20f ? d.z : copysignf(1e-20f, d.z));
+    int stack[kGeomStack];
+    int sp = 0;
+    stack[sp++] = 0;
+    while (sp > 0) {
+        const GeomNode nd = a.gnodes[stack[--sp]];
+        const float tx0 = (nd.lo[0] - o.x) * ix, tx1 = (nd.hi[0] - o.x) * ix;
+        const float ty0 = (nd.lo[1] - o.y) * iy, ty1 = (nd.hi[1] - o.y) * iy;
+        const float tz0 = (nd.lo[2] - o.z) * iz, tz1 = (nd.hi[2] - o.z) * iz;
+        const float entry = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fminf(tz0, tz1));
+        const float exit = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1));
+        const float slack = 1e-4f * fmaxf(fabsf(entry), fabsf(exit)) + 1e-6f;
+        if (!(entry <= exit + slack && exit + slack >= tmin && entry - slack <= t)) continue;
+        if (nd.count > 0) {
+            for (int k = 0; k < nd.count; k++) analytic_one(a, a.gidx[nd.first + k], o, d, tmin, t, prim, hu, hv);
+        } else if (sp + 2 <= kGeomStack) {
+            stack[sp++] = nd.first + 1;
+            stack[sp++] = nd.first;
+        } else {  // deeper than the stack: every object, as the reference does
+            for (int i = 0; i < a.num_geoms; i++) analytic_one(a, i, o, d, tmin, t, prim, hu, hv);
+            return;
         }
     }
 }

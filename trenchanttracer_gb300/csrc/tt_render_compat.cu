@@ -445,7 +445,7 @@ tt_status tt_renderer_create(const tt_dbvh *bvh, const tt_scene *scene, tt_rende
     r->num_geoms = (int)sc.geoms.size();
     r->env_w = sc.env_w;
     r->env_h = sc.env_h;
-    tt_status st = native_setup(r);
+    tt_status st = native_setup(r, sc.geoms);
     if (st != TT_OK) {
         renderer_release(r);
         delete r;

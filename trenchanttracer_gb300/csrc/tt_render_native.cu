@@ -33,6 +33,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -675,10 +676,100 @@ static tt_status cuda_fail_n(cudaError_t e, const char *what) {
         if (e_ != cudaSuccess) return cuda_fail_n(e_, #call); \
     } while (0)
 
-tt_status native_setup(tt_renderer *r) {
+// Median-split box hierarchy over more than kGeomBrute analytic objects (leaves of at most two).
+// Each box is grown by 1e-4 of its extent plus its largest coordinate, so that a hit point the
+// exact float tests accept always lies inside its object's box.
+constexpr int kGeomBrute = 4;
+
+static void geom_box(const GeomRec &g, float lo[3], float hi[3]) {
+    for (int k = 0; k < 3; k++) {
+        if (g.kind == GEOM_SPHERE) {
+            lo[k] = g.p0[k] - g.radius;
+            hi[k] = g.p0[k] + g.radius;
+        } else {  // parallelogram p0, p1, p2, p1 + p2 - p0
+            const float p3 = g.p1[k] + g.p2[k] - g.p0[k];
+            lo[k] = std::min(std::min(g.p0[k], g.p1[k]), std::min(g.p2[k], p3));
+            hi[k] = std::max(std::max(g.p0[k], g.p1[k]), std::max(g.p2[k], p3));
+        }
+    }
+    float ext = 0.0f, mag = 0.0f;
+    for (int k = 0; k < 3; k++) {
+        ext = std::max(ext, hi[k] - lo[k]);
+        mag = std::max(mag, std::max(std::fabs(lo[k]), std::fabs(hi[k])));
+    }
+    const float pad = 1e-4f * (ext + mag) + 1e-6f;
+    for (int k = 0; k < 3; k++) {
+        lo[k] -= pad;
+        hi[k] += pad;
+    }
+}
+
+static tt_status build_geom_tree(tt_renderer *r, const std::vector<GeomRec> &geoms) {
+    const int n = (int)geoms.size();
+    if (n <= kGeomBrute) return TT_OK;
+    std::vector<std::array<float, 6>> box(n);
+    std::vector<int> idx(n);
+    for (int i = 0; i < n; i++) {
+        geom_box(geoms[i], box[i].data(), box[i].data() + 3);
+        idx[i] = i;
+    }
+    std::vector<GeomNode> nodes(1);
+    struct Item {
+        int node, b, e;
+    };
+    std::vector<Item> todo{{0, 0, n}};
+    while (!todo.empty()) {
+        const Item it = todo.back();
+        todo.pop_back();
+        GeomNode nd;
+        float clo[3] = {3e38f, 3e38f, 3e38f}, chi[3] = {-3e38f, -3e38f, -3e38f};
+        for (int k = 0; k < 3; k++) {
+            nd.lo[k] = 3e38f;
+            nd.hi[k] = -3e38f;
+        }
+        for (int j = it.b; j < it.e; j++)
+            for (int k = 0; k < 3; k++) {
+                const auto &bx = box[idx[j]];
+                nd.lo[k] = std::min(nd.lo[k], bx[k]);
+                nd.hi[k] = std::max(nd.hi[k], bx[3 + k]);
+                const float c = 0.5f * (bx[k] + bx[3 + k]);
+                clo[k] = std::min(clo[k], c);
+                chi[k] = std::max(chi[k], c);
+            }
+        if (it.e - it.b <= 2) {
+            nd.first = it.b;
+            nd.count = it.e - it.b;
+        } else {
+            int axis = 0;
+            for (int k = 1; k < 3; k++)
+                if (chi[k] - clo[k] > chi[axis] - clo[axis]) axis = k;
+            const int mid = (it.b + it.e) / 2;
+            std::nth_element(idx.begin() + it.b, idx.begin() + mid, idx.begin() + it.e, [&](int x, int y) {
+                const float cx = box[x][axis] + box[x][3 + axis], cy = box[y][axis] + box[y][3 + axis];
+                return cx < cy || (cx == cy && x < y);
+            });
+            nd.first = (int)nodes.size();
+            nd.count = 0;
+            nodes.resize(nodes.size() + 2);
+            todo.push_back({nd.first + 1, mid, it.e});
+            todo.push_back({nd.first, it.b, mid});
+        }
+        nodes[it.node] = nd;
+    }
+    const size_t nb = sizeof(GeomNode) * nodes.size(), ib = sizeof(int) * idx.size();
+    TT_CUDA_N(cudaMalloc(&r->geom_tree, nb + ib));
+    TT_CUDA_N(cudaMemcpy(r->geom_tree, nodes.data(), nb, cudaMemcpyHostToDevice));
+    TT_CUDA_N(cudaMemcpy(static_cast<char *>(r->geom_tree) + nb, idx.data(), ib, cudaMemcpyHostToDevice));
+    r->num_geom_nodes = (int)nodes.size();
+    return TT_OK;
+}
+
+tt_status native_setup(tt_renderer *r, const std::vector<GeomRec> &geoms) {
     int dev = 0;
     TT_CUDA_N(cudaGetDevice(&dev));
     TT_CUDA_N(cudaDeviceGetAttribute(&r->num_sms, cudaDevAttrMultiProcessorCount, dev));
+    const tt_status gst = build_geom_tree(r, geoms);
+    if (gst != TT_OK) return gst;
     if (r->env_w <= 0) return TT_OK;
     const int w = r->env_w, h = r->env_h;
     TT_CUDA_N(cudaMalloc(&r->env_marg, sizeof(float) * (h + 1)));
@@ -698,6 +789,9 @@ void native_release(tt_renderer *r) {
     if (r->env_cond) cudaFree(r->env_cond);
     if (r->paths) cudaFree(r->paths);
     if (r->cache_mem) cudaFree(r->cache_mem);
+    if (r->geom_tree) cudaFree(r->geom_tree);
+    r->geom_tree = nullptr;
+    r->num_geom_nodes = 0;
     r->env_marg = r->env_cond = nullptr;
     r->paths = nullptr;
     r->paths_bytes = 0;
@@ -856,6 +950,11 @@ static NativeArgs base_args(tt_renderer *r, const tt_render_params &p, const Pat
     a.num_materials = r->num_materials;
     a.geoms = r->geoms;
     a.num_geoms = r->num_geoms;
+    if (r->geom_tree) {
+        a.gnodes = static_cast<const GeomNode *>(r->geom_tree);
+        a.gidx = reinterpret_cast<const int *>(static_cast<const char *>(r->geom_tree) +
+                                               sizeof(GeomNode) * r->num_geom_nodes);
+    }
     a.env.tex = r->env;
     a.env.marg = r->env_marg;
     a.env.cond = r->env_cond;
