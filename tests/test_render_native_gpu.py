@@ -185,7 +185,7 @@ def _many_analytic_objects(seed: int = 9) -> list:
 
 
 def test_native_box_hierarchy_over_many_analytic_objects_matches_oracle():
-    """More than four analytic objects go through the native tracer's box hierarchy instead of a
+    """More than 32 analytic objects go through the native tracer's box hierarchy instead of a
     loop over all of them per ray; the image must stay bit-identical to the oracle's loop."""
     mesh, _ = scenes.material_showcase(subdiv=2)
     sc = Scene.from_mesh(mesh)

@@ -117,8 +117,9 @@ __device__ __forceinline__ int find_view(const NativeArgs &a, long long g) {
 
 __device__ __forceinline__ ViewRec view_of(const NativeArgs &a, int v) { return a.views ? a.views[v] : a.view0; }
 
-// A node of the box hierarchy over the analytic objects: an inner node (count == 0) has its
-// children at `first` and `first + 1`; a leaf holds objects gidx[first .. first + count).
+// A node of the box hierarchy over the analytic objects: an inner node (count = -1 - split axis)
+// has its children at `first` (lower centroids along the axis) and `first + 1`; a leaf holds
+// objects gidx[first .. first + count).
 struct GeomNode {
     float lo[3];
     int first;
@@ -171,37 +172,68 @@ __device__ __forceinline__ void analytic_one(const NativeArgs &a, int i, const V
     }
 }
 
-// Closest hit among the analytic objects: the reference's loop over all of them, or, when the
-// renderer holds a box hierarchy over them, its traversal (boxes padded on the host so that no
-// hit the exact tests accept is culled; a stack that would overflow falls back to the loop).
-__device__ __forceinline__ void analytic_hit(const NativeArgs &a, const V3 &o, const V3 &d, float tmin,
-                                             float &t, int &prim, float &hu, float &hv) {
+// Hits among the analytic objects for the lanes of `mask` (every lane of `mask` calls this
+// together; `live` lanes want the test): the closest one, or with any_hit whether there is one
+// below t (prim != -1 afterwards). Without a box hierarchy, the reference's loop over all objects.
+// With one, the warp walks the hierarchy together: it enters a node when the node's box passes
+// the box test of any live lane, so node and object reads are the same address across the warp,
+// and each lane tests a leaf's objects only when its own ray passes the leaf's box. The boxes
+// are padded on the host so that no hit the exact tests accept is culled; a warp never tests
+// more objects than the loop would, and a stack that would overflow falls back to the loop.
+__device__ __forceinline__ void analytic_hit(const NativeArgs &a, unsigned mask, bool live, const V3 &o,
+                                             const V3 &d, float tmin, float &t, int &prim, float &hu, float &hv,
+                                             bool any_hit) {
     if (!a.gnodes) {
-        for (int i = 0; i < a.num_geoms; i++) analytic_one(a, i, o, d, tmin, t, prim, hu, hv);
+        if (!live) return;
+        for (int i = 0; i < a.num_geoms; i++) {
+            analytic_one(a, i, o, d, tmin, t, prim, hu, hv);
+            if (any_hit && prim != -1) return;
+        }
         return;
     }
+    const unsigned live_m = __ballot_sync(mask, live);
+    if (!live_m) return;
+    // the warp's near-first order: per axis, whether most live rays point towards -axis
+    const int half = __popc(live_m);
+    const int order = (2 * __popc(__ballot_sync(mask, live && d.x < 0.0f)) > half ? 1 : 0) |
+                      (2 * __popc(__ballot_sync(mask, live && d.y < 0.0f)) > half ? 2 : 0) |
+                      (2 * __popc(__ballot_sync(mask, live && d.z < 0.0f)) > half ? 4 : 0);
     const float ix = 1.0f / (fabsf(d.x) > 1e-20f ? d.x : copysignf(1e-20f, d.x));
     const float iy = 1.0f / (fabsf(d.y) > 1e-20f ? d.y : copysignf(1e-20f, d.y));
     const float iz = 1.0f / (fabsf(d.z) > 1e-20f ? d.z : copysignf(1e-20f, d.z));
-    int stack[kGeomStack];
+    const float4 *nodes = reinterpret_cast<const float4 *>(a.gnodes);
+    int stack[kGeomStack];  // the same contents in every lane
     int sp = 0;
     stack[sp++] = 0;
     while (sp > 0) {
-        const GeomNode nd = a.gnodes[stack[--sp]];
-        const float tx0 = (nd.lo[0] - o.x) * ix, tx1 = (nd.hi[0] - o.x) * ix;
-        const float ty0 = (nd.lo[1] - o.y) * iy, ty1 = (nd.hi[1] - o.y) * iy;
-        const float tz0 = (nd.lo[2] - o.z) * iz, tz1 = (nd.hi[2] - o.z) * iz;
-        const float entry = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fminf(tz0, tz1));
-        const float exit = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1));
-        const float slack = 1e-4f * fmaxf(fabsf(entry), fabsf(exit)) + 1e-6f;
-        if (!(entry <= exit + slack && exit + slack >= tmin && entry - slack <= t)) continue;
-        if (nd.count > 0) {
-            for (int k = 0; k < nd.count; k++) analytic_one(a, a.gidx[nd.first + k], o, d, tmin, t, prim, hu, hv);
+        const int ni = stack[--sp];
+        const float4 n0 = __ldg(nodes + 2 * ni), n1 = __ldg(nodes + 2 * ni + 1);
+        bool h = false;
+        if (live) {
+            const float tx0 = (n0.x - o.x) * ix, tx1 = (n1.x - o.x) * ix;
+            const float ty0 = (n0.y - o.y) * iy, ty1 = (n1.y - o.y) * iy;
+            const float tz0 = (n0.z - o.z) * iz, tz1 = (n1.z - o.z) * iz;
+            const float entry = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fminf(tz0, tz1));
+            const float exit = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fmaxf(tz0, tz1));
+            const float slack = 1e-4f * fmaxf(fabsf(entry), fabsf(exit)) + 1e-6f;
+            h = entry <= exit + slack && exit + slack >= tmin && entry - slack <= t;
+        }
+        if (!__any_sync(mask, h)) continue;
+        const int first = __float_as_int(n0.w), count = __float_as_int(n1.w);
+        if (count > 0) {
+            if (h)
+                for (int k = 0; k < count; k++) analytic_one(a, __ldg(a.gidx + first + k), o, d, tmin, t, prim, hu, hv);
+            if (any_hit) {
+                live = live && prim == -1;
+                if (!__any_sync(mask, live)) return;
+            }
         } else if (sp + 2 <= kGeomStack) {
-            stack[sp++] = nd.first + 1;
-            stack[sp++] = nd.first;
+            const int far_first = (order >> (-1 - count)) & 1;  // the warp travels towards -axis
+            stack[sp++] = first + 1 - far_first;
+            stack[sp++] = first + far_first;
         } else {  // deeper than the stack: every object, as the reference does
-            for (int i = 0; i < a.num_geoms; i++) analytic_one(a, i, o, d, tmin, t, prim, hu, hv);
+            if (live)
+                for (int i = 0; i < a.num_geoms; i++) analytic_one(a, i, o, d, tmin, t, prim, hu, hv);
             return;
         }
     }

@@ -33,12 +33,14 @@ __global__ void __launch_bounds__(kBlock) k_extend(NativeArgs a, int cur) {
         base = __shfl_sync(0xffffffffu, base, 0);
         if (base >= n) break;
         const int q = base + lane;
+        const unsigned mask = __ballot_sync(0xffffffffu, q < n);
         if (q < n) {
             const float4 r0 = rays[2 * q], r1 = rays[2 * q + 1];
             const TraceResult tr = traverse_on<true>(stack, a.bvh, r0, r1, err);
             float t = tr.t, hu = tr.u, hv = tr.v;
             int prim = tr.addr;
-            if (a.num_geoms) analytic_hit(a, V3(r0.x, r0.y, r0.z), V3(r0.w, r1.x, r1.y), r1.z, t, prim, hu, hv);
+            if (a.num_geoms)
+                analytic_hit(a, mask, true, V3(r0.x, r0.y, r0.z), V3(r0.w, r1.x, r1.y), r1.z, t, prim, hu, hv, false);
             a.ps.hit_t[q] = t;
             a.ps.hit_prim[q] = prim;
             a.ps.hit_u[q] = hu;
@@ -65,15 +67,17 @@ __global__ void __launch_bounds__(kBlock) k_shadow(NativeArgs a) {
         base = __shfl_sync(0xffffffffu, base, 0);
         if (base >= n) break;
         const int j = base + lane;
+        const unsigned mask = __ballot_sync(0xffffffffu, j < n);
         if (j < n) {
             const float4 r0 = a.ps.shadow_ray[2 * j], r1 = a.ps.shadow_ray[2 * j + 1];
             const TraceResult tr = traverse_on<false>(stack, a.bvh, r0, r1, err);
             bool blocked = tr.addr >= 0;
-            if (!blocked && a.num_geoms) {
+            if (a.num_geoms) {
                 float t = r1.w, hu, hv;
                 int prim = -1;
-                analytic_hit(a, V3(r0.x, r0.y, r0.z), V3(r0.w, r1.x, r1.y), r1.z, t, prim, hu, hv);
-                blocked = prim != -1;
+                analytic_hit(a, mask, !blocked, V3(r0.x, r0.y, r0.z), V3(r0.w, r1.x, r1.y), r1.z, t, prim, hu, hv,
+                             true);
+                blocked = blocked || prim != -1;
             }
             if (!blocked) {
                 const int i = a.ps.shadow_path[j];
