@@ -196,6 +196,17 @@ def test_full_size_properties(terrain_full):
     assert (cc["id"][hit] == -1).mean() > 0.999
 
 
+def test_host_path_full_size_matches_device_path(terrain_full):
+    """The host-buffer entry point at 4M rays: coherent rays go in 1M-ray chunks in their own order,
+    incoherent ones in growing chunks that are each ordered; every hit equals the device path's."""
+    for name, rays in terrain_full.sets.items():
+        hits = np.empty((rays.shape[0], 2), np.int32)
+        terrain_full.dbvh.intersect_host(np.ascontiguousarray(rays), hits, closest=True)
+        dev = trace(terrain_full.dbvh, rays, True)
+        assert np.array_equal(hits[:, 0], dev["id"]), name
+        assert np.array_equal(hits[:, 1], dev["t"].view(np.int32)), name
+
+
 def test_host_buffers_match_device_buffers(cornell):
     rays = small_ray_sets(cornell, "cornell")["diffuse"]
     hits = np.empty((rays.shape[0], 2), np.int32)
@@ -230,6 +241,11 @@ def test_edge_rays(cornell):
         mine = trace(cornell.dbvh, rays, closest, ext=True)
         ref = oracle.intersect(cornell.arrays, rays, closest, normals=True)
         assert_same(mine, ref, normals=True, what="edge rays")
+        # enough copies to go through the ray ordering (zero directions, rays out of the bounds)
+        tiled = np.tile(rays, (10, 1))
+        mine = trace(cornell.dbvh, tiled, closest, ext=True)
+        ref_t = {k: np.concatenate([ref[k]] * 10) for k in ("id", "t", "mat", "normal")}
+        assert_same(mine, ref_t, normals=True, what="edge rays, ordered")
         assert (mine["id"][1024:1536] == -1).all()
 
 

@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstddef>
 #include <cstdint>
 
@@ -10,13 +11,103 @@
 
 namespace tt {
 
-constexpr int kOrderBits = 21;  // direction octant (3) + Morton code of a 64^3 origin grid (18)
+// direction cell (8: 16 x 16 octahedral grid) above the origin's cell (up to 13: Morton-like code
+// of a grid over the scene bounds whose bits go to the longest remaining cell side first; fewer
+// bits for fewer rays, about 2^(origin bits + 9) rays each)
+constexpr int kOrderDirBits = 8;
+constexpr int kOrderOriginBits = 13;
+constexpr int kOrderMinOriginBits = 6;
+constexpr int kOrderBits = kOrderDirBits + kOrderOriginBits;  // the largest key
+// Fewer rays than this are traced in their own order: ordering them cannot pay for the scan of
+// the 2^21 key counts.
+constexpr int64_t kOrderMinRays = 1 << 15;
+// Error-word bit: a sorted slot came out of range (the ray's hit is then left unwritten).
+constexpr uint32_t kErrOrder = 4u;
 
-// Device scratch for ordering n rays: keys, permutation, 2^21 counts and the scan's block sums.
+// The origin grid: q_k = clamp((o_k - lo_k) * scale_k, 0, cells_k - 1), and bit j of q_k goes to
+// the j-th lowest set bit of mask_k in the origin code.
+struct OrderGrid {
+    float3 lo, scale, qmax;
+    unsigned mask[3];
+    int origin_bits;
+};
+
+__host__ __device__ inline unsigned deposit(unsigned q, unsigned mask) {
+    unsigned r = 0;
+    for (unsigned m = mask; m; m &= m - 1u) {
+        if (q & 1u) r |= m & (0u - m);
+        q >>= 1;
+    }
+    return r;
+}
+
+__host__ __device__ inline unsigned order_key(const float4 r0, const float4 r1, const OrderGrid &g) {
+    // direction: octahedral map (x, z over |x| + |y| + |z|, the lower hemisphere folded out),
+    // 4 bits per map axis, interleaved; non-finite or zero directions go to cell 0
+    const float dx = r0.w, dy = r1.x, dz = r1.y;
+    const float s = fabsf(dx) + fabsf(dy) + fabsf(dz);
+    unsigned dcell = 0;
+    if (s > 0.0f && s < INFINITY) {
+        float u = dx / s, v = dz / s;
+        if (dy < 0.0f) {
+            const float fu = (1.0f - fabsf(v)) * (u < 0.0f ? -1.0f : 1.0f);
+            v = (1.0f - fabsf(u)) * (v < 0.0f ? -1.0f : 1.0f);
+            u = fu;
+        }
+        const unsigned qu = (unsigned)fminf(fmaxf((u + 1.0f) * 8.0f, 0.0f), 15.0f);
+        const unsigned qv = (unsigned)fminf(fmaxf((v + 1.0f) * 8.0f, 0.0f), 15.0f);
+        dcell = deposit(qu, 0xAAu) | deposit(qv, 0x55u);
+    }
+    // origin (NaN coordinates clamp to cell 0: fmaxf returns the non-NaN operand)
+    const unsigned qx = (unsigned)fminf(fmaxf((r0.x - g.lo.x) * g.scale.x, 0.0f), g.qmax.x);
+    const unsigned qy = (unsigned)fminf(fmaxf((r0.y - g.lo.y) * g.scale.y, 0.0f), g.qmax.y);
+    const unsigned qz = (unsigned)fminf(fmaxf((r0.z - g.lo.z) * g.scale.z, 0.0f), g.qmax.z);
+    const unsigned ocell = deposit(qx, g.mask[0]) | deposit(qy, g.mask[1]) | deposit(qz, g.mask[2]);
+    return (dcell << g.origin_bits) | ocell;
+}
+
+// Origin bits of the key for n rays, and the grid they index (host).
+int order_origin_bits(int64_t n);
+OrderGrid order_grid(const float lo[3], const float hi[3], int origin_bits);
+
+// Whether 64 warps of 32 consecutive rays (8 floats each, host memory), evenly spaced over the n,
+// are mostly uniform in key (six lanes of each compared with its first): the host-side twin of
+// the device probe, for callers that still hold the rays on the host.
+bool host_rays_coherent(const float *rays, int64_t n, const float lo[3], const float hi[3]);
+
+// Device scratch for ordering n rays: key + rank, sorted slot of each ray, sorted ray copy, sorted
+// hit records (up to 24 B), 2^21 counts, the scan's chunk totals and the 256-byte state block
+// (which must be zero when the scratch is new).
 size_t reorder_scratch_bytes(int64_t n);
-// Writes to *perm_out a device array of n ray indices grouped by key (launch only, on stream s).
-// scene bounds lo < hi per axis.
+// Byte offset of the state block inside the scratch (to clear it on allocation).
+size_t reorder_state_offset(int64_t n);
+
+struct OrderOut {
+    const int *pos;                   // sorted slot of each ray
+    const float4 *sorted;             // 2 float4 per sorted slot
+    void *sorted_hits;                // hit record per sorted slot, written by the trace kernel
+    const unsigned long long *state;  // order_built(state): whether pos / sorted were built
+};
+
+// Launches (on stream s) the ordering of n rays within scene bounds lo < hi per axis. The scratch
+// holds at least reorder_scratch_bytes(n); its state block sits at byte state_at, fixed for the
+// scratch's life (reorder_state_offset of the size it was made for). `parity` must alternate
+// between consecutive calls on the same scratch, which must all be on one stream (each call
+// clears the other parity's counters for the next one). Device-side errors go to *err as
+// kErrOrder.
 tt_status reorder_rays(const float4 *rays, int64_t n, const float lo[3], const float hi[3], void *scratch,
-                       int num_sms, cudaStream_t s, const int **perm_out);
+                       size_t state_at, unsigned parity, unsigned *err, cudaStream_t s, OrderOut *out);
+
+// After the trace kernel wrote hits of hit_bytes (8 or 24) per sorted slot into out.sorted_hits:
+// moves each ray's hit to hits[ray] (launch only; nothing to do when the order was not built).
+tt_status reorder_unpermute(const OrderOut &out, int64_t n, void *hits, size_t hit_bytes, unsigned *err,
+                            cudaStream_t s);
+
+// state[0]: sampled warps whose 32 keys are all equal, state[1]: sampled full warps. False when
+// more than half were uniform: the rays are coherent already (camera rays share one origin cell
+// and neighbouring pixels one direction cell) and are traced in their own order.
+__device__ __forceinline__ bool order_built(const unsigned long long *state) {
+    return 2ull * state[0] <= state[1];
+}
 
 }  // namespace tt

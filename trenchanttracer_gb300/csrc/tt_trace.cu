@@ -17,8 +17,8 @@
 //                         corner cases (a leaf box whose entry rounds above a nearly equal hit
 //                         distance) the result can depend on the other rays of the warp.
 //   TT_VARIANT_SORTED     WARP_SH16 over the rays in the order of a counting sort by direction
-//                         octant and origin cell (tt_reorder.cu); each hit still goes to its
-//                         own ray's slot.
+//                         cell and origin cell (tt_reorder.cu), or in their own order when a
+//                         sample finds them coherent; each hit still goes to its own ray's slot.
 //   TT_VARIANT_SH16_OCC,  WARP_SH16 and SORTED compiled for 12 resident blocks per SM (40
 //   TT_VARIANT_SORTED_OCC registers and a few spilled values instead of 54 registers), trading
 //                         spills for more warps to hide the node-fetch latency.
@@ -65,6 +65,8 @@ struct DeviceBVH {
     // ray-ordering scratch per work-counter slot (caller stream, three pipeline streams)
     void *order[4] = {nullptr, nullptr, nullptr, nullptr};
     size_t order_bytes[4] = {0, 0, 0, 0};
+    size_t order_state_at[4] = {0, 0, 0, 0};        // byte offset of the ordering state block
+    unsigned long long order_calls[4] = {0, 0, 0, 0};  // calls per scratch (the low bit is the parity)
     // device staging, streams and events for the host-buffer entry point's copy/compute pipeline
     void *d_stage = nullptr;
     size_t d_stage_bytes = 0;
@@ -85,15 +87,19 @@ struct TraceArgs {
     void *hits;
     unsigned long long *counter;
     unsigned int *err;
-    const int *perm;  // TT_VARIANT_SORTED: ray index of each slot
+    // TT_VARIANT_SORTED, when order_built(order_state): rays and hits by sorted slot (the hits
+    // are moved to their rays' places afterwards)
+    const float4 *sorted;
+    void *sorted_hits;
+    const unsigned long long *order_state;
 };
 
 template <bool kExt>
-__device__ __forceinline__ void store_hit(const TraceArgs &a, int64_t i, const TravState &s) {
+__device__ __forceinline__ void store_hit(const TraceArgs &a, void *hits, int64_t i, const TravState &s) {
     int id = -1;
     if (s.addr >= 0) id = __ldg(a.bvh.tri_idx + s.addr);
     if (!kExt) {
-        reinterpret_cast<int2 *>(a.hits)[i] = make_int2(id, __float_as_int(s.t));
+        reinterpret_cast<int2 *>(hits)[i] = make_int2(id, __float_as_int(s.t));
     } else {
         int mat = -1;
         float nx = 0.f, ny = 0.f, nz = 0.f;
@@ -101,7 +107,7 @@ __device__ __forceinline__ void store_hit(const TraceArgs &a, int64_t i, const T
             mat = (int)__ldg(a.bvh.mat_idx + s.addr);
             hit_normal(a.bvh, s.addr, s.u, s.v, nx, ny, nz);
         }
-        tt_hit_ext *o = reinterpret_cast<tt_hit_ext *>(a.hits) + i;
+        tt_hit_ext *o = reinterpret_cast<tt_hit_ext *>(hits) + i;
         o->id = id;
         o->mat = mat;
         o->t = s.t;
@@ -111,8 +117,8 @@ __device__ __forceinline__ void store_hit(const TraceArgs &a, int64_t i, const T
     }
 }
 
-// Warp-batched: each warp claims 32 consecutive rays (kPerm: 32 consecutive slots of the ray
-// permutation). kSh stack entries live in shared memory.
+// Warp-batched: each warp claims 32 consecutive rays (kPerm: 32 consecutive slots of the sorted
+// ray copy, when the ordering built one). kSh stack entries live in shared memory.
 template <bool kClosest, bool kExt, bool kSpec, int kSh, bool kPerm = false, int kMinBlocks = 1>
 __global__ void __launch_bounds__(kTraceBlock, kMinBlocks) trace_warp_kernel(TraceArgs a) {
     __shared__ int sh_stack[(kSh > 0 ? kSh : 1) * kTraceBlock];
@@ -120,6 +126,7 @@ __global__ void __launch_bounds__(kTraceBlock, kMinBlocks) trace_warp_kernel(Tra
     uint32_t err = 0;
     TravStack<kSh, kTraceBlock> stack;
     stack.sh = sh_stack + threadIdx.x;
+    const bool use_perm = kPerm && order_built(a.order_state);
     for (;;) {
         unsigned long long base = 0;
         if (lane == 0) base = atomicAdd(a.counter, 32ull);
@@ -127,13 +134,14 @@ __global__ void __launch_bounds__(kTraceBlock, kMinBlocks) trace_warp_kernel(Tra
         if ((int64_t)base >= a.n) break;
         const int64_t slot = (int64_t)base + lane;
         if (slot < a.n) {
-            const int64_t i = kPerm ? (int64_t)a.perm[slot] : slot;
+            // sorted: rays and hits by sorted slot (contiguous); else by ray
+            const float4 *rays = use_perm ? a.sorted : a.rays;
+            const float4 r0 = __ldg(rays + 2 * slot), r1 = __ldg(rays + 2 * slot + 1);
             TravState s;
-            const float4 r0 = __ldg(a.rays + 2 * i), r1 = __ldg(a.rays + 2 * i + 1);
             trav_init(s, stack, r0, r1);
             while (!trav_iterate<kClosest, kSpec>(s, stack, a.bvh, err, r1.w)) {
             }
-            store_hit<kExt>(a, i, s);
+            store_hit<kExt>(a, use_perm ? a.sorted_hits : a.hits, slot, s);
         }
         __syncwarp();
     }
@@ -177,7 +185,7 @@ __global__ void __launch_bounds__(kTraceBlock) trace_dynamic_kernel(TraceArgs a)
         if (__all_sync(0xffffffffu, exhausted)) break;
         if (ray >= 0) {
             if (trav_iterate<kClosest, false>(s, stack, a.bvh, err, tmax)) {
-                store_hit<kExt>(a, ray, s);
+                store_hit<kExt>(a, a.hits, ray, s);
                 ray = -1;
             }
         }
@@ -305,8 +313,9 @@ static void launch_variant(int variant, unsigned blocks, cudaStream_t stream, co
     }
 }
 
+// unordered = true traces a SORTED / SORTED_OCC variant's rays in their own order (its unsorted twin).
 static tt_status launch_trace(const DeviceBVH &d, const void *d_rays, int64_t n, void *d_hits, bool closest,
-                              bool ext, cudaStream_t stream, int counter_slot = 0) {
+                              bool ext, cudaStream_t stream, int counter_slot = 0, bool unordered = false) {
     if (n < 0 || n > ((int64_t)1 << 40)) return fail(TT_ERR_INVALID, "ray count out of range");
     if (n == 0) return TT_OK;
     if (!d_rays || !d_hits) return fail(TT_ERR_INVALID, "null ray or hit buffer");
@@ -320,10 +329,15 @@ static tt_status launch_trace(const DeviceBVH &d, const void *d_rays, int64_t n,
     a.hits = d_hits;
     a.counter = d.scratch + counter_slot;
     a.err = reinterpret_cast<unsigned int *>(d.scratch + kScratchErr);
-    a.perm = nullptr;
+    a.sorted = nullptr;
+    a.sorted_hits = nullptr;
+    a.order_state = nullptr;
+    OrderOut order{};
     int variant = d.variant;
     const bool sorted = variant == VARIANT_SORTED || variant == VARIANT_SORTED_OCC;
-    if (sorted && n >= ((int64_t)1 << 31)) variant = VARIANT_WARP_SH16;  // the permutation is int
+    // slots are int; too few rays cannot pay for the ordering
+    if (sorted && (unordered || n >= ((int64_t)1 << 31) || n < kOrderMinRays))
+        variant = variant == VARIANT_SORTED_OCC ? VARIANT_SH16_OCC : VARIANT_WARP_SH16;
     if (variant == VARIANT_SORTED || variant == VARIANT_SORTED_OCC) {
         // one scratch per work-counter slot, so the pipeline streams never share one
         const int k = counter_slot == 0 ? 0 : 1 + (counter_slot - kScratchPipe) % 3;
@@ -336,9 +350,18 @@ static tt_status launch_trace(const DeviceBVH &d, const void *d_rays, int64_t n,
             cudaError_t e = cudaMalloc(&dm.order[k], need);
             if (e != cudaSuccess) return fail(TT_ERR_OOM, std::string("ray ordering scratch: ") + cudaGetErrorString(e));
             dm.order_bytes[k] = need;
+            dm.order_state_at[k] = reorder_state_offset(n);
+            dm.order_calls[k] = 0;
+            e = cudaMemsetAsync(static_cast<char *>(dm.order[k]) + dm.order_state_at[k], 0, 256, stream);
+            if (e != cudaSuccess) return fail(TT_ERR_CUDA, std::string("ray ordering scratch: ") + cudaGetErrorString(e));
         }
-        const tt_status st = reorder_rays(a.rays, n, d.lo, d.hi, dm.order[k], d.num_sms, stream, &a.perm);
+        const tt_status st = reorder_rays(a.rays, n, d.lo, d.hi, dm.order[k], dm.order_state_at[k],
+                                          (unsigned)dm.order_calls[k], a.err, stream, &order);
         if (st != TT_OK) return st;
+        dm.order_calls[k]++;
+        a.sorted = order.sorted;
+        a.sorted_hits = order.sorted_hits;
+        a.order_state = order.state;
     }
     const int64_t warps_needed = (n + 31) / 32;
     int64_t blocks = (int64_t)d.num_sms * d.blocks_per_sm[variant];
@@ -353,6 +376,7 @@ static tt_status launch_trace(const DeviceBVH &d, const void *d_rays, int64_t n,
         else launch_variant<false, false>(variant, (unsigned)blocks, stream, a);
     }
     TT_CUDA(cudaGetLastError());
+    if (a.order_state) return reorder_unpermute(order, n, d_hits, ext ? sizeof(tt_hit_ext) : sizeof(tt_hit), a.err, stream);
     return TT_OK;
 }
 
@@ -364,6 +388,8 @@ static tt_status read_error_word(const DeviceBVH &d, cudaStream_t stream) {
         TT_CUDA(cudaMemsetAsync(d.scratch + 1, 0, 8, stream));
         TT_CUDA(cudaStreamSynchronize(stream));
         if (w & kErrStack) return fail(TT_ERR_BOUNDS, "traversal stack overflow (BVH deeper than 66 levels)");
+        if (w & kErrOrder)
+            return fail(TT_ERR_BOUNDS, "ray ordering: a sorted slot was out of range");
         return fail(TT_ERR_TIMEOUT, "traversal iteration cap reached (corrupt BVH?)");
     }
     return TT_OK;
@@ -534,12 +560,24 @@ tt_status tt_trace_host(const tt_dbvh *bvh, const tt_ray *h_rays, int64_t n, tt_
     char *dh = dr + rb;
     // Chunks rotate over three streams so that the copy in of chunk i+1, the trace of chunk i and
     // the copy out of chunk i-1 overlap; everything is ordered after prior work on `stream`.
-    const int64_t chunk = n < (int64_t)(1 << 21) ? n : (int64_t)(1 << 20);
+    // Coherent rays (a sample of the host buffer decides, as the device probe would) are bound by
+    // the copy in: 1M-ray chunks, traced in their own order. Incoherent ones are bound by the
+    // trace: chunks of n/16, 3n/16, 6n/16 and the rest, each ordered when the variant orders, so
+    // that the trace starts early and the later chunks are large enough for ordering to pay
+    // (measured on 4M terrain rays at 190 GB/s per copy direction: 2.04 ms against 2.32 ms for
+    // 1M chunks).
+    const bool sorted_variant = d.variant == VARIANT_SORTED || d.variant == VARIANT_SORTED_OCC;
+    const bool coherent = !sorted_variant || n < (int64_t)(1 << 21) ||
+                          host_rays_coherent(reinterpret_cast<const float *>(h_rays), n, d.lo, d.hi);
+    const int64_t sched[4] = {n / 16, 3 * (n / 16), 6 * (n / 16), 0};
     TT_CUDA(cudaEventRecord(d.pipe_start, s));
     tt_status st = TT_OK;
     int used = 0;
-    for (int64_t off = 0, k = 0; off < n && st == TT_OK; off += chunk, k++) {
-        const int64_t m = (n - off) < chunk ? (n - off) : chunk;
+    for (int64_t off = 0, k = 0, m = 0; off < n && st == TT_OK; off += m, k++) {
+        if (n < (int64_t)(1 << 21)) m = n;
+        else if (coherent) m = (int64_t)(1 << 20);
+        else m = k < 3 ? sched[k] : n - off;
+        if (m > n - off) m = n - off;
         const int p = (int)(k % 3);
         cudaStream_t ps = d.pipe[p];
         if (k < 3) {
@@ -548,7 +586,8 @@ tt_status tt_trace_host(const tt_dbvh *bvh, const tt_ray *h_rays, int64_t n, tt_
         }
         TT_CUDA(cudaMemcpyAsync(dr + 32 * off, reinterpret_cast<const char *>(h_rays) + 32 * off, 32ull * m,
                                 cudaMemcpyHostToDevice, ps));
-        st = launch_trace(d, dr + 32 * off, m, dh + 8 * off, closest != 0, false, ps, kScratchPipe + p);
+        st = launch_trace(d, dr + 32 * off, m, dh + 8 * off, closest != 0, false, ps, kScratchPipe + p,
+                          coherent && n >= (int64_t)(1 << 21));
         if (st == TT_OK)
             TT_CUDA(cudaMemcpyAsync(reinterpret_cast<char *>(h_hits) + 8 * off, dh + 8 * off, 8ull * m,
                                     cudaMemcpyDeviceToHost, ps));
