@@ -363,12 +363,16 @@ def run_ours(args) -> None:
 RENDER_CONFIGS = {
     "cornell": dict(desc="Cornell box (10 wall tris + 0.25 x 0.25 ceiling light 17,12,4) + subdivision-5 "
                          "icosphere r 0.3 (seed-42 noise 0.03, Lambert 0.8), 20,492 tris; 512 x 512, 16 spp, "
-                         "depth 8, Russian roulette from 4, PCG32", width=512, height=512, spp=16, depth=8),
+                         "depth 8, Russian roulette from 4, PCG32", width=512, height=512, spp=16, depth=8,
+                    ordered=1),
     "multimaterial": dict(desc="400 displaced subdivision-5 icospheres (8,192,002 tris incl. ground), Lambert / "
                                "GGX / dielectric 1.5; 2048 x 1024 sky with a 0.5-degree sun of 5e4, 2D-CDF light "
                                "sampling with MIS; 1920 x 1080, 64 spp, depth 16, Russian roulette from 4",
-                          width=1920, height=1080, spp=64, depth=16),
+                          width=1920, height=1080, spp=64, depth=16, ordered=0),
 }
+# ordered: whether the extension queues are ordered before tracing, the faster setting measured
+# on a GB300 (Cornell 921 vs 801 Msamples/s; multi-material 314 vs 325: pixel-order queues there
+# are coherent enough that the ordering passes cost more than they save)
 
 
 def render_scene(name: str, width: int, height: int):
@@ -399,9 +403,11 @@ def render_scene(name: str, width: int, height: int):
     return sc, mesh, cam
 
 
-def render_cpu_baseline(bvh, sc, cam, spp: int, depth: int, budget_s: float = 15.0) -> dict:
-    """The oracle's C restatement of the native path tracer (OpenMP, all host cores) on a
-    reduced-resolution image of the same view: paths per second."""
+def render_cpu_baseline(bvh, sc, cam, spp: int, depth: int, budget_s: float = 15.0, min_s: float = 10.0) -> dict:
+    """The oracle's C restatement of the native path tracer (OpenMP, all host cores) on the same
+    view, at the highest resolution (halving from the full one down to 1/16) whose render takes
+    under a quarter of budget_s, repeated with further samples until min_s have passed: paths
+    per second."""
     import ctypes as C
     from oracle import oracle
     from trenchanttracer_gb300 import _lib, make_camera_meta, render_params
@@ -411,20 +417,29 @@ def render_cpu_baseline(bvh, sc, cam, spp: int, depth: int, budget_s: float = 15
     env = sc.env()
     arr = bvh.arrays()
     threads = oracle.max_threads()
-    scale, out = 16, None
-    while True:
+    tx = float(np.float32(np.tan(np.radians(cam.fov[0]) / 2)))
+    ty = float(np.float32(np.tan(np.radians(cam.fov[1]) / 2)))
+
+    def render(scale: int, offset: int):
         w, h = max(8, cam.width // scale), max(8, cam.height // scale)
         small = make_camera_meta(w, h, list(cam.position), list(cam.view), list(cam.up), tuple(cam.fov))
-        p = render_params(spp=spp, max_depth=depth, rr_depth=4, seed=1)
-        tx = float(np.float32(np.tan(np.radians(cam.fov[0]) / 2)))
-        ty = float(np.float32(np.tan(np.radians(cam.fov[1]) / 2)))
+        p = render_params(spp=spp, sample_offset=offset, max_depth=depth, rr_depth=4, seed=1)
         t0 = time.perf_counter()
         oracle.render_native(arr, mats, geos, env, small, p, tx, ty, threads=threads)
-        dt = time.perf_counter() - t0
-        out = {"paths_per_s": w * h * spp / dt, "seconds": dt, "threads": threads, "sample": f"{w}x{h} x {spp} spp"}
+        return w, h, time.perf_counter() - t0
+
+    scale = 16
+    while True:
+        w, h, dt = render(scale, 0)
         if dt > budget_s / 4 or scale == 1:
-            return out
+            break
         scale //= 2
+    total, passes = dt, 1
+    while total < min_s:
+        total += render(scale, passes * spp)[2]
+        passes += 1
+    return {"paths_per_s": passes * w * h * spp / total, "seconds": total, "threads": threads,
+            "sample": f"{w}x{h} x {spp} spp x {passes} passes"}
 
 
 def run_render(args) -> None:
@@ -439,6 +454,7 @@ def run_render(args) -> None:
     bvh = BVHCompact.build(sc, 1e-5, 1, 8)
     build_s = time.perf_counter() - t0
     r = Renderer(DeviceBVH(bvh), sc)
+    r.set_launch(128, 16, 1 << 22, cfg["ordered"] if args.ordered < 0 else args.ordered)
     npx = cfg["width"] * cfg["height"] * 3
     acc = torch.zeros(npx, dtype=torch.float32, device=dev)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=dev)
@@ -479,7 +495,9 @@ def run_render(args) -> None:
     img = host.numpy()
     assert np.isfinite(img).all()
     cpu = render_cpu_baseline(bvh, sc, cam, cfg["spp"], cfg["depth"])
-    launches = args.steps * (1 + 3 * cfg["depth"] + 1) * -(-paths // r.launch[2])
+    # per wave: raygen, per bounce extend / shade / shadow (+ 4 ordering kernels and the hit gather
+    # when ordered), accumulate
+    launches = args.steps * (1 + (3 + 5 * r.launch[3]) * cfg["depth"] + 1) * -(-paths // r.launch[2])
     line = {
         "metric": f"Msamples/s native path tracer ({args.workload})", "value": round(paths / mean_ms / 1e3, 2),
         "unit": "Msamples/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
@@ -744,6 +762,9 @@ def main() -> None:
     ap.add_argument("--workload", choices=["terrain", "cornell", "multimaterial", "batch", "cache", "mlp"], default="terrain")
     ap.add_argument("--cache-scene", choices=["multimaterial", "terrain"], default="multimaterial")
     ap.add_argument("--width", type=int, default=1920)
+    ap.add_argument("--ordered", type=int, choices=[-1, 0, 1], default=-1,
+                    help="cornell / multimaterial: order each extension queue before tracing it "
+                         "(-1: the workload's measured setting)")
     ap.add_argument("--trace-width", type=int, default=WIDTH,
                     help="terrain workload: camera width; each ray set has width^2 rays (profiling a "
                          "smaller case of the same kernels)")

@@ -308,9 +308,12 @@ typedef struct tt_launch_shape {
     int32_t block;        /* threads per block: 64, 128 or 256 */
     int32_t stack_shared; /* traversal stack entries per thread kept in shared memory: 0, 8 or 16 */
     int32_t wave_paths;   /* paths in flight per wave (queue capacity): 1 .. 2^24 */
+    int32_t ordered;      /* 1: order each extension queue by direction and origin cell before
+                             tracing it (coherent queues, e.g. camera rays, are left alone) */
     float ms;             /* tt_batch_autotune: the trial's time; otherwise 0 */
 } tt_launch_shape;
-/* Default: 128 threads, 16 shared entries, 2^22 paths. Results do not depend on the shape. */
+/* Default: 128 threads, 16 shared entries, 2^22 paths, unordered. Results do not depend on the
+ * shape. */
 tt_status tt_renderer_set_launch(tt_renderer *renderer, const tt_launch_shape *shape);
 tt_status tt_renderer_get_launch(const tt_renderer *renderer, tt_launch_shape *shape);
 /* Counters of the native path tracer since the last reset: out[0] extension rays (closest hit),

@@ -72,7 +72,9 @@ def test_batch_equals_sequential_renders(showcase):
     assert np.array_equal(plain.view(np.uint32), seq.view(np.uint32))
 
 
-@pytest.mark.parametrize("shape", [(64, 0, 777), (256, 8, 4096), (128, 16, 1 << 20), (64, 16, 31)])
+@pytest.mark.parametrize("shape", [(64, 0, 777, 0), (256, 8, 4096, 0), (128, 16, 1 << 20, 0), (64, 16, 31, 0),
+                                   (64, 0, 777, 1), (256, 8, 4096, 1), (128, 16, 1 << 20, 1), (64, 16, 31, 1),
+                                   (128, 16, 65536, 1)])
 def test_result_does_not_depend_on_launch_shape(showcase, shape):
     views = _views(seed=1, count=5)
     base = _sequential(showcase, views)
@@ -126,7 +128,8 @@ def test_ray_counters_and_autotune(showcase):
     assert s_seq == s_batch
     assert s_seq["paths"] == sum(c.width * c.height * s for c, s, _, _ in views)
     assert s_seq["extension_rays"] >= s_seq["paths"] and s_seq["shadow_rays"] > 0
-    assert len(trials) >= 9 and all(t[3] > 0 for t in trials)
-    best = min(trials, key=lambda t: t[3])
-    assert showcase.launch == best[:3]
+    assert len(trials) >= 18 and all(t[4] > 0 for t in trials)
+    assert {t[3] for t in trials} == {0, 1}
+    best = min(trials, key=lambda t: t[4])
+    assert showcase.launch == best[:4]
     assert np.array_equal(got.view(np.uint32), seq.view(np.uint32))

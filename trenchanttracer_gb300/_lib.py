@@ -65,10 +65,11 @@ RENDER_NO_ENV_SAMPLING = 2
 
 class LaunchShape(C.Structure):
     """tt_launch_shape (include/tt.h)."""
-    _fields_ = [("block", C.c_int32), ("stack_shared", C.c_int32), ("wave_paths", C.c_int32), ("ms", C.c_float)]
+    _fields_ = [("block", C.c_int32), ("stack_shared", C.c_int32), ("wave_paths", C.c_int32), ("ordered", C.c_int32),
+                ("ms", C.c_float)]
 
     def as_tuple(self) -> tuple:
-        return (self.block, self.stack_shared, self.wave_paths)
+        return (self.block, self.stack_shared, self.wave_paths, self.ordered)
 
 
 class CacheParams(C.Structure):

@@ -295,9 +295,10 @@ class Renderer:
         check(lib().tt_render_cached(self._h, cache._h, C.byref(cam), C.byref(params), C.c_void_p(accum.data_ptr()),
                                      int(bool(train)), C.c_void_p(stream)))
 
-    def set_launch(self, block: int, stack_shared: int, wave_paths: int) -> None:
-        """Launch shape of the native kernels (include/tt.h, tt_launch_shape)."""
-        shape = _lib.LaunchShape(int(block), int(stack_shared), int(wave_paths), 0.0)
+    def set_launch(self, block: int, stack_shared: int, wave_paths: int, ordered: int = 0) -> None:
+        """Launch shape of the native kernels (include/tt.h, tt_launch_shape); ordered = 1 orders
+        each extension queue by direction and origin cell before tracing it."""
+        shape = _lib.LaunchShape(int(block), int(stack_shared), int(wave_paths), int(ordered), 0.0)
         check(lib().tt_renderer_set_launch(self._h, C.byref(shape)))
 
     @property
@@ -358,11 +359,11 @@ class Batch:
 
     def autotune(self, sample_paths: int = 0, stream: int = 0) -> list:
         """Times every launch shape on the batch's first paths, keeps the fastest; returns
-        [(block, stack_shared, wave_paths, ms)]."""
+        [(block, stack_shared, wave_paths, ordered, ms)]."""
         res = (_lib.LaunchShape * 64)()
         n = C.c_int32()
         check(lib().tt_batch_autotune(self._h, int(sample_paths), C.c_void_p(stream), res, 64, C.byref(n)))
-        return [(r.block, r.stack_shared, r.wave_paths, r.ms) for r in res[:min(n.value, 64)]]
+        return [(r.block, r.stack_shared, r.wave_paths, r.ordered, r.ms) for r in res[:min(n.value, 64)]]
 
     def split(self, accum) -> list:
         """The per-view (H, W, 3) images of an accumulation buffer (torch tensor or numpy array)."""

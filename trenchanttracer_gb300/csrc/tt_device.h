@@ -8,8 +8,10 @@
 
 namespace tt {
 
-// The device arrays of an uploaded BVH (tt_trace.cu owns the handle's layout).
+// The device arrays of an uploaded BVH (tt_trace.cu owns the handle's layout), and its scene
+// bounds from the root's boxes (the ray-ordering grid).
 BvhView dbvh_view(const tt_dbvh *bvh);
+void dbvh_bounds(const tt_dbvh *bvh, float lo[3], float hi[3]);
 
 }  // namespace tt
 
@@ -38,6 +40,10 @@ struct tt_renderer {
     int num_sms = 0;
     // launch shape of the native kernels (tt_renderer_set_launch, tt_batch_autotune)
     int launch_block = 128, launch_stack = 16, launch_wave = 1 << 22;
+    int launch_order = 0;  // order each extension queue by direction and origin cell before tracing
+    float order_lo[3] = {-1.f, -1.f, -1.f}, order_hi[3] = {1.f, 1.f, 1.f};  // scene bounds
+    size_t order_off = 0;       // byte offset of the ordering scratch inside `paths` (0: none)
+    size_t order_state_at = 0;  // its state block, relative to the scratch
     int occ_trace[3][3] = {};  // resident blocks per SM by (block shape, stack shape); 0 = unknown
     int occ_shade[3] = {};
     // radiance-cache queries and training records of cached renders

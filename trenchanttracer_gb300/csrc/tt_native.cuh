@@ -20,6 +20,7 @@
 
 #include "tt_device.h"
 #include "tt_ptmath.cuh"
+#include "tt_reorder.h"
 
 namespace tt {
 
@@ -83,6 +84,17 @@ struct CacheView {
     int *counts;              // [0] queries, [1] training records
 };
 
+// Ordering of an extension queue (tt_reorder.cu): when order_built(state), k_extend reads the
+// ordered copy of the queue's rays and writes hits by ordered slot, and k_order_gather_hits moves
+// each hit back to its queue slot (pos: the ordered slot of each queue slot).
+struct OrderView {
+    const float4 *sorted;  // nullptr: ordering off
+    float *hit_t, *hit_u, *hit_v;
+    int *hit_prim;
+    const int *pos;
+    const unsigned long long *state;
+};
+
 struct NativeArgs {
     BvhView bvh;
     const MaterialRec *materials;
@@ -102,6 +114,7 @@ struct NativeArgs {
     CacheView cache;
     const struct GeomNode *gnodes;  // box hierarchy over the analytic objects, or nullptr
     const int *gidx;
+    OrderView order;
 };
 
 __device__ __forceinline__ int find_view(const NativeArgs &a, long long g) {
@@ -244,6 +257,9 @@ struct TraceKernels {
     void (*extend)(NativeArgs, int);
     void (*shadow)(NativeArgs);
 };
+// Moves the hits of an ordered extension queue back to their queue slots (nothing when the
+// queue was not ordered).
+__global__ void k_order_gather_hits(NativeArgs a, int cur);
 // Block sizes and shared stack depths the traversal kernels are built for.
 constexpr int kNumBlockShapes = 3;
 constexpr int kBlockShapes[kNumBlockShapes] = {64, 128, 256};

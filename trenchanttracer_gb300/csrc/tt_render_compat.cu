@@ -422,6 +422,7 @@ tt_status tt_renderer_create(const tt_dbvh *bvh, const tt_scene *scene, tt_rende
     const Scene &sc = scene->s;
     auto *r = new tt_renderer();
     r->bvh = dbvh_view(bvh);
+    dbvh_bounds(bvh, r->order_lo, r->order_hi);
     auto up = [&](void **dst, const void *src, size_t bytes) -> cudaError_t {
         if (!bytes) return cudaSuccess;
         cudaError_t e = cudaMalloc(dst, bytes);

@@ -26,7 +26,13 @@ __global__ void __launch_bounds__(kBlock) k_extend(NativeArgs a, int cur) {
     TravStack<kSh, kBlock> stack;
     stack.sh = sh_stack + threadIdx.x;
     uint32_t err = 0;
-    const float4 *rays = a.ps.ray[cur];
+    // an ordered queue: rays and hits by ordered slot, moved back by k_order_gather_hits
+    const bool ordered = a.order.sorted && order_built(a.order.state);
+    const float4 *rays = ordered ? a.order.sorted : a.ps.ray[cur];
+    float *hit_t = ordered ? a.order.hit_t : a.ps.hit_t;
+    float *hit_u = ordered ? a.order.hit_u : a.ps.hit_u;
+    float *hit_v = ordered ? a.order.hit_v : a.ps.hit_v;
+    int *hit_prim = ordered ? a.order.hit_prim : a.ps.hit_prim;
     for (;;) {
         int base = 0;
         if (lane == 0) base = atomicAdd(a.ps.counts + 3, 32);
@@ -41,10 +47,10 @@ __global__ void __launch_bounds__(kBlock) k_extend(NativeArgs a, int cur) {
             int prim = tr.addr;
             if (a.num_geoms)
                 analytic_hit(a, mask, true, V3(r0.x, r0.y, r0.z), V3(r0.w, r1.x, r1.y), r1.z, t, prim, hu, hv, false);
-            a.ps.hit_t[q] = t;
-            a.ps.hit_prim[q] = prim;
-            a.ps.hit_u[q] = hu;
-            a.ps.hit_v[q] = hv;
+            hit_t[q] = t;
+            hit_prim[q] = prim;
+            hit_u[q] = hu;
+            hit_v[q] = hv;
         }
         __syncwarp();
     }
@@ -92,6 +98,25 @@ __global__ void __launch_bounds__(kBlock) k_shadow(NativeArgs a) {
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(a.stats + 1, (unsigned long long)n);
     if (err) atomicOr(a.err, err);
+}
+
+__global__ void __launch_bounds__(256) k_order_gather_hits(NativeArgs a, int cur) {
+    if (!a.order.sorted || !order_built(a.order.state)) return;
+    const int n = a.ps.counts[cur];
+    unsigned bad = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int p = __ldcs(a.order.pos + i);
+        if ((unsigned)p < (unsigned)n) {
+            a.ps.hit_t[i] = a.order.hit_t[p];
+            a.ps.hit_u[i] = a.order.hit_u[p];
+            a.ps.hit_v[i] = a.order.hit_v[p];
+            a.ps.hit_prim[i] = a.order.hit_prim[p];
+        } else {  // not reachable with a consistent ordering: report, and let the path miss
+            a.ps.hit_prim[i] = -1;
+            bad = 1;
+        }
+    }
+    if (bad) atomicOr(a.err, kErrOrder);
 }
 
 template <int kBlock, int kSh>

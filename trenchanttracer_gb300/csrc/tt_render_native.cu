@@ -820,8 +820,13 @@ static tt_status ensure_paths(tt_renderer *r, int cap, PathSoA &ps) {
         return total;
     };
     size_t sizes[kArrays];
-    if (r->path_capacity < cap || !r->paths) {
-        const size_t total = layout((size_t)cap, sizes);
+    // the ordering scratch of the extension queues follows the arrays when ordering is on
+    const bool want_order = r->launch_order != 0;
+    if (r->path_capacity < cap || !r->paths || (want_order && !r->order_off)) {
+        const int c = std::max(cap, r->path_capacity);
+        const size_t arrays = layout((size_t)c, sizes);
+        const size_t total = arrays + (want_order ? reorder_scratch_bytes(c) : 0);
+        cap = c;
         if (r->paths) cudaFree(r->paths);
         r->paths = nullptr;
         r->paths_bytes = 0;
@@ -831,6 +836,12 @@ static tt_status ensure_paths(tt_renderer *r, int cap, PathSoA &ps) {
         r->paths_bytes = total;
         r->path_capacity = cap;
         r->paths_gen++;
+        r->order_off = want_order ? arrays : 0;
+        r->order_state_at = want_order ? reorder_state_offset(c) : 0;
+        if (want_order) {  // the ordering state starts at zero
+            e = cudaMemset(static_cast<char *>(r->paths) + r->order_off + r->order_state_at, 0, 256);
+            if (e != cudaSuccess) return fail(TT_ERR_CUDA, std::string("path state: ") + cudaGetErrorString(e));
+        }
     }
     layout((size_t)r->path_capacity, sizes);
     char *p = static_cast<char *>(r->paths);
@@ -880,17 +891,38 @@ static int stack_index(int sh) {
 struct Launch {
     TraceKernels tk;
     int block = 0, wave = 0;
-    int grid_trace = 0, grid_shade = 0;
+    int grid_trace = 0, grid_shade = 0, grid_gather = 0;
+    bool order = false;  // order the extension queues (scratch in the path allocation)
 };
 
-static tt_status resolve_launch(tt_renderer *r, int block, int sh, int wave, Launch &L) {
+// Where a render's queue ordering works: the scratch inside the path allocation and the scene
+// bounds of the origin grid (scratch = nullptr: the allocation has none).
+struct OrderPlan {
+    void *scratch = nullptr;
+    size_t state_at = 0;
+    const float *lo = nullptr, *hi = nullptr;
+};
+
+static OrderPlan order_plan(const tt_renderer *r) {
+    OrderPlan o;
+    if (r->order_off) {
+        o.scratch = static_cast<char *>(r->paths) + r->order_off;
+        o.state_at = r->order_state_at;
+        o.lo = r->order_lo;
+        o.hi = r->order_hi;
+    }
+    return o;
+}
+
+static tt_status resolve_launch(tt_renderer *r, int block, int sh, int wave, int order, Launch &L) {
     const int bi = block_index(block), si = stack_index(sh);
-    if (bi < 0 || si < 0 || wave < 1 || wave > kMaxWavePaths)
+    if (bi < 0 || si < 0 || wave < 1 || wave > kMaxWavePaths || (order != 0 && order != 1))
         return fail(TT_ERR_INVALID, "launch shape: block must be 64/128/256, stack_shared 0/8/16, "
-                                    "wave_paths 1..16777216");
+                                    "wave_paths 1..16777216, ordered 0 or 1");
     L.tk = trace_kernels(block, sh);
     L.block = block;
     L.wave = wave;
+    L.order = order != 0;
     if (!r->occ_trace[bi][si]) {
         int b = 0;
         TT_CUDA_N(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, (const void *)L.tk.extend, block, 0));
@@ -905,6 +937,7 @@ static tt_status resolve_launch(tt_renderer *r, int block, int sh, int wave, Lau
     }
     L.grid_trace = r->num_sms * r->occ_trace[bi][si];
     L.grid_shade = r->num_sms * r->occ_shade[bi];
+    L.grid_gather = r->num_sms * 8;
     return TT_OK;
 }
 
@@ -975,9 +1008,11 @@ static NativeArgs base_args(tt_renderer *r, const tt_render_params &p, const Pat
 // Issues the kernels of `total` paths (waves of L.wave) on stream s. accum = nullptr: no
 // accumulation (autotuning trials). cache: the radiance cache of a cached render (a.cache set up),
 // queried after the second bounce and trained after every wave when `train`.
-static tt_status issue(NativeArgs a, long long total, const Launch &L, void *accum, cudaStream_t s,
-                       tt_cache *cache = nullptr, bool train = false) {
+static tt_status issue(NativeArgs a, long long total, const Launch &L, const OrderPlan &plan, void *accum,
+                       cudaStream_t s, tt_cache *cache = nullptr, bool train = false) {
     const bool f64 = (a.p.flags & TT_RENDER_ACCUM_F64) != 0;
+    if (L.order && !plan.scratch) return fail(TT_ERR_INVALID, "queue ordering: no scratch for it");
+    const long long qcap = std::min<long long>(L.wave, total);  // queue capacity: the path arrays' size
     for (long long done = 0; done < total; done += L.wave) {
         a.wave_first = done;
         a.wave_paths = (int)std::min<long long>(total - done, L.wave);
@@ -989,7 +1024,22 @@ static tt_status issue(NativeArgs a, long long total, const Launch &L, void *acc
         }
         k_raygen<<<L.grid_shade, L.block, 0, s>>>(a);
         for (int b = 0; b < a.p.max_depth; b++) {
+            if (L.order) {  // order the queue; the probe leaves coherent queues (camera rays) alone
+                OrderOut oo;
+                const tt_status st = reorder_rays(a.ps.ray[b & 1], qcap, a.ps.counts + (b & 1), plan.lo, plan.hi,
+                                                  plan.scratch, plan.state_at, a.err, s, &oo);
+                if (st != TT_OK) return st;
+                float *h = static_cast<float *>(oo.sorted_hits);
+                a.order.sorted = oo.sorted;
+                a.order.pos = oo.pos;
+                a.order.state = oo.state;
+                a.order.hit_t = h;
+                a.order.hit_u = h + qcap;
+                a.order.hit_v = h + 2 * qcap;
+                a.order.hit_prim = reinterpret_cast<int *>(h + 3 * qcap);
+            }
             L.tk.extend<<<L.grid_trace, L.block, 0, s>>>(a, b & 1);
+            if (L.order) k_order_gather_hits<<<L.grid_gather, 256, 0, s>>>(a, b & 1);
             k_shade<<<L.grid_shade, L.block, 0, s>>>(a, b & 1);
             L.tk.shadow<<<L.grid_trace, L.block, 0, s>>>(a);
         }
@@ -1065,7 +1115,7 @@ struct tt_batch {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     void *graph_accum = nullptr;
-    int graph_block = 0, graph_stack = -1, graph_wave = 0;
+    int graph_block = 0, graph_stack = -1, graph_wave = 0, graph_order = -1;
     unsigned long long graph_paths_gen = 0;
     int graph_kernels = 0;
 };
@@ -1115,7 +1165,7 @@ tt_status tt_render_native(tt_renderer *r, const tt_camera_meta *cam, const tt_r
     if (st != TT_OK) return st;
     const ViewRec v = make_view(*cam, p->spp, p->sample_offset, p->seed, 0, 0);
     Launch L;
-    st = resolve_launch(r, r->launch_block, r->launch_stack, r->launch_wave, L);
+    st = resolve_launch(r, r->launch_block, r->launch_stack, r->launch_wave, r->launch_order, L);
     if (st != TT_OK) return st;
     PathSoA ps;
     st = ensure_paths(r, (int)std::min<long long>(v.paths, L.wave), ps);
@@ -1124,7 +1174,7 @@ tt_status tt_render_native(tt_renderer *r, const tt_camera_meta *cam, const tt_r
     a.views = nullptr;
     a.n_views = 1;
     a.view0 = v;
-    return issue(a, v.paths, L, d_accum, (cudaStream_t)stream);
+    return issue(a, v.paths, L, order_plan(r), d_accum, (cudaStream_t)stream);
 }
 
 tt_status tt_render_cached(tt_renderer *r, tt_cache *c, const tt_camera_meta *cam, const tt_render_params *p,
@@ -1136,7 +1186,7 @@ tt_status tt_render_cached(tt_renderer *r, tt_cache *c, const tt_camera_meta *ca
     const tt_cache_params &cp = nrc::cache_params(c);
     const ViewRec v = make_view(*cam, p->spp, p->sample_offset, p->seed, 0, 0);
     Launch L;
-    st = resolve_launch(r, r->launch_block, r->launch_stack, r->launch_wave, L);
+    st = resolve_launch(r, r->launch_block, r->launch_stack, r->launch_wave, r->launch_order, L);
     if (st != TT_OK) return st;
     const int wave = (int)std::min<long long>(v.paths, L.wave);
     PathSoA ps;
@@ -1153,17 +1203,18 @@ tt_status tt_render_cached(tt_renderer *r, tt_cache *c, const tt_camera_meta *ca
     a.cache.train = train ? 1 : 0;
     a.cache.spread_c = cp.spread_c;
     a.cache.train_stride = 1;
-    return issue(a, v.paths, L, d_accum, (cudaStream_t)stream, c, train != 0);
+    return issue(a, v.paths, L, order_plan(r), d_accum, (cudaStream_t)stream, c, train != 0);
 }
 
 tt_status tt_renderer_set_launch(tt_renderer *r, const tt_launch_shape *shape) {
     if (!r || !shape) return fail(TT_ERR_INVALID, "null argument");
     Launch L;
-    tt_status st = resolve_launch(r, shape->block, shape->stack_shared, shape->wave_paths, L);
+    tt_status st = resolve_launch(r, shape->block, shape->stack_shared, shape->wave_paths, shape->ordered, L);
     if (st != TT_OK) return st;
     r->launch_block = shape->block;
     r->launch_stack = shape->stack_shared;
     r->launch_wave = shape->wave_paths;
+    r->launch_order = shape->ordered;
     return TT_OK;
 }
 
@@ -1172,6 +1223,7 @@ tt_status tt_renderer_get_launch(const tt_renderer *r, tt_launch_shape *shape) {
     shape->block = r->launch_block;
     shape->stack_shared = r->launch_stack;
     shape->wave_paths = r->launch_wave;
+    shape->ordered = r->launch_order;
     shape->ms = 0.0f;
     return TT_OK;
 }
@@ -1228,20 +1280,20 @@ tt_status tt_batch_render(tt_batch *b, void *d_accum, int use_graph, void *strea
     if (!b || !d_accum) return fail(TT_ERR_INVALID, "null argument");
     tt_renderer *r = b->r;
     Launch L;
-    tt_status st = resolve_launch(r, r->launch_block, r->launch_stack, r->launch_wave, L);
+    tt_status st = resolve_launch(r, r->launch_block, r->launch_stack, r->launch_wave, r->launch_order, L);
     if (st != TT_OK) return st;
     PathSoA ps;
     st = ensure_paths(r, (int)std::min<long long>(b->total_paths, L.wave), ps);
     if (st != TT_OK) return st;
     const NativeArgs a = batch_args(b, ps);
-    if (!use_graph) return issue(a, b->total_paths, L, d_accum, (cudaStream_t)stream);
+    if (!use_graph) return issue(a, b->total_paths, L, order_plan(r), d_accum, (cudaStream_t)stream);
     const bool stale = !b->exec || b->graph_accum != d_accum || b->graph_block != L.block ||
-                       b->graph_stack != r->launch_stack || b->graph_wave != L.wave ||
+                       b->graph_stack != r->launch_stack || b->graph_wave != L.wave || b->graph_order != r->launch_order ||
                        b->graph_paths_gen != r->paths_gen;
     if (stale) {
         drop_graph(b);
         TT_CUDA_N(cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal));
-        st = issue(a, b->total_paths, L, d_accum, b->cap);
+        st = issue(a, b->total_paths, L, order_plan(r), d_accum, b->cap);
         cudaGraph_t g = nullptr;
         const cudaError_t e = cudaStreamEndCapture(b->cap, &g);
         if (st != TT_OK) {
@@ -1262,6 +1314,7 @@ tt_status tt_batch_render(tt_batch *b, void *d_accum, int use_graph, void *strea
         b->graph_block = L.block;
         b->graph_stack = r->launch_stack;
         b->graph_wave = L.wave;
+        b->graph_order = r->launch_order;
         b->graph_paths_gen = r->paths_gen;
     }
     TT_CUDA_N(cudaGraphLaunch(b->exec, (cudaStream_t)stream));
@@ -1282,24 +1335,29 @@ tt_status tt_batch_autotune(tt_batch *b, int64_t sample_paths, void *stream, tt_
     const long long sample = std::min<long long>(b->total_paths, sample_paths > 0 ? sample_paths : (8ll << 20));
     static const int kWaves[] = {1 << 20, 1 << 21, 1 << 22};
     PathSoA ps;
+    const int order_was = r->launch_order;
+    r->launch_order = 1;  // the trials with ordered queues need its scratch
     tt_status st = ensure_paths(r, (int)std::min<long long>(sample, kWaves[2]), ps);
+    r->launch_order = order_was;
     if (st != TT_OK) return st;
     NativeArgs a = batch_args(b, ps);
+    const OrderPlan plan = order_plan(r);
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     TT_CUDA_N(cudaEventCreate(&e0));
     TT_CUDA_N(cudaEventCreate(&e1));
     float best = 3.4e38f;
-    tt_launch_shape best_shape{r->launch_block, r->launch_stack, r->launch_wave, 0.0f};
+    tt_launch_shape best_shape{r->launch_block, r->launch_stack, r->launch_wave, r->launch_order, 0.0f};
     int count = 0;
     for (int bi = 0; bi < kNumBlockShapes; bi++)
         for (int si = 0; si < kNumStackShapes; si++)
-            for (int wave : kWaves) {
+            for (int wave : kWaves)
+                for (int order = 0; order < 2; order++) {
                 if (wave > kWaves[0] && wave / 2 >= sample) continue;  // the same as a smaller wave
                 Launch L;
-                st = resolve_launch(r, kBlockShapes[bi], kStackShapes[si], wave, L);
-                if (st == TT_OK) st = issue(a, std::min<long long>(sample, 1 << 16), L, nullptr, s);  // warm-up
+                st = resolve_launch(r, kBlockShapes[bi], kStackShapes[si], wave, order, L);
+                if (st == TT_OK) st = issue(a, std::min<long long>(sample, 1 << 16), L, plan, nullptr, s);  // warm-up
                 cudaError_t e = cudaEventRecord(e0, s);
-                if (st == TT_OK && e == cudaSuccess) st = issue(a, sample, L, nullptr, s);
+                if (st == TT_OK && e == cudaSuccess) st = issue(a, sample, L, plan, nullptr, s);
                 if (e == cudaSuccess) e = cudaEventRecord(e1, s);
                 if (e == cudaSuccess) e = cudaEventSynchronize(e1);
                 float ms = 0.0f;
@@ -1309,7 +1367,7 @@ tt_status tt_batch_autotune(tt_batch *b, int64_t sample_paths, void *stream, tt_
                     cudaEventDestroy(e1);
                     return st != TT_OK ? st : cuda_fail_n(e, "autotune timing");
                 }
-                const tt_launch_shape shape{kBlockShapes[bi], kStackShapes[si], wave, ms};
+                const tt_launch_shape shape{kBlockShapes[bi], kStackShapes[si], wave, order, ms};
                 if (results && count < max_results) results[count] = shape;
                 count++;
                 if (ms < best) {
@@ -1322,6 +1380,7 @@ tt_status tt_batch_autotune(tt_batch *b, int64_t sample_paths, void *stream, tt_
     r->launch_block = best_shape.block;
     r->launch_stack = best_shape.stack_shared;
     r->launch_wave = best_shape.wave_paths;
+    r->launch_order = best_shape.ordered;
     if (n_results) *n_results = count;
     return TT_OK;
 }

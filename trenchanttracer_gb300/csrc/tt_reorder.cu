@@ -39,11 +39,13 @@ constexpr int kProbeStride = 16;  // the coherence probe looks at every 16th war
 static_assert(kScanChunk == 8 * kOrderBlock && kNumChunks == 4 * kOrderBlock, "scan shapes");
 static_assert(((1 << (kOrderDirBits + kOrderMinOriginBits)) / kScanChunk) % 4 == 0, "whole uint4 of chunk totals");
 
-// State block (64-bit words): for call parity p, words 2p and 2p + 1 = sampled uniform warps and
-// sampled full warps of that call; each call clears the other parity's pair for the next one.
+// State block (64-bit words): [0] sampled uniform warps, [1] sampled full warps, [2] probe blocks
+// done, [3] the decision (1: ordered). The probe's last block to finish writes the decision and
+// clears [0..2] for the next call, so calls need no other bookkeeping (and replay in a graph).
 struct OrderArgs {
     const float4 *rays;
-    int64_t n;
+    int64_t n;         // rays, or the capacity when n_dev is set
+    const int *n_dev;  // rays = min(*n_dev, n) when set
     OrderGrid g;
     uint2 *kr;         // per ray: key, rank within the key
     int *pos;          // per ray: its sorted slot
@@ -51,10 +53,15 @@ struct OrderArgs {
     unsigned *counts;  // 2^key_bits
     unsigned *sums;    // chunk totals
     int key_bits;
-    unsigned long long *state;  // this call's pair
-    unsigned long long *next;   // the next call's pair
+    unsigned long long *state;
     unsigned *err;
 };
+
+__device__ __forceinline__ int64_t order_rays(const OrderArgs &a) {
+    if (!a.n_dev) return a.n;
+    const int64_t m = *a.n_dev;
+    return m < 0 ? 0 : (m > a.n ? a.n : m);
+}
 
 // inclusive scan of one value per lane
 __device__ __forceinline__ unsigned warp_scan(unsigned x) {
@@ -85,21 +92,21 @@ __device__ __forceinline__ unsigned block_exclusive_scan(unsigned x, unsigned *s
     return excl;
 }
 
-// (1) clear the counts and the next call's pair; probe
+// (1) clear the counts; probe; the last block decides
 __global__ void __launch_bounds__(kOrderBlock) k_order_probe(OrderArgs a) {
     __shared__ unsigned s_probe[2];
     const int lane = threadIdx.x & 31;
     const int64_t tid = (int64_t)blockIdx.x * kOrderBlock + threadIdx.x;
     const int64_t nthreads = (int64_t)gridDim.x * kOrderBlock;
-    if (tid < 2) a.next[tid] = 0ull;
+    const int64_t n = order_rays(a);
     for (int64_t j = tid; j < (1 << a.key_bits) / 4; j += nthreads)
         reinterpret_cast<uint4 *>(a.counts)[j] = make_uint4(0u, 0u, 0u, 0u);
     if (threadIdx.x < 2) s_probe[threadIdx.x] = 0u;
     __syncthreads();
-    const int64_t warps = (a.n + 31) / 32;
+    const int64_t warps = (n + 31) / 32;
     unsigned uniform = 0, full = 0;
     for (int64_t w = (tid >> 5) * kProbeStride; w < warps; w += (nthreads >> 5) * kProbeStride) {
-        if (w * 32 + 32 > a.n) continue;  // only full warps count; w is the same in every lane
+        if (w * 32 + 32 > n) continue;  // only full warps count; w is the same in every lane
         const int64_t i = w * 32 + lane;
         const unsigned key = order_key(__ldg(a.rays + 2 * i), __ldg(a.rays + 2 * i + 1), a.g);
         full++;
@@ -110,9 +117,21 @@ __global__ void __launch_bounds__(kOrderBlock) k_order_probe(OrderArgs a) {
         atomicAdd(&s_probe[1], full);
     }
     __syncthreads();
-    if (threadIdx.x == 0 && s_probe[1]) {
-        atomicAdd(a.state + 0, (unsigned long long)s_probe[0]);
-        atomicAdd(a.state + 1, (unsigned long long)s_probe[1]);
+    if (threadIdx.x == 0) {
+        if (s_probe[1]) {
+            atomicAdd(a.state + 0, (unsigned long long)s_probe[0]);
+            atomicAdd(a.state + 1, (unsigned long long)s_probe[1]);
+        }
+        __threadfence();
+        if (atomicAdd(a.state + 2, 1ull) == (unsigned long long)gridDim.x - 1) {  // every block's counts are in
+            const unsigned long long u = atomicAdd(a.state + 0, 0ull), f = atomicAdd(a.state + 1, 0ull);
+            // ordered unless mostly uniform; fewer than kOrderMinRays stay in their own order
+            a.state[3] = (f > 0 && 2 * u <= f && n >= kOrderMinRays) ? 1ull : 0ull;
+            a.state[0] = 0ull;
+            a.state[1] = 0ull;
+            a.state[2] = 0ull;
+            __threadfence();
+        }
     }
 }
 
@@ -121,10 +140,11 @@ __global__ void __launch_bounds__(kOrderBlock) k_order_keys(OrderArgs a) {
     if (!order_built(a.state)) return;
     const int lane = threadIdx.x & 31;
     const int64_t nthreads = (int64_t)gridDim.x * kOrderBlock;
-    for (int64_t base = ((int64_t)blockIdx.x * kOrderBlock + threadIdx.x) & ~int64_t(31); base < a.n;
+    const int64_t n = order_rays(a);
+    for (int64_t base = ((int64_t)blockIdx.x * kOrderBlock + threadIdx.x) & ~int64_t(31); base < n;
          base += nthreads) {
         const int64_t i = base + lane;
-        const bool valid = i < a.n;
+        const bool valid = i < n;
         unsigned key = 0xffffffffu;  // no real key has bit 31 set
         if (valid) key = order_key(__ldg(a.rays + 2 * i), __ldg(a.rays + 2 * i + 1), a.g);
         const unsigned peers = __match_any_sync(0xffffffffu, key);
@@ -180,7 +200,8 @@ __global__ void __launch_bounds__(kOrderBlock) k_order_scatter(OrderArgs a) {
     }
     __syncthreads();
     unsigned bad = 0;
-    for (int64_t i = (int64_t)blockIdx.x * kOrderBlock + threadIdx.x; i < a.n; i += (int64_t)gridDim.x * kOrderBlock) {
+    const int64_t n = order_rays(a);
+    for (int64_t i = (int64_t)blockIdx.x * kOrderBlock + threadIdx.x; i < n; i += (int64_t)gridDim.x * kOrderBlock) {
         const uint2 kr = a.kr[i];
         if (kr.x >= (1u << a.key_bits)) {
             a.pos[i] = -1;
@@ -188,7 +209,7 @@ __global__ void __launch_bounds__(kOrderBlock) k_order_scatter(OrderArgs a) {
             continue;
         }
         const uint64_t pos = (uint64_t)s_prefix[kr.x / kScanChunk] + a.counts[kr.x] + kr.y;
-        if (pos < (uint64_t)a.n) {
+        if (pos < (uint64_t)n) {
             a.sorted[2 * pos] = __ldg(a.rays + 2 * i);
             a.sorted[2 * pos + 1] = __ldg(a.rays + 2 * i + 1);
             a.pos[i] = (int)pos;
@@ -275,8 +296,8 @@ size_t reorder_scratch_bytes(int64_t n) { return reorder_state_offset(n) + 256; 
 
 static std::atomic<int> g_order_sms[64];  // SMs per device (0 = not yet known)
 
-tt_status reorder_rays(const float4 *rays, int64_t n, const float lo[3], const float hi[3], void *scratch,
-                       size_t state_at, unsigned parity, unsigned *err, cudaStream_t s, OrderOut *out) {
+tt_status reorder_rays(const float4 *rays, int64_t n, const int *n_dev, const float lo[3], const float hi[3],
+                       void *scratch, size_t state_at, unsigned *err, cudaStream_t s, OrderOut *out) {
     if (n <= 0 || n >= ((int64_t)1 << 31)) return fail(TT_ERR_INVALID, "ray ordering: n must be in 1..2^31-1");
     if (state_at < reorder_state_offset(n) || (state_at & 255))
         return fail(TT_ERR_INVALID, "ray ordering: scratch too small for this many rays");
@@ -294,6 +315,7 @@ tt_status reorder_rays(const float4 *rays, int64_t n, const float lo[3], const f
     OrderArgs a;
     a.rays = rays;
     a.n = n;
+    a.n_dev = n_dev;
     const int ob = order_origin_bits(n);
     a.g = order_grid(lo, hi, ob);
     a.key_bits = kOrderDirBits + ob;
@@ -308,9 +330,7 @@ tt_status reorder_rays(const float4 *rays, int64_t n, const float lo[3], const f
     a.counts = reinterpret_cast<unsigned *>(p);
     p += al256(4ull << kOrderBits);
     a.sums = reinterpret_cast<unsigned *>(p);
-    unsigned long long *state = reinterpret_cast<unsigned long long *>(static_cast<char *>(scratch) + state_at);
-    a.state = state + 2 * (parity & 1u);
-    a.next = state + 2 * ((parity & 1u) ^ 1u);
+    a.state = reinterpret_cast<unsigned long long *>(static_cast<char *>(scratch) + state_at);
     a.err = err;
     const int64_t want = (n + kOrderBlock - 1) / kOrderBlock;
     const unsigned grid = (unsigned)(want < (int64_t)sms * 8 ? want : (int64_t)sms * 8);

@@ -89,25 +89,24 @@ struct OrderOut {
     const unsigned long long *state;  // order_built(state): whether pos / sorted were built
 };
 
-// Launches (on stream s) the ordering of n rays within scene bounds lo < hi per axis. The scratch
-// holds at least reorder_scratch_bytes(n); its state block sits at byte state_at, fixed for the
-// scratch's life (reorder_state_offset of the size it was made for). `parity` must alternate
-// between consecutive calls on the same scratch, which must all be on one stream (each call
-// clears the other parity's counters for the next one). Device-side errors go to *err as
-// kErrOrder.
-tt_status reorder_rays(const float4 *rays, int64_t n, const float lo[3], const float hi[3], void *scratch,
-                       size_t state_at, unsigned parity, unsigned *err, cudaStream_t s, OrderOut *out);
+// Launches (on stream s) the ordering of n rays (or of min(*n_dev, n) when n_dev is set: a count
+// that lives on the device) within scene bounds lo < hi per axis. The scratch holds at least
+// reorder_scratch_bytes(n); its 256-byte state block sits at byte state_at, zeroed when the
+// scratch was made and fixed for its life (reorder_state_offset of the size it was made for).
+// Calls on one scratch must be ordered (one stream). Launches only, no allocation, so a call can
+// be captured in a CUDA graph. Device-side errors go to *err as kErrOrder.
+tt_status reorder_rays(const float4 *rays, int64_t n, const int *n_dev, const float lo[3], const float hi[3],
+                       void *scratch, size_t state_at, unsigned *err, cudaStream_t s, OrderOut *out);
 
 // After the trace kernel wrote hits of hit_bytes (8 or 24) per sorted slot into out.sorted_hits:
 // moves each ray's hit to hits[ray] (launch only; nothing to do when the order was not built).
 tt_status reorder_unpermute(const OrderOut &out, int64_t n, void *hits, size_t hit_bytes, unsigned *err,
                             cudaStream_t s);
 
-// state[0]: sampled warps whose 32 keys are all equal, state[1]: sampled full warps. False when
-// more than half were uniform: the rays are coherent already (camera rays share one origin cell
-// and neighbouring pixels one direction cell) and are traced in their own order.
-__device__ __forceinline__ bool order_built(const unsigned long long *state) {
-    return 2ull * state[0] <= state[1];
-}
+// Whether this call's rays were ordered: false when more than half of the sampled warps held 32
+// equal keys (the rays are coherent already: camera rays share one origin cell and neighbouring
+// pixels one direction cell) or fewer than kOrderMinRays rays came; they are then traced in their
+// own order.
+__device__ __forceinline__ bool order_built(const unsigned long long *state) { return state[3] == 1ull; }
 
 }  // namespace tt

@@ -65,8 +65,7 @@ struct DeviceBVH {
     // ray-ordering scratch per work-counter slot (caller stream, three pipeline streams)
     void *order[4] = {nullptr, nullptr, nullptr, nullptr};
     size_t order_bytes[4] = {0, 0, 0, 0};
-    size_t order_state_at[4] = {0, 0, 0, 0};        // byte offset of the ordering state block
-    unsigned long long order_calls[4] = {0, 0, 0, 0};  // calls per scratch (the low bit is the parity)
+    size_t order_state_at[4] = {0, 0, 0, 0};  // byte offset of the ordering state block
     // device staging, streams and events for the host-buffer entry point's copy/compute pipeline
     void *d_stage = nullptr;
     size_t d_stage_bytes = 0;
@@ -351,14 +350,12 @@ static tt_status launch_trace(const DeviceBVH &d, const void *d_rays, int64_t n,
             if (e != cudaSuccess) return fail(TT_ERR_OOM, std::string("ray ordering scratch: ") + cudaGetErrorString(e));
             dm.order_bytes[k] = need;
             dm.order_state_at[k] = reorder_state_offset(n);
-            dm.order_calls[k] = 0;
             e = cudaMemsetAsync(static_cast<char *>(dm.order[k]) + dm.order_state_at[k], 0, 256, stream);
             if (e != cudaSuccess) return fail(TT_ERR_CUDA, std::string("ray ordering scratch: ") + cudaGetErrorString(e));
         }
-        const tt_status st = reorder_rays(a.rays, n, d.lo, d.hi, dm.order[k], dm.order_state_at[k],
-                                          (unsigned)dm.order_calls[k], a.err, stream, &order);
+        const tt_status st =
+            reorder_rays(a.rays, n, nullptr, d.lo, d.hi, dm.order[k], dm.order_state_at[k], a.err, stream, &order);
         if (st != TT_OK) return st;
-        dm.order_calls[k]++;
         a.sorted = order.sorted;
         a.sorted_hits = order.sorted_hits;
         a.order_state = order.state;
@@ -447,6 +444,12 @@ using namespace tt;
 
 namespace tt {
 BvhView dbvh_view(const tt_dbvh *bvh) { return bvh->d.view; }
+void dbvh_bounds(const tt_dbvh *bvh, float lo[3], float hi[3]) {
+    for (int k = 0; k < 3; k++) {
+        lo[k] = bvh->d.lo[k];
+        hi[k] = bvh->d.hi[k];
+    }
+}
 }  // namespace tt
 
 extern "C" {
