@@ -200,11 +200,17 @@ def test_host_path_full_size_matches_device_path(terrain_full):
     """The host-buffer entry point at 4M rays: coherent rays go in 1M-ray chunks in their own order,
     incoherent ones in growing chunks that are each ordered; every hit equals the device path's."""
     for name, rays in terrain_full.sets.items():
+        dev = trace(terrain_full.dbvh, rays, True)
         hits = np.empty((rays.shape[0], 2), np.int32)
         terrain_full.dbvh.intersect_host(np.ascontiguousarray(rays), hits, closest=True)
-        dev = trace(terrain_full.dbvh, rays, True)
         assert np.array_equal(hits[:, 0], dev["id"]), name
         assert np.array_equal(hits[:, 1], dev["t"].view(np.int32)), name
+        # page-locked buffers: coherent rays are traced straight from and into host memory
+        h_rays = torch.from_numpy(np.ascontiguousarray(rays)).pin_memory()
+        h_hits = torch.full((rays.shape[0], 2), -7, dtype=torch.int32).pin_memory()
+        terrain_full.dbvh.intersect_host(h_rays.numpy(), h_hits.numpy(), closest=True)
+        assert np.array_equal(h_hits.numpy()[:, 0], dev["id"]), name + " (page-locked)"
+        assert np.array_equal(h_hits.numpy()[:, 1], dev["t"].view(np.int32)), name + " (page-locked)"
 
 
 def test_host_buffers_match_device_buffers(cornell):
