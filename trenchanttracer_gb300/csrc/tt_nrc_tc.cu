@@ -2,22 +2,27 @@
 // accumulator in tensor memory (TMEM), operands in shared memory, weights and feature records
 // brought in by bulk asynchronous copies (cp.async.bulk) that signal an mbarrier.
 //
-// One CTA of 128 threads owns a tile of 128 rows at a time (row r = thread r = TMEM lane r):
-//   records  cp.async.bulk of the tile's 128 x 64 B into shared memory
-//   encode   each thread builds its row's 160 BF16 inputs in the A buffer
-//   layers   one thread issues the layer's tcgen05.mma (M = 128, N = 64 or 16, K = 16 each) and a
-//            tcgen05.commit to an mbarrier; after the wait every warp reads its 32 TMEM lanes
-//            (tcgen05.ld 32x32b), applies ReLU, rounds to BF16 and writes the next layer's A
+// One CTA per SM, three warpgroups of 128 threads sharing one copy of the network's weights
+// (55.3 KB, loaded once per CTA). Each warpgroup owns its own stream of tiles of 128 rows (row r =
+// thread r of the group = TMEM lane r), its own A operand, its own 64 TMEM columns and two record
+// buffers, so three tiles are in flight per SM and a tile's records arrive while the previous tile
+// computes:
+//   records  cp.async.bulk of the next tile's 128 x 64 B into the other record buffer
+//   encode   each thread builds its row's 160 BF16 inputs in the group's A buffer
+//   layers   one thread of the group issues the layer's tcgen05.mma (M = 128, N = 64 or 16, K = 16
+//            each) and a tcgen05.commit to the group's mbarrier; after the wait every warp of the
+//            group reads its 32 TMEM lanes (tcgen05.ld 32x32b), applies ReLU, rounds to BF16 and
+//            writes the next layer's A
 //   output   exp of the first three columns of the last layer
-// The network's weights (55.3 KB, in the operand layout below) are loaded once per CTA.
+// A warpgroup synchronises on its own named barrier, so the three advance independently.
 //
 // Operand layout: no swizzle, K-major, 8 x 16-byte core matrices. A (128 x K): core (m8, k8) at
 // byte (k8 * 16 + m8) * 128, so the stride between 8-row groups (SBO) is 128 and between the two
 // K halves of one instruction (LBO) 2048. Weights W_l (N x K): core (n8, k8) at (k8 * N/8 + n8) *
-// 128 from the layer's base: SBO 128, LBO N/8 * 128. Shared memory holds A first, then the
-// weights, the records and the barriers, so that every operand address the descriptors can form
-// (with either of the two byte offsets applied along either dimension) lies inside the CTA's
-// own allocation.
+// 128 from the layer's base: SBO 128, LBO N/8 * 128. Shared memory holds the three A buffers
+// first, then the weights, the records and the barriers, so that every operand address the
+// descriptors can form (with either of the two byte offsets applied along either dimension) lies
+// inside the CTA's own allocation.
 //
 // Every wait is bounded (a clock budget of about a second): one thread waits, the outcome goes
 // to all threads through shared memory and a block barrier, so a failure is uniform; it is
@@ -34,8 +39,9 @@ namespace tt {
 namespace nrc {
 
 constexpr int kTcRows = 128;
-constexpr int kTcThreads = 128;
-constexpr int kTmemCols = 64;
+constexpr int kTcGroups = 3;                         // warpgroups (tiles in flight) per CTA
+constexpr int kTcThreads = 128 * kTcGroups;
+constexpr int kTmemCols = 256;                       // 64 per group, allocated as a power of two
 constexpr int kABytes = kTcRows * kIn * 2;           // 40960
 constexpr int kRecBytes = kTcRows * kRec * 4;        // 8192
 constexpr long long kWaitCycles = 2000000000ll;      // ~1 s at 2 GHz
@@ -45,7 +51,9 @@ __host__ __device__ constexpr int tc_out(int l) { return l == kLayers - 1 ? 16 :
 __host__ __device__ constexpr int tc_offset(int l) { return l == 0 ? 0 : tc_offset(l - 1) + layer_in(l - 1) * tc_out(l - 1); }
 constexpr int kTcWeights = tc_offset(kLayers);        // 27648 bf16
 constexpr int kTcWeightBytes = kTcWeights * 2;        // 55296
-constexpr int kTcSmem = kTcWeightBytes + kABytes + kRecBytes + 64;
+constexpr int kTcBarBytes = 128;  // weights barrier, per group 2 record + 1 product barriers, TMEM slot, flags
+constexpr int kTcSmem = kTcGroups * (kABytes + 2 * kRecBytes) + kTcWeightBytes + kTcBarBytes;
+static_assert(kTcSmem <= 232448, "fits the 227 KB a CTA may use");
 static_assert(kTcWeightBytes % 16 == 0 && kABytes % 16 == 0 && kRecBytes % 16 == 0, "bulk copy sizes");
 
 __host__ __device__ inline int tc_index(int l, int n, int k) {
@@ -160,16 +168,25 @@ struct TcArgs {
     unsigned *err;
 };
 
+__device__ __forceinline__ void group_sync(int group) {  // the 128 threads of one warpgroup
+    asm volatile("bar.sync %0, 128;" ::"r"(1 + group) : "memory");
+}
+
 __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(TcArgs a) {
     extern __shared__ __align__(128) uint8_t smem[];
-    __nv_bfloat16 *A = reinterpret_cast<__nv_bfloat16 *>(smem);
-    uint16_t *W = reinterpret_cast<uint16_t *>(smem + kABytes);
-    float *R = reinterpret_cast<float *>(smem + kABytes + kTcWeightBytes);
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kABytes + kTcWeightBytes + kRecBytes);  // [0] w [1] rec [2] mma
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 3);
-    int *ok = reinterpret_cast<int *>(bars + 4);
-    int *failed = ok + 1;  // the barrier (0..2) and parity of a wait that ran out
-    const int tid = threadIdx.x, warp = tid >> 5;
+    const int tid = threadIdx.x, group = tid >> 7, gt = tid & 127, warp_in_group = gt >> 5;
+    __nv_bfloat16 *A = reinterpret_cast<__nv_bfloat16 *>(smem + group * kABytes);
+    uint16_t *W = reinterpret_cast<uint16_t *>(smem + kTcGroups * kABytes);
+    float *R = reinterpret_cast<float *>(smem + kTcGroups * kABytes + kTcWeightBytes) +
+               (size_t)group * 2 * kTcRows * kRec;  // this group's two record buffers
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kTcGroups * (kABytes + 2 * kRecBytes) + kTcWeightBytes);
+    uint64_t *bar_w = bars;                      // weights
+    uint64_t *bar_rec = bars + 1 + 3 * group;    // [0] [1]: the group's record buffers
+    uint64_t *bar_mma = bars + 3 + 3 * group;    // the group's products
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 1 + 3 * kTcGroups);
+    int *ok_w = reinterpret_cast<int *>(tmem_slot + 1);  // the weights arrived
+    int *ok = ok_w + 1 + group;                          // this group's waits all ended
+    static_assert(8 * (1 + 3 * kTcGroups) + 4 + 4 * (1 + kTcGroups) <= kTcBarBytes, "barrier block");
 
     long long n = a.n_host;
     if (a.n_dev) {
@@ -177,73 +194,90 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(TcArgs a) {
         n = n < 0 ? 0 : (n > a.cap ? a.cap : n);
     }
     const long long ntiles = (n + kTcRows - 1) / kTcRows;
-    if ((long long)blockIdx.x >= ntiles) return;  // uniform per block: nothing allocated yet
+    if ((long long)blockIdx.x * kTcGroups >= ntiles) return;  // uniform per block: nothing allocated yet
 
     if (tid == 0) {
-        mbar_init(bars + 0, 1);
-        mbar_init(bars + 1, 1);
-        mbar_init(bars + 2, 1);
-        *ok = 1;
+        mbar_init(bar_w, 1);
+        for (int g = 0; g < kTcGroups; g++) {
+            mbar_init(bars + 1 + 3 * g, 1);
+            mbar_init(bars + 2 + 3 * g, 1);
+            mbar_init(bars + 3 + 3 * g, 1);
+            ok_w[1 + g] = 1;
+        }
+        *ok_w = 1;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
-    if (warp == 0) tmem_alloc(tmem_slot, kTmemCols);
+    if (tid < 32) tmem_alloc(tmem_slot, kTmemCols);
+    // Asynchronous operations of this group, counted by its issuing thread (gt == 0): the k-th
+    // completion of a barrier is awaited with parity k & 1, and whatever was issued and not yet
+    // awaited is drained (bounded) before the block exits.
+    int rec_issued[2] = {0, 0}, rec_done[2] = {0, 0}, mma_issued = 0, mma_done = 0;
+    const long long tstride = (long long)gridDim.x * kTcGroups;
+    const long long first = (long long)blockIdx.x * kTcGroups + group;
+    if (gt == 0 && first < ntiles) {  // the group's first records, while the weights come in
+        const long long r0 = first * kTcRows;
+        const uint32_t bytes = (uint32_t)((n - r0) < kTcRows ? (n - r0) : kTcRows) * kRec * 4;
+        mbar_expect_tx(bar_rec, bytes);
+        bulk_load(R, a.rec + r0 * kRec, bytes, bar_rec);
+        rec_issued[0]++;
+    }
     if (tid == 0) {
-        mbar_expect_tx(bars + 0, kTcWeightBytes);
-        bulk_load(W, a.w, kTcWeightBytes, bars + 0);
-        if (!mbar_wait(bars + 0, 0)) {
-            *ok = 0;
-            *failed = 0;
-        }
+        mbar_expect_tx(bar_w, kTcWeightBytes);
+        bulk_load(W, a.w, kTcWeightBytes, bar_w);
+        if (!mbar_wait(bar_w, 0)) *ok_w = 0;
     }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    const uint32_t tmem = *tmem_slot;
-    uint32_t ph_rec = 0, ph_mma = 0;
-    for (long long tile = blockIdx.x; tile < ntiles && *ok; tile += gridDim.x) {
+    const uint32_t tmem = *tmem_slot + (uint32_t)(group * 64);
+    if (!*ok_w && gt == 0) *ok = 0;
+    group_sync(group);
+    int buf = 0;
+    for (long long tile = first; *ok && tile < ntiles; tile += tstride) {
         const long long r0 = tile * kTcRows;
         const int rows = (int)((n - r0) < kTcRows ? (n - r0) : kTcRows);
-        if (tid == 0) {
-            mbar_expect_tx(bars + 1, (uint32_t)rows * kRec * 4);
-            bulk_load(R, a.rec + r0 * kRec, (uint32_t)rows * kRec * 4, bars + 1);
-            if (!mbar_wait(bars + 1, ph_rec)) {
-                *ok = 0;
-                *failed = 2 + (int)ph_rec;
-            }
+        float *Rb = R + buf * kTcRows * kRec;
+        if (gt == 0) {
+            if (mbar_wait(bar_rec + buf, (uint32_t)(rec_done[buf] & 1))) rec_done[buf]++;
+            else *ok = 0;
         }
-        ph_rec ^= 1;
-        __syncthreads();
+        group_sync(group);
         if (!*ok) break;
-        if (tid < rows) {
-            encode_row(R + tid * kRec, a.enc, A, tid);
+        if (gt < rows) {
+            encode_row(Rb + gt * kRec, a.enc, A, gt);
         } else {
             for (int k = 0; k < kIn; k += 8)
-                *reinterpret_cast<uint4 *>(A + a_offset(tid, k)) = make_uint4(0u, 0u, 0u, 0u);
+                *reinterpret_cast<uint4 *>(A + a_offset(gt, k)) = make_uint4(0u, 0u, 0u, 0u);
         }
         fence_async_smem();
         tc_fence_before();
-        __syncthreads();
+        group_sync(group);  // every row encoded: Rb is free again and A is ready
         tc_fence_after();
+        if (gt == 0 && tile + tstride < ntiles) {  // the next tile's records into the other buffer
+            const long long nr0 = (tile + tstride) * kTcRows;
+            const uint32_t bytes = (uint32_t)((n - nr0) < kTcRows ? (n - nr0) : kTcRows) * kRec * 4;
+            mbar_expect_tx(bar_rec + (buf ^ 1), bytes);
+            bulk_load(R + (buf ^ 1) * kTcRows * kRec, a.rec + nr0 * kRec, bytes, bar_rec + (buf ^ 1));
+            rec_issued[buf ^ 1]++;
+        }
         for (int l = 0; l < kLayers; l++) {
             const int K = layer_in(l), N = tc_out(l);
-            if (tid == 0) {
+            if (gt == 0) {
                 const uint32_t a0 = saddr(A), b0 = saddr(W + tc_offset(l));
                 const uint32_t idesc = idesc_bf16(kTcRows, N);
                 for (int s = 0; s < K / 16; s++)
                     umma(tmem, sdesc(a0 + s * 2 * 2048, 2048, 128), sdesc(b0 + s * 2 * (N / 8) * 128, (N / 8) * 128, 128),
                          idesc, s > 0 ? 1u : 0u);
-                umma_commit(bars + 2);
-                if (!mbar_wait(bars + 2, ph_mma)) {
-                    *ok = 0;
-                    *failed = 4 + (int)ph_mma;
-                }
+                umma_commit(bar_mma);
+                mma_issued++;
+                if (mbar_wait(bar_mma, (uint32_t)(mma_done & 1))) mma_done++;
+                else *ok = 0;
             }
-            ph_mma ^= 1;
-            __syncthreads();
+            group_sync(group);
             tc_fence_after();
             if (!*ok) break;
-            const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
+            const uint32_t lane_addr = tmem + ((uint32_t)(warp_in_group * 32) << 16);
             if (l < kLayers - 1) {
 #pragma unroll
                 for (int c = 0; c < kHidden; c += 16) {
@@ -256,36 +290,38 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(TcArgs a) {
                         const __nv_bfloat162 b = __floats2bfloat162_rn(fmaxf(v[2 * j], 0.f), fmaxf(v[2 * j + 1], 0.f));
                         w[j] = *reinterpret_cast<const uint32_t *>(&b);
                     }
-                    *reinterpret_cast<uint4 *>(A + a_offset(tid, c)) = make_uint4(w[0], w[1], w[2], w[3]);
-                    *reinterpret_cast<uint4 *>(A + a_offset(tid, c + 8)) = make_uint4(w[4], w[5], w[6], w[7]);
+                    *reinterpret_cast<uint4 *>(A + a_offset(gt, c)) = make_uint4(w[0], w[1], w[2], w[3]);
+                    *reinterpret_cast<uint4 *>(A + a_offset(gt, c + 8)) = make_uint4(w[4], w[5], w[6], w[7]);
                 }
                 fence_async_smem();
             } else {
                 float v[16];
                 tmem_ld16(lane_addr, v);
                 tmem_wait_ld();
-                if (tid < rows) {
-                    float *o = a.rgb + (r0 + tid) * 3;
+                if (gt < rows) {
+                    float *o = a.rgb + (r0 + gt) * 3;
                     o[0] = expf(fminf(v[0], 20.0f));
                     o[1] = expf(fminf(v[1], 20.0f));
                     o[2] = expf(fminf(v[2], 20.0f));
                 }
             }
             tc_fence_before();
-            __syncthreads();
+            group_sync(group);
             tc_fence_after();
         }
+        buf ^= 1;
     }
-    if (tid == 0 && !*ok) {
-        atomicOr(a.err, kErrMlpWait);
-        // let the copy or the products still in flight land (bounded again) before TMEM is freed
-        const int f = *failed;
-        mbar_wait(bars + (f == 0 ? 0 : (f < 4 ? 1 : 2)), f == 0 ? 0u : (uint32_t)(f & 1));
+    if (gt == 0) {
+        if (!*ok) atomicOr(a.err, kErrMlpWait);
+        // drain what this group issued and did not see complete (bounded again), before TMEM is freed
+        for (int b = 0; b < 2; b++)
+            while (rec_done[b] < rec_issued[b] && mbar_wait(bar_rec + b, (uint32_t)(rec_done[b] & 1))) rec_done[b]++;
+        while (mma_done < mma_issued && mbar_wait(bar_mma, (uint32_t)(mma_done & 1))) mma_done++;
     }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    if (warp == 0) tmem_free(tmem, kTmemCols);
+    if (tid < 32) tmem_free(*tmem_slot, kTmemCols);
 }
 
 __global__ void k_tc_layout(const float *w, uint16_t *out) {
@@ -334,8 +370,8 @@ tt_status tc_infer(const uint16_t *w_tc, const float *rec, long long n_host, con
     a.err = err;
     const long long rows = n_dev ? cap : n_host;
     const long long tiles = (rows + kTcRows - 1) / kTcRows;
-    const long long cap_blocks = 2ll * num_sms;
-    const int grid = (int)(tiles < 1 ? 1 : (tiles < cap_blocks ? tiles : cap_blocks));
+    const long long want = (tiles + kTcGroups - 1) / kTcGroups;  // blocks, each with three groups
+    const int grid = (int)(want < 1 ? 1 : (want < num_sms ? want : num_sms));
     k_mlp_forward_tc<<<grid, kTcThreads, kTcSmem, s>>>(a);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(TT_ERR_CUDA, std::string("tensor-core MLP: ") + cudaGetErrorString(e));
