@@ -35,7 +35,7 @@ constexpr int kThreads = 32 * kWarps;
 constexpr int kEncStride = kIn + kRowPad;  // bf16 per row of a warp's encoding tile
 constexpr int kWeightBytes = kPadded * 2;
 constexpr int kFwdSmem = kWeightBytes + kWarps * 16 * kEncStride * 2;
-constexpr int kChunkRows = 512;            // rows per weight-gradient CTA
+constexpr int kChunkRows = 128;            // rows per weight-gradient CTA (128 CTAs x 6 layers per 16K batch)
 constexpr int kSub = 32;                   // rows per staged weight-gradient tile
 constexpr int kSubStride = kSub + 8;
 
@@ -418,7 +418,8 @@ struct AdamArgs {
     float *grad;  // optional: the summed gradient
     float *master, *m, *v, *ema;
     uint16_t *w_train, *w_ema;
-    int *step;   // device step counter (incremented by k_adam_step)
+    uint16_t *w_tc_train, *w_tc_ema;  // the same in the tcgen05 operand layout
+    int *step;   // [0] device step counter, advanced by the last block; [1] blocks done
     const int *n_dev;
     long long n_host, off;
     float lr, beta1, beta2, eps, ema_f;
@@ -433,7 +434,7 @@ __device__ __forceinline__ int padded_index(int i) {
     return p_offset(l) + (local / in) * (in + kRowPad) + local % in;
 }
 
-__global__ void k_adam(AdamArgs a) {
+__device__ __forceinline__ void k_adam_body(const AdamArgs &a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kParams) return;
     long long n = a.n_host;
@@ -442,7 +443,7 @@ __global__ void k_adam(AdamArgs a) {
     for (int c = 0; c < a.chunks; c++) g += a.partial[(size_t)c * kParams + i];
     if (a.grad) a.grad[i] = g;
     if (!a.update || n <= 0) return;
-    const int t = *a.step + 1;
+    const int t = a.step[0] + 1;
     const float m = a.beta1 * a.m[i] + (1.0f - a.beta1) * g;
     const float v = a.beta2 * a.v[i] + (1.0f - a.beta2) * g * g;
     a.m[i] = m;
@@ -457,10 +458,30 @@ __global__ void k_adam(AdamArgs a) {
     const __nv_bfloat16 wb = __float2bfloat16_rn(w), eb = __float2bfloat16_rn(e);
     a.w_train[pi] = *reinterpret_cast<const uint16_t *>(&wb);
     a.w_ema[pi] = *reinterpret_cast<const uint16_t *>(&eb);
+    int l = 0;
+    while (l + 1 < kLayers && i >= w_offset(l + 1)) l++;
+    const int local = i - w_offset(l);
+    const int ti = tc_index(l, local / layer_in(l), local % layer_in(l));
+    a.w_tc_train[ti] = *reinterpret_cast<const uint16_t *>(&wb);
+    a.w_tc_ema[ti] = *reinterpret_cast<const uint16_t *>(&eb);
 }
 
-__global__ void k_adam_step(int *step, const int *n_dev, long long off) {
-    if (!n_dev || (long long)*n_dev - off > 0) *step += 1;
+__global__ void k_adam(AdamArgs a) { k_adam_body(a); }
+
+// k_adam with the step counter advanced by its last block to finish, once every block has read it
+__global__ void k_adam_update(AdamArgs a) {
+    k_adam_body(a);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(a.step + 1, 1) == (int)gridDim.x - 1) {
+            long long n = a.n_host;
+            if (a.n_dev) n = (long long)*a.n_dev - a.off;
+            if (n > 0) a.step[0] += 1;
+            a.step[1] = 0;
+            __threadfence();
+        }
+    }
 }
 
 }  // namespace nrc
@@ -617,6 +638,8 @@ tt_status train_pass(tt_cache *c, const float *rec, const float *target, long lo
     ad.ema = c->ema;
     ad.w_train = c->w_train;
     ad.w_ema = c->w_ema;
+    ad.w_tc_train = c->w_tc_train;
+    ad.w_tc_ema = c->w_tc_ema;
     ad.step = c->step;
     ad.n_dev = n_dev;
     ad.n_host = a.n_host;
@@ -627,12 +650,8 @@ tt_status train_pass(tt_cache *c, const float *rec, const float *target, long lo
     ad.eps = c->p.eps;
     ad.ema_f = c->p.ema;
     ad.update = update;
-    k_adam<<<(kParams + 255) / 256, 256, 0, s>>>(ad);
-    if (update) {
-        k_adam_step<<<1, 1, 0, s>>>(c->step, n_dev, n_dev ? off : 0);
-        tc_relayout(c->master, c->w_tc_train, s);
-        tc_relayout(c->ema, c->w_tc_ema, s);
-    }
+    if (update) k_adam_update<<<(kParams + 255) / 256, 256, 0, s>>>(ad);  // also the tcgen05-layout copies
+    else k_adam<<<(kParams + 255) / 256, 256, 0, s>>>(ad);
     TT_CUDA_C(cudaGetLastError());
     return TT_OK;
 }

@@ -51,6 +51,17 @@ constexpr int kParams = w_offset(kLayers);     // 27136
 constexpr int kPadded = p_offset(kLayers);     // 29760 bf16 = 59520 bytes
 static_assert(kParams == 160 * 64 + 4 * 64 * 64 + 8 * 64, "parameter count");
 
+// The tcgen05 operand layout of the weights (tt_nrc_tc.cu): layer l as N = tc_out(l) rows of K =
+// layer_in(l) BF16 values in 8 x 8 core matrices, K-major; rows beyond the layer's outputs are 0.
+__host__ __device__ constexpr int tc_out(int l) { return l == kLayers - 1 ? 16 : kHidden; }
+__host__ __device__ constexpr int tc_offset(int l) { return l == 0 ? 0 : tc_offset(l - 1) + layer_in(l - 1) * tc_out(l - 1); }
+constexpr int kTcWeights = tc_offset(kLayers);  // 27648 bf16
+__host__ __device__ inline int tc_index(int l, int n, int k) {
+    const int ng = tc_out(l) / 8;
+    return tc_offset(l) + ((k / 8) * ng + n / 8) * 64 + (n % 8) * 8 + (k % 8);
+}
+
+
 #ifdef __CUDACC__
 // sin(pi x) and cos(pi x): the argument reduced exactly to r = x - 2 rint(x / 2) in [-1, 1],
 // then the hardware approximations of sin and cos of pi r (absolute error ~4e-7, far below the

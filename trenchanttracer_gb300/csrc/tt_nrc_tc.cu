@@ -47,19 +47,12 @@ constexpr int kRecBytes = kTcRows * kRec * 4;        // 8192
 constexpr long long kWaitCycles = 2000000000ll;      // ~1 s at 2 GHz
 constexpr unsigned kErrMlpWait = 8u;                 // error word bit: a tensor-core wait ran out
 
-__host__ __device__ constexpr int tc_out(int l) { return l == kLayers - 1 ? 16 : kHidden; }
-__host__ __device__ constexpr int tc_offset(int l) { return l == 0 ? 0 : tc_offset(l - 1) + layer_in(l - 1) * tc_out(l - 1); }
-constexpr int kTcWeights = tc_offset(kLayers);        // 27648 bf16
 constexpr int kTcWeightBytes = kTcWeights * 2;        // 55296
 constexpr int kTcBarBytes = 128;  // weights barrier, per group 2 record + 1 product barriers, TMEM slot, flags
 constexpr int kTcSmem = kTcGroups * (kABytes + 2 * kRecBytes) + kTcWeightBytes + kTcBarBytes;
 static_assert(kTcSmem <= 232448, "fits the 227 KB a CTA may use");
 static_assert(kTcWeightBytes % 16 == 0 && kABytes % 16 == 0 && kRecBytes % 16 == 0, "bulk copy sizes");
 
-__host__ __device__ inline int tc_index(int l, int n, int k) {
-    const int ng = tc_out(l) / 8;
-    return tc_offset(l) + ((k / 8) * ng + n / 8) * 64 + (n % 8) * 8 + (k % 8);
-}
 
 // ---- PTX helpers ------------------------------------------------------------------------------
 __device__ __forceinline__ uint32_t saddr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
