@@ -25,6 +25,7 @@
 // All but WARP_VOTE return the per-ray result of the reference's algorithm, bit for bit.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -61,6 +62,9 @@ struct DeviceBVH {
     int num_sms = 0;
     int blocks_per_sm[NUM_VARIANTS] = {1, 1, 1, 1, 1, 1, 1, 1};
     int variant = VARIANT_SORTED;
+    // L2 access-policy window over the node array for the trace launches (0 bytes: none)
+    size_t l2_window_bytes = 0;
+    float l2_hit_ratio = 0.0f;
     float lo[3] = {-1.f, -1.f, -1.f}, hi[3] = {1.f, 1.f, 1.f};  // scene bounds (root boxes)
     // ray-ordering scratch per work-counter slot (caller stream, three pipeline streams)
     void *order[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -228,6 +232,22 @@ static tt_status upload(const CompactBVH &b, DeviceBVH &d) {
     }
     const size_t nb = 16ull * b.nodes.size(), vb = 16ull * b.vertices.size(), mb = 16ull * b.normals.size();
     const size_t tb = 4ull * b.tri_idx.size(), ab = 4ull * b.mat_idx.size();
+    {  // L2 set-aside for the node array (a limit of this process's context; it ends with it)
+        int max_persist = 0, max_window = 0;
+        if (cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&max_window, cudaDevAttrMaxAccessPolicyWindowSize, dev) == cudaSuccess &&
+            max_persist > 0 && max_window > 0) {
+            size_t cur = 0;
+            cudaDeviceGetLimit(&cur, cudaLimitPersistingL2CacheSize);
+            const size_t want = std::min(nb, (size_t)max_persist);
+            if (want > cur && cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, want) == cudaSuccess)
+                cudaDeviceGetLimit(&cur, cudaLimitPersistingL2CacheSize);
+            d.l2_window_bytes = std::min(nb, (size_t)max_window);
+            d.l2_hit_ratio = cur >= d.l2_window_bytes ? 1.0f : (float)cur / (float)d.l2_window_bytes;
+            if (cur == 0) d.l2_window_bytes = 0;
+        }
+        cudaGetLastError();
+    }
     auto align = [](size_t x) { return (x + 255) & ~size_t(255); };
     d.bytes = align(nb) + align(vb) + align(mb) + align(tb) + align(ab);
     cudaError_t e = cudaMalloc(&d.base, d.bytes);
@@ -283,33 +303,31 @@ static void release(DeviceBVH &d) {
     d = DeviceBVH();
 }
 
+// Launches a variant's kernel. The node array is the launch's L2 access-policy window when the
+// device allows one: node lines persist in the L2 set-aside and the rest of the window's traffic
+// (rays, triangles, hits lie outside it) keeps the normal policy, so streaming triangles cannot
+// push the nodes out.
 template <bool kClosest, bool kExt>
-static void launch_variant(int variant, unsigned blocks, cudaStream_t stream, const TraceArgs &a) {
-    switch (variant) {
-        case VARIANT_WARP:
-            trace_warp_kernel<kClosest, kExt, false, 0><<<blocks, kTraceBlock, 0, stream>>>(a);
-            break;
-        case VARIANT_WARP_SH16:
-            trace_warp_kernel<kClosest, kExt, false, 16><<<blocks, kTraceBlock, 0, stream>>>(a);
-            break;
-        case VARIANT_WARP_SH32:
-            trace_warp_kernel<kClosest, kExt, false, 32><<<blocks, kTraceBlock, 0, stream>>>(a);
-            break;
-        case VARIANT_DYNAMIC:
-            trace_dynamic_kernel<kClosest, kExt, 16><<<blocks, kTraceBlock, 0, stream>>>(a);
-            break;
-        case VARIANT_SORTED:
-            trace_warp_kernel<kClosest, kExt, false, 16, true><<<blocks, kTraceBlock, 0, stream>>>(a);
-            break;
-        case VARIANT_SH16_OCC:
-            trace_warp_kernel<kClosest, kExt, false, 16, false, kOccBlocks><<<blocks, kTraceBlock, 0, stream>>>(a);
-            break;
-        case VARIANT_SORTED_OCC:
-            trace_warp_kernel<kClosest, kExt, false, 16, true, kOccBlocks><<<blocks, kTraceBlock, 0, stream>>>(a);
-            break;
-        default:
-            trace_warp_kernel<kClosest, kExt, true, 0><<<blocks, kTraceBlock, 0, stream>>>(a);
+static cudaError_t launch_variant(const DeviceBVH &d, int variant, unsigned blocks, cudaStream_t stream,
+                                  TraceArgs a) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(blocks);
+    cfg.blockDim = dim3(kTraceBlock);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    if (d.l2_window_bytes) {
+        attr[0].id = cudaLaunchAttributeAccessPolicyWindow;
+        attr[0].val.accessPolicyWindow.base_ptr = const_cast<float4 *>(d.view.nodes);
+        attr[0].val.accessPolicyWindow.num_bytes = d.l2_window_bytes;
+        attr[0].val.accessPolicyWindow.hitRatio = d.l2_hit_ratio;
+        attr[0].val.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+        attr[0].val.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
     }
+    void *args[] = {&a};
+    return cudaLaunchKernelExC(&cfg, kernel_for<kClosest, kExt>(variant), args);
 }
 
 // unordered = true traces a SORTED / SORTED_OCC variant's rays in their own order (its unsorted twin).
@@ -365,14 +383,12 @@ static tt_status launch_trace(const DeviceBVH &d, const void *d_rays, int64_t n,
     const int64_t max_useful = (warps_needed * 32 + kTraceBlock - 1) / kTraceBlock;
     if (blocks > max_useful) blocks = max_useful;
     if (blocks < 1) blocks = 1;
-    if (closest) {
-        if (ext) launch_variant<true, true>(variant, (unsigned)blocks, stream, a);
-        else launch_variant<true, false>(variant, (unsigned)blocks, stream, a);
-    } else {
-        if (ext) launch_variant<false, true>(variant, (unsigned)blocks, stream, a);
-        else launch_variant<false, false>(variant, (unsigned)blocks, stream, a);
-    }
-    TT_CUDA(cudaGetLastError());
+    cudaError_t le;
+    if (closest) le = ext ? launch_variant<true, true>(d, variant, (unsigned)blocks, stream, a)
+                          : launch_variant<true, false>(d, variant, (unsigned)blocks, stream, a);
+    else le = ext ? launch_variant<false, true>(d, variant, (unsigned)blocks, stream, a)
+                  : launch_variant<false, false>(d, variant, (unsigned)blocks, stream, a);
+    TT_CUDA(le);
     if (a.order_state) return reorder_unpermute(order, n, d_hits, ext ? sizeof(tt_hit_ext) : sizeof(tt_hit), a.err, stream);
     return TT_OK;
 }
