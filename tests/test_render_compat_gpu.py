@@ -99,3 +99,45 @@ def test_compat_render_is_deterministic():
         out.append(acc.cpu().numpy())
     assert np.array_equal(out[0], out[1])
     assert out[0].mean() > 0.01
+
+
+@needs_ref
+def test_render_speed_beside_reference_kernel():
+    """The bench's Cornell view (512 x 512, 16 samples per frame): the reference's own
+    pathTracingKernel, tt_render_compat (the same algorithm, bit-compatible) and the native
+    wavefront tracer (its own algorithm: depth 8, roulette from 4, ordered queues), timed with CUDA
+    events on the same GB300. Printed for the record; the assertion only guards against the port
+    falling far behind the reference."""
+    from trenchanttracer_gb300 import render_params
+    sc = Scene.from_mesh(scenes.cornell(subdiv=5))
+    bvh = BVHCompact.build(sc, 1e-5, 1, 8)
+    r = Renderer(DeviceBVH(bvh), sc)
+    cam = make_camera_meta(512, 512, [0.0, 0.0, 1.55], [0.0, 0.0, -1.0], fov=(45.0, 45.0))
+    spp, npx = 16, 512 * 512
+    init = np.zeros(3 * npx, np.float32)
+    ref_ms = min(refgpu.render(bvh.arrays(), sc.materials_raw(), sc.geometries_raw(), sc.env(), cam,
+                               render_meta(f, spp), init)[1] for f in (1, 2, 3))
+    acc = torch.zeros(3 * npx, dtype=torch.float32, device="cuda")
+
+    def timed(fn):
+        best = 1e9
+        for f in range(4):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn(f)
+            e1.record()
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1)) if f else best
+        r.check()
+        return best
+
+    compat_ms = timed(lambda f: r.render_compat(cam, render_meta(f + 1, spp), acc))
+    old = r.launch
+    r.set_launch(128, 16, 1 << 22, 1)
+    native_ms = timed(lambda f: r.render_native(cam, render_params(spp=spp, sample_offset=f * spp, max_depth=8,
+                                                                   rr_depth=4, seed=1), acc))
+    r.set_launch(*old)
+    rate = lambda ms: spp * npx / ms / 1e3
+    print(f"\nCornell 512x512 x {spp} spp, Msamples/s: reference pathTracingKernel {rate(ref_ms):.1f} ({ref_ms:.2f} ms), "
+          f"tt_render_compat {rate(compat_ms):.1f} ({compat_ms:.2f} ms), native {rate(native_ms):.1f} ({native_ms:.2f} ms)")
+    assert compat_ms < 2.0 * ref_ms
