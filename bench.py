@@ -54,6 +54,7 @@ sys.path.insert(0, str(ROOT))
 N_CELLS = 1024
 SCALE = 8.0
 WIDTH = 2048
+SHADOW_LIGHT = [8.0 * SCALE, 2.0 * SCALE, 0.0]  # the point (8, 2, 0) of the unit terrain
 METRIC = "Mrays/s closest-hit; time to relMSE 0.01, cached vs plain tracer, 1 GB300"
 UNIT = "Mrays/s"
 L2_FLUSH_BYTES = 256 << 20
@@ -84,7 +85,9 @@ def workload(trace_ext=None, width: int = WIDTH):
     primary = scenes.pinhole_rays(width, width, cam["eye"], cam["target"], cam["tan_half_fov"])
     t, normal = trace_ext(bvh, primary)
     secondary, _ = scenes.secondary_rays(primary, t, normal, primary.shape[0], 11, 1e-4 * SCALE)
-    return mesh, bvh, primary, secondary
+    # shadow rays from first hits to the point (8, 2, 0) of the unit terrain, tmax = the distance
+    shadow = scenes.shadow_rays(primary, t, SHADOW_LIGHT, primary.shape[0], 5, 1e-4 * SCALE)
+    return mesh, bvh, primary, secondary, shadow
 
 
 class Clocks:
@@ -137,6 +140,25 @@ def bytes_per_ray(counters: np.ndarray) -> float:
     """Algorithmic bytes per ray from the oracle's (node, leaf, tri, hit-update) counts."""
     c = counters.astype(np.float64).mean(axis=0)
     return 32.0 + 8.0 + 64.0 * c[0] + 16.0 * c[1] + 48.0 * c[2] + 56.0 * c[3]
+
+
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo, else the architecture)."""
+    try:
+        out = subprocess.run(["lscpu"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.split(":")[0].strip() == "Model name":
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for line in Path("/proc/cpuinfo").read_text().splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.machine()
 
 
 def cpu_baseline(bvh_arrays: dict, rays: np.ndarray, stride: int, want_counters: bool, min_seconds: float = 0.0) -> dict:
@@ -200,7 +222,7 @@ def run_reference(args) -> None:
         o = oracle.intersect(bvh.arrays(), rays, True, arith=oracle.PLAIN, normals=True)
         return o["t"], o["normal"]
 
-    _, bvh, primary, secondary = workload(host_ext)
+    _, bvh, primary, secondary, _ = workload(host_ext)
     arr = bvh.arrays()
     rays = np.concatenate([primary, secondary])
     vals, secs = [], []
@@ -217,7 +239,7 @@ def run_reference(args) -> None:
             "data": "synthetic (seeded fBm terrain, seed 7)",
             "config": {"workload": "terrain ray-cast: 2,097,152 tris, 4M coherent + 4M incoherent closest-hit rays",
                        "sample_rays_per_step": r["rays"]},
-            "cpu_baseline": {"value": round(v, 3), "unit": UNIT, "cores": cores, "kind": "port",
+            "cpu_baseline": {"value": round(v, 3), "unit": UNIT, "cores": cores, "kind": "port", "cpu": cpu_model(),
                              "sample": f"all {r['rays']:,} rays of both sets per step, "
                                        f"{float(np.median(secs)):.2f} s per step"},
             "e2e": {"value": round(v, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -249,7 +271,7 @@ def run_ours(args) -> None:
         h = dh.cpu().numpy()
         return h[:, 2].copy().view(np.float32), h[:, 3:6].copy().view(np.float32)
 
-    mesh, bvh, primary, secondary = workload(gpu_ext, args.trace_width)
+    mesh, bvh, primary, secondary, shadow = workload(gpu_ext, args.trace_width)
     dbvh = state["dbvh"]
     sets = [torch.from_numpy(primary).to(dev), torch.from_numpy(secondary).to(dev)]
     hits = [torch.empty((s.shape[0], 2), dtype=torch.int32, device=dev) for s in sets]
@@ -289,6 +311,26 @@ def run_ours(args) -> None:
     clocks = clk.summary()
     ms = max_over_ranks(float(np.sum(step_ms)) / args.steps, world, dev)
     value = whole_job_rate(n_rays, ms, world)  # whole-job Mrays/s
+
+    # any hit on both sets and on the shadow rays (not part of the closest-hit value)
+    any_hit = {}
+    for name, rr in (("primary", sets[0]), ("incoherent", sets[1]), ("shadow", torch.from_numpy(shadow).to(dev))):
+        hh = torch.empty((rr.shape[0], 2), dtype=torch.int32, device=dev)
+        for _ in range(3):
+            dbvh.intersect(rr, hh, closest=False, stream=s)
+        ts = []
+        for _ in range(max(3, args.steps // 2)):
+            flush.fill_(1)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            dbvh.intersect(rr, hh, closest=False, stream=s)
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            ts.append(e0.elapsed_time(e1))
+        any_hit[f"{name}_mrays"] = round(rr.shape[0] / float(np.median(ts)) / 1e3, 1)
+        if name == "shadow":
+            any_hit["shadow_occluded_fraction"] = round(float((hh[:, 0] >= 0).float().mean().item()), 4)
+    dbvh.check(s)
 
     # end to end through the host-buffer entry point (pinned host memory)
     h_sets = [torch.from_numpy(primary).pin_memory(), torch.from_numpy(secondary).pin_memory()]
@@ -339,6 +381,7 @@ def run_ours(args) -> None:
                     "incoherent_mrays": round(sets[1].shape[0] / np.mean(launch_ms[1]) / 1e3, 1),
                     "primary_hit_fraction": round(float((ids_p >= 0).mean()), 4),
                     "incoherent_hit_fraction": round(hit_frac, 4)},
+        "any_hit": dict(any_hit, light=SHADOW_LIGHT),
         "e2e": {"value": round(e2e_val, 2), "unit": UNIT, "h2d_bytes_per_step": int(n_rays * 32),
                 "d2h_bytes_per_step": int(n_rays * 8)},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
@@ -349,6 +392,7 @@ def run_ours(args) -> None:
                      else "fallback 6.8 TB/s", "bytes_per_ray": round(bpr, 1),
                      "kernel": "tt_trace: ray ordering + trace_warp_kernel<closest> (avg per ray set)", "avg_launch_ms": round(float(kernel_ms), 4)},
         "cpu_baseline": {"value": round(cpu["mrays"], 3), "unit": UNIT, "cores": cpu["threads"], "kind": "port",
+                         "cpu": cpu_model(),
                          "sample": f"all {cpu['rays']:,} rays of both sets, {cpu['passes']} passes, "
                                    f"{cpu['seconds']:.1f} s"},
         "clocks": clocks,
@@ -510,6 +554,7 @@ def run_render(args) -> None:
         "e2e": {"value": round(paths / float(np.mean(e2e)) / 1e3, 2), "unit": "Msamples/s",
                 "h2d_bytes_per_step": 0, "d2h_bytes_per_step": int(npx * 4)},
         "cpu_baseline": {"value": round(cpu["paths_per_s"] / 1e6, 4), "unit": "Msamples/s", "cores": cpu["threads"],
+                         "cpu": cpu_model(),
                          "kind": "port", "sample": cpu["sample"] + f", {cpu['seconds']:.1f} s (same view)"},
         "clocks": clk.summary(),
         "gpu_launches": int(launches),

@@ -116,7 +116,10 @@ def terrain_full():
     prim = scenes.pinhole_rays(2048, 2048, cam["eye"], cam["target"], cam["tan_half_fov"])
     first = trace(case.dbvh, prim, True, ext=True)
     sec, _ = scenes.secondary_rays(prim, first["t"], first["normal"], prim.shape[0], 11, 8e-4)
-    case.sets = {"primary": prim, "incoherent": sec}
+    # shadow rays from first hits to the point (8, 2, 0) of the unit terrain (x 8), tmax = the
+    # distance: about 23 % of them are occluded
+    shadow = scenes.shadow_rays(prim, first["t"], [64.0, 16.0, 0.0], prim.shape[0], 5, 8e-4)
+    case.sets = {"primary": prim, "incoherent": sec, "shadow": shadow}
     return case
 
 
@@ -312,23 +315,25 @@ def test_corrupt_bvh_reports_error_not_hang(tmp_path, child1_empty, status):
 
 @pytest.mark.skipif(not refgpu.available(), reason="reference cubin / loader not built")
 def test_faster_than_reference_kernel(terrain_full, capsys):
-    """Closest-hit throughput on the terrain config against the reference's own kernel."""
+    """Closest- and any-hit throughput of every terrain ray set against the reference's own
+    kernel on the same GPU."""
     case = terrain_full
     out = {}
-    for name, rays in case.sets.items():
-        ref = refgpu.intersect(case.arrays, rays, True, reps=7)
-        d_rays = torch.from_numpy(rays).cuda()
-        d_hits = torch.empty((rays.shape[0], 2), dtype=torch.int32, device="cuda")
-        ts = []
-        for _ in range(7):
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record()
-            case.dbvh.intersect(d_rays, d_hits)
-            e1.record()
-            e1.synchronize()
-            ts.append(e0.elapsed_time(e1))
-        mine = float(np.median(ts))
-        out[name] = (rays.shape[0] / mine / 1e3, rays.shape[0] / ref["ms"] / 1e3)
-        assert mine < ref["ms"], f"{name}: {mine:.3f} ms vs reference {ref['ms']:.3f} ms"
+    for closest in (True, False):
+        for name, rays in case.sets.items():
+            ref = refgpu.intersect(case.arrays, rays, closest, reps=7)
+            d_rays = torch.from_numpy(rays).cuda()
+            d_hits = torch.empty((rays.shape[0], 2), dtype=torch.int32, device="cuda")
+            ts = []
+            for _ in range(7):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                case.dbvh.intersect(d_rays, d_hits, closest=closest)
+                e1.record()
+                e1.synchronize()
+                ts.append(e0.elapsed_time(e1))
+            mine = float(np.median(ts))
+            out[(name, "closest" if closest else "any")] = (rays.shape[0] / mine / 1e3, rays.shape[0] / ref["ms"] / 1e3)
+            assert mine < ref["ms"], f"{name} closest={closest}: {mine:.3f} ms vs reference {ref['ms']:.3f} ms"
     with capsys.disabled():
-        print("\nclosest-hit Mrays/s (ours, reference kernel):", {k: tuple(round(x) for x in v) for k, v in out.items()})
+        print("\nMrays/s (ours, reference kernel):", {f"{k[0]}/{k[1]}": tuple(round(x) for x in v) for k, v in out.items()})
