@@ -62,9 +62,12 @@ struct DeviceBVH {
     int num_sms = 0;
     int blocks_per_sm[NUM_VARIANTS] = {1, 1, 1, 1, 1, 1, 1, 1};
     int variant = VARIANT_SORTED;
-    // L2 access-policy window over the node array for the trace launches (0 bytes: none)
+    // L2 access-policy window over the node array for the trace launches (0 bytes: none), set up
+    // at the first trace launch (the persisting set-aside shrinks the L2 left to other work, so a
+    // BVH that is only rendered never asks for one)
     size_t l2_window_bytes = 0;
     float l2_hit_ratio = 0.0f;
+    bool l2_setup = false;
     float lo[3] = {-1.f, -1.f, -1.f}, hi[3] = {1.f, 1.f, 1.f};  // scene bounds (root boxes)
     // ray-ordering scratch per work-counter slot (caller stream, three pipeline streams)
     void *order[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -232,22 +235,6 @@ static tt_status upload(const CompactBVH &b, DeviceBVH &d) {
     }
     const size_t nb = 16ull * b.nodes.size(), vb = 16ull * b.vertices.size(), mb = 16ull * b.normals.size();
     const size_t tb = 4ull * b.tri_idx.size(), ab = 4ull * b.mat_idx.size();
-    {  // L2 set-aside for the node array (a limit of this process's context; it ends with it)
-        int max_persist = 0, max_window = 0;
-        if (cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, dev) == cudaSuccess &&
-            cudaDeviceGetAttribute(&max_window, cudaDevAttrMaxAccessPolicyWindowSize, dev) == cudaSuccess &&
-            max_persist > 0 && max_window > 0) {
-            size_t cur = 0;
-            cudaDeviceGetLimit(&cur, cudaLimitPersistingL2CacheSize);
-            const size_t want = std::min(nb, (size_t)max_persist);
-            if (want > cur && cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, want) == cudaSuccess)
-                cudaDeviceGetLimit(&cur, cudaLimitPersistingL2CacheSize);
-            d.l2_window_bytes = std::min(nb, (size_t)max_window);
-            d.l2_hit_ratio = cur >= d.l2_window_bytes ? 1.0f : (float)cur / (float)d.l2_window_bytes;
-            if (cur == 0) d.l2_window_bytes = 0;
-        }
-        cudaGetLastError();
-    }
     auto align = [](size_t x) { return (x + 255) & ~size_t(255); };
     d.bytes = align(nb) + align(vb) + align(mb) + align(tb) + align(ab);
     cudaError_t e = cudaMalloc(&d.base, d.bytes);
@@ -330,6 +317,26 @@ static cudaError_t launch_variant(const DeviceBVH &d, int variant, unsigned bloc
     return cudaLaunchKernelExC(&cfg, kernel_for<kClosest, kExt>(variant), args);
 }
 
+// The L2 set-aside for the node array (a limit of this process's own context, which ends with it)
+// and the window of the trace launches.
+static void setup_l2_window(DeviceBVH &d) {
+    d.l2_setup = true;
+    int max_persist = 0, max_window = 0;
+    if (cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, d.device) == cudaSuccess &&
+        cudaDeviceGetAttribute(&max_window, cudaDevAttrMaxAccessPolicyWindowSize, d.device) == cudaSuccess &&
+        max_persist > 0 && max_window > 0) {
+        const size_t nb = 16ull * d.num_nodes;
+        size_t cur = 0;
+        cudaDeviceGetLimit(&cur, cudaLimitPersistingL2CacheSize);
+        const size_t want = std::min(nb, (size_t)max_persist);
+        if (want > cur && cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, want) == cudaSuccess)
+            cudaDeviceGetLimit(&cur, cudaLimitPersistingL2CacheSize);
+        d.l2_window_bytes = cur ? std::min(nb, (size_t)max_window) : 0;
+        d.l2_hit_ratio = cur >= d.l2_window_bytes ? 1.0f : (float)cur / (float)d.l2_window_bytes;
+    }
+    cudaGetLastError();
+}
+
 // unordered = true traces a SORTED / SORTED_OCC variant's rays in their own order (its unsorted twin).
 static tt_status launch_trace(const DeviceBVH &d, const void *d_rays, int64_t n, void *d_hits, bool closest,
                               bool ext, cudaStream_t stream, int counter_slot = 0, bool unordered = false) {
@@ -338,6 +345,7 @@ static tt_status launch_trace(const DeviceBVH &d, const void *d_rays, int64_t n,
     if (!d_rays || !d_hits) return fail(TT_ERR_INVALID, "null ray or hit buffer");
     if ((reinterpret_cast<uintptr_t>(d_rays) & 15) || (reinterpret_cast<uintptr_t>(d_hits) & 7))
         return fail(TT_ERR_INVALID, "ray buffer must be 16-byte aligned and hit buffer 8-byte aligned");
+    if (!d.l2_setup) setup_l2_window(const_cast<DeviceBVH &>(d));
     TT_CUDA(cudaMemsetAsync(d.scratch + counter_slot, 0, 8, stream));
     TraceArgs a;
     a.bvh = d.view;
@@ -679,6 +687,7 @@ tt_status tt_trace_host_noalloc(const void *d_nodes, const void *d_vertices, con
     d.num_sms = nd.num_sms;
     d.variant = VARIANT_WARP_SH16;
     d.blocks_per_sm[VARIANT_WARP_SH16] = nd.blocks_per_sm;
+    d.l2_setup = true;  // no L2 window: the call changes no limit of the context
     cudaStream_t s = (cudaStream_t)stream;
     char *dr = reinterpret_cast<char *>(nd.scratch) + kNoAllocHeader;
     char *dh = dr + 32 * (size_t)kNoAllocMaxRays;
