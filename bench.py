@@ -64,6 +64,11 @@ L2_FLUSH_BYTES = 256 << 20
 # the ordering kernels before them add 140 MB (primary) and 187 MB (incoherent). bench.py cannot
 # run ncu itself.
 TRACE_DRAM_BYTES_PER_LAUNCH = 573_100_000
+# L2 of the same GB300 from one ncu capture of the incoherent trace launch: 95.84 sectors/ns were
+# 8.43 % of the sustained peak, i.e. 1,136.5 sectors/ns x 32 B; the launch's own L2 traffic was
+# that 8.4 % of it
+TRACE_L2_PEAK_GBS = 36_370.0
+TRACE_L2_TRAFFIC_PCT = 8.4
 
 
 def load_peaks() -> dict:
@@ -390,7 +395,12 @@ def run_ours(args) -> None:
                                        "workload (mean of the primary and incoherent launches)",
                      "peak_source": f"{peaks['source']} hbm_gbs (MEASURED_PEAKS.json)" if peaks["source"] == "measured"
                      else "fallback 6.8 TB/s", "bytes_per_ray": round(bpr, 1),
-                     "kernel": "tt_trace: ray ordering + trace_warp_kernel<closest> (avg per ray set)", "avg_launch_ms": round(float(kernel_ms), 4)},
+                     "kernel": "tt_trace: ray ordering + trace_warp_kernel<closest> (avg per ray set)", "avg_launch_ms": round(float(kernel_ms), 4),
+                     "l2": {"achieved": round(achieved, 1), "peak": TRACE_L2_PEAK_GBS, "unit": "GB/s",
+                            "frac": round(achieved / TRACE_L2_PEAK_GBS, 4),
+                            "l2_traffic_pct_of_peak": TRACE_L2_TRAFFIC_PCT,
+                            "peak_source": "ncu: lts__t_sectors.sum.per_second / lts__t_sectors.sum.pct_of_peak_"
+                                           "sustained_elapsed x 32 B, incoherent trace launch"}},
         "cpu_baseline": {"value": round(cpu["mrays"], 3), "unit": UNIT, "cores": cpu["threads"], "kind": "port",
                          "cpu": cpu_model(),
                          "sample": f"all {cpu['rays']:,} rays of both sets, {cpu['passes']} passes, "
