@@ -1,12 +1,13 @@
 // Ray ordering before traversal: a counting sort of the rays by a key of up to 21 bits. The key's
-// high 8 bits are the ray direction's cell in a 16 x 16 octahedral map of the sphere, the low bits
-// (13 for 4M rays, 2 fewer per quartering of the count, 6 at least) the origin's cell in a grid
-// over the scene bounds, in an order that halves the longest remaining cell side first (13 bits
-// on a 16 x 1.8 x 16 terrain: 6, 2 and 5 per axis). Rays that leave the same region in nearly
-// the same direction then share a warp, so their lanes fetch the same nodes and diverge less
-// (on 4M cosine-distributed terrain rays the direction cell is worth 11 % of traversal time over
-// the direction octant alone). Each ray's hit still goes to its own slot, and traversal has
-// per-ray semantics, so the results do not depend on the order.
+// high bits (13 for 4M rays, 2 fewer per quartering of the count, 6 at least) are the origin's
+// cell in a grid over the scene bounds, in an order that halves the longest remaining cell side
+// first (13 bits on a 16 x 1.8 x 16 terrain: 6, 2 and 5 per axis); its low 8 bits are the ray
+// direction's cell in a 16 x 16 octahedral map of the sphere. Rays that leave the same region in
+// nearly the same direction then share a warp, so their lanes fetch the same nodes and diverge
+// less (on 4M cosine-distributed terrain rays the direction cell is worth 11 % of traversal time
+// over the direction octant alone, and origin-major order 2.4 % over direction-major). Each ray's
+// hit still goes to its own slot, and traversal has per-ray semantics, so the results do not
+// depend on the order.
 //
 // Kernels, in stream order: (1) clear the key counts and probe every 16th warp of rays (a
 // warp is uniform when its 32 keys are equal); when more than half of the sampled warps are

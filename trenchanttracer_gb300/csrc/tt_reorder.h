@@ -11,9 +11,9 @@
 
 namespace tt {
 
-// direction cell (8: 16 x 16 octahedral grid) above the origin's cell (up to 13: Morton-like code
-// of a grid over the scene bounds whose bits go to the longest remaining cell side first; fewer
-// bits for fewer rays, about 2^(origin bits + 9) rays each)
+// the origin's cell (up to 13 bits: Morton-like code of a grid over the scene bounds whose bits go
+// to the longest remaining cell side first; fewer bits for fewer rays, about 2^(origin bits + 9)
+// rays each) above the direction's cell (8 bits: 16 x 16 octahedral grid)
 constexpr int kOrderDirBits = 8;
 constexpr int kOrderOriginBits = 13;
 constexpr int kOrderMinOriginBits = 6;
@@ -63,7 +63,7 @@ __host__ __device__ inline unsigned order_key(const float4 r0, const float4 r1, 
     const unsigned qy = (unsigned)fminf(fmaxf((r0.y - g.lo.y) * g.scale.y, 0.0f), g.qmax.y);
     const unsigned qz = (unsigned)fminf(fmaxf((r0.z - g.lo.z) * g.scale.z, 0.0f), g.qmax.z);
     const unsigned ocell = deposit(qx, g.mask[0]) | deposit(qy, g.mask[1]) | deposit(qz, g.mask[2]);
-    return (dcell << g.origin_bits) | ocell;
+    return (ocell << kOrderDirBits) | dcell;
 }
 
 // Origin bits of the key for n rays, and the grid they index (host).
