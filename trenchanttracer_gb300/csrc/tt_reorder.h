@@ -18,6 +18,7 @@ constexpr int kOrderDirBits = 8;
 constexpr int kOrderOriginBits = 13;
 constexpr int kOrderMinOriginBits = 6;
 constexpr int kOrderBits = kOrderDirBits + kOrderOriginBits;  // the largest key
+static_assert(kOrderDirBits % 2 == 0 && kOrderBits <= 21, "direction cells square; counts for 2^21 keys at most");
 // Fewer rays than this are traced in their own order: ordering them cannot pay for the scan of
 // the 2^21 key counts.
 constexpr int64_t kOrderMinRays = 1 << 15;
@@ -43,7 +44,7 @@ __host__ __device__ inline unsigned deposit(unsigned q, unsigned mask) {
 
 __host__ __device__ inline unsigned order_key(const float4 r0, const float4 r1, const OrderGrid &g) {
     // direction: octahedral map (x, z over |x| + |y| + |z|, the lower hemisphere folded out),
-    // 4 bits per map axis, interleaved; non-finite or zero directions go to cell 0
+    // kOrderDirBits / 2 bits per map axis, interleaved; non-finite or zero directions go to cell 0
     const float dx = r0.w, dy = r1.x, dz = r1.y;
     const float s = fabsf(dx) + fabsf(dy) + fabsf(dz);
     unsigned dcell = 0;
@@ -54,9 +55,11 @@ __host__ __device__ inline unsigned order_key(const float4 r0, const float4 r1, 
             v = (1.0f - fabsf(u)) * (v < 0.0f ? -1.0f : 1.0f);
             u = fu;
         }
-        const unsigned qu = (unsigned)fminf(fmaxf((u + 1.0f) * 8.0f, 0.0f), 15.0f);
-        const unsigned qv = (unsigned)fminf(fmaxf((v + 1.0f) * 8.0f, 0.0f), 15.0f);
-        dcell = deposit(qu, 0xAAu) | deposit(qv, 0x55u);
+        constexpr float kCells = (float)(1 << (kOrderDirBits / 2));  // per map axis
+        constexpr unsigned kMask = (1u << kOrderDirBits) - 1u;
+        const unsigned qu = (unsigned)fminf(fmaxf((u + 1.0f) * (0.5f * kCells), 0.0f), kCells - 1.0f);
+        const unsigned qv = (unsigned)fminf(fmaxf((v + 1.0f) * (0.5f * kCells), 0.0f), kCells - 1.0f);
+        dcell = deposit(qu, 0xAAAAAAAAu & kMask) | deposit(qv, 0x55555555u & kMask);
     }
     // origin (NaN coordinates clamp to cell 0: fmaxf returns the non-NaN operand)
     const unsigned qx = (unsigned)fminf(fmaxf((r0.x - g.lo.x) * g.scale.x, 0.0f), g.qmax.x);
