@@ -86,6 +86,31 @@ def test_tcgen05_inference_matches_mma_sync_and_oracle(n):
     assert np.median(np.abs(a - b) / np.abs(b)) < 1e-3
 
 
+def test_a_tensor_core_wait_that_runs_out_is_reported_and_the_context_stays_usable():
+    """With a one-cycle budget every wait of the tcgen05 inference kernel runs out at once: the
+    launch ends after its copies in flight have landed, tt_cache_check reports TT_ERR_TIMEOUT (once:
+    the word is cleared), and on the same context a cache with the normal budget then agrees with
+    the mma.sync kernel."""
+    from trenchanttracer_gb300 import TTError
+    w = nrc.init_weights(21)
+    rec_t = torch.from_numpy(_records(3000, 7)).cuda()
+    bad = Cache(LO, HI, batch=4096, mma_kind=0, wait_limit=1)
+    bad.set_weights(w)
+    bad.infer(rec_t)
+    torch.cuda.synchronize()
+    with pytest.raises(TTError, match="ran out"):
+        bad.check()
+    bad.check()  # reported once, then cleared
+    tc = Cache(LO, HI, batch=4096, mma_kind=0)
+    ms = Cache(LO, HI, batch=4096, mma_kind=1)
+    tc.set_weights(w)
+    ms.set_weights(w)
+    a = tc.infer(rec_t).cpu().numpy()
+    b = ms.infer(rec_t).cpu().numpy()
+    tc.check()
+    assert np.median(np.abs(a - b) / np.abs(b)) < 1e-3
+
+
 def test_gradient_matches_oracle():
     cache = Cache(LO, HI, batch=4096)
     w = nrc.init_weights(12)

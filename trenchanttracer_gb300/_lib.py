@@ -77,7 +77,8 @@ class CacheParams(C.Structure):
     _fields_ = [("lr", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float), ("eps", C.c_float),
                 ("ema", C.c_float), ("batch", C.c_int32), ("steps", C.c_int32), ("train_paths", C.c_int32),
                 ("spread_c", C.c_float), ("seed", C.c_uint32), ("use_ema", C.c_int32),
-                ("bbox_lo", C.c_float * 3), ("bbox_hi", C.c_float * 3), ("mma_kind", C.c_int32)]
+                ("bbox_lo", C.c_float * 3), ("bbox_hi", C.c_float * 3), ("mma_kind", C.c_int32),
+                ("wait_limit", C.c_int32)]
 
 
 class View(C.Structure):

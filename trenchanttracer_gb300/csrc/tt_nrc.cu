@@ -666,7 +666,7 @@ tt_status cache_infer_device(tt_cache *c, const float *rec, const int *n_dev, lo
     if (c->p.mma_kind == 0) {
         const Encoding e = encoding_of(c->p);
         return tc_infer(use_ema ? c->w_tc_ema : c->w_tc_train, rec, 0, n_dev, cap, e.lo, e.inv_ext, rgb,
-                        err ? err : c->err, c->num_sms, s);
+                        err ? err : c->err, c->num_sms, c->p.wait_limit, s);
     }
     MlpArgs a;
     std::memset(&a, 0, sizeof(a));
@@ -711,6 +711,7 @@ tt_status tt_cache_params_default(tt_cache_params *p) {
     p->seed = 1;
     p->use_ema = 1;
     p->mma_kind = 0;
+    p->wait_limit = 0;
     for (int i = 0; i < 3; i++) {
         p->bbox_lo[i] = -1.0f;
         p->bbox_hi[i] = 1.0f;
@@ -850,7 +851,7 @@ tt_status tt_cache_infer(tt_cache *c, const float *d_records, int64_t n, float *
             return fail(TT_ERR_INVALID, "cache: records must be 16-byte aligned");
         const Encoding e = encoding_of(c->p);
         return tc_infer(use_ema ? c->w_tc_ema : c->w_tc_train, d_records, n, nullptr, 0, e.lo, e.inv_ext, d_rgb,
-                        c->err, c->num_sms, (cudaStream_t)stream);
+                        c->err, c->num_sms, c->p.wait_limit, (cudaStream_t)stream);
     }
     MlpArgs a;
     std::memset(&a, 0, sizeof(a));

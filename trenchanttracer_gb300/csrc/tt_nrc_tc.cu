@@ -72,11 +72,11 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
-// bounded wait for the phase of the given parity
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+// bounded wait for the phase of the given parity (budget in clock cycles)
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, long long budget = kWaitCycles) {
     const long long t0 = clock64();
     while (!mbar_try_wait(bar, parity))
-        if (clock64() - t0 > kWaitCycles) return false;
+        if (clock64() - t0 > budget) return false;
     return true;
 }
 __device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
@@ -159,6 +159,7 @@ struct TcArgs {
     TcEncoding enc;
     float *rgb;
     unsigned *err;
+    long long wait_cycles;  // budget of the waits in the main path (the drain at exit keeps ~1 s)
 };
 
 __device__ __forceinline__ void group_sync(int group) {  // the 128 threads of one warpgroup
@@ -215,10 +216,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(TcArgs a) {
         bulk_load(R, a.rec + r0 * kRec, bytes, bar_rec);
         rec_issued[0]++;
     }
+    bool w_pending = false;  // tid 0: the weights copy was issued and not seen complete
     if (tid == 0) {
         mbar_expect_tx(bar_w, kTcWeightBytes);
         bulk_load(W, a.w, kTcWeightBytes, bar_w);
-        if (!mbar_wait(bar_w, 0)) *ok_w = 0;
+        if (!mbar_wait(bar_w, 0, a.wait_cycles)) {
+            *ok_w = 0;
+            w_pending = true;
+        }
     }
     tc_fence_before();
     __syncthreads();
@@ -232,7 +237,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(TcArgs a) {
         const int rows = (int)((n - r0) < kTcRows ? (n - r0) : kTcRows);
         float *Rb = R + buf * kTcRows * kRec;
         if (gt == 0) {
-            if (mbar_wait(bar_rec + buf, (uint32_t)(rec_done[buf] & 1))) rec_done[buf]++;
+            if (mbar_wait(bar_rec + buf, (uint32_t)(rec_done[buf] & 1), a.wait_cycles)) rec_done[buf]++;
             else *ok = 0;
         }
         group_sync(group);
@@ -264,7 +269,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(TcArgs a) {
                          idesc, s > 0 ? 1u : 0u);
                 umma_commit(bar_mma);
                 mma_issued++;
-                if (mbar_wait(bar_mma, (uint32_t)(mma_done & 1))) mma_done++;
+                if (mbar_wait(bar_mma, (uint32_t)(mma_done & 1), a.wait_cycles)) mma_done++;
                 else *ok = 0;
             }
             group_sync(group);
@@ -311,6 +316,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(TcArgs a) {
             while (rec_done[b] < rec_issued[b] && mbar_wait(bar_rec + b, (uint32_t)(rec_done[b] & 1))) rec_done[b]++;
         while (mma_done < mma_issued && mbar_wait(bar_mma, (uint32_t)(mma_done & 1))) mma_done++;
     }
+    if (tid == 0 && w_pending) mbar_wait(bar_w, 0);  // the weights copy, if its wait ran out
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -348,8 +354,9 @@ void tc_relayout(const float *w_f32, uint16_t *w_tc, cudaStream_t s) {
 
 tt_status tc_infer(const uint16_t *w_tc, const float *rec, long long n_host, const int *n_dev, long long cap,
                    const float lo[3], const float inv_ext[3], float *rgb, unsigned *err, int num_sms,
-                   cudaStream_t s) {
+                   long long wait_cycles, cudaStream_t s) {
     TcArgs a;
+    a.wait_cycles = wait_cycles > 0 ? wait_cycles : kWaitCycles;
     a.w = w_tc;
     a.rec = rec;
     a.n_host = n_host;
