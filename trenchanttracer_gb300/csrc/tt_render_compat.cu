@@ -207,8 +207,11 @@ __device__ __forceinline__ void refr_sample(curandState *rs, RRay &ray, const RH
         return;
     }
     const float k = __fmul_rn((float)(into ? 1 : -1), __fmaf_rn(ddn, nnt, __fsqrt_rn(cos2t)));
-    V3 tdir(__fmaf_rn(ray.d.x, nnt, -__fmul_rn(h.n.x, k)), __fmaf_rn(ray.d.y, nnt, -__fmul_rn(h.n.y, k)),
-            __fmaf_rn(ray.d.z, nnt, -__fmul_rn(h.n.z, k)));
+    // `tdir = d * nnt; tdir -= n * k;`: the compiled reference keeps d * nnt rounded and fuses n * k
+    // into the subtraction (the other fusion matches 96.8 % of the showcase's glass pixels, this one
+    // 99.2 %)
+    V3 tdir(__fmaf_rn(-h.n.x, k, __fmul_rn(ray.d.x, nnt)), __fmaf_rn(-h.n.y, k, __fmul_rn(ray.d.y, nnt)),
+            __fmaf_rn(-h.n.z, k, __fmul_rn(ray.d.z, nnt)));
     tdir = r_normalize(tdir);
     const float a = __fsub_rn(nt, nc);
     const float R0 = __fmul_rn(__fdiv_rn(__fmul_rn(a, a), __fadd_rn(nt, nc)), __fadd_rn(nt, nc));
