@@ -36,8 +36,6 @@ constexpr int kEncStride = kIn + kRowPad;  // bf16 per row of a warp's encoding 
 constexpr int kWeightBytes = kPadded * 2;
 constexpr int kFwdSmem = kWeightBytes + kWarps * 16 * kEncStride * 2;
 constexpr int kChunkRows = 128;            // rows per weight-gradient CTA (128 CTAs x 6 layers per 16K batch)
-constexpr int kSub = 32;                   // rows per staged weight-gradient tile
-constexpr int kSubStride = kSub + 8;
 
 __device__ __forceinline__ uint32_t pack2(float lo, float hi) {
     const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
@@ -333,56 +331,82 @@ struct WgradArgs {
     float *partial;  // [chunk][kParams]
 };
 
-// Partial dW_l = dZ_l^T H_l over this CTA's row chunk. kInW = in width, kOutW = out width.
+// Partial dW_l = dZ_l^T H_l over this CTA's chunk of kChunkRows rows. kInW = in width, kOutW =
+// out width. The chunk's rows of dZ_l and H_l are copied into shared memory as they are (16-byte
+// cp.async; rows padded by 16 bytes so that the eight row addresses of an ldmatrix fall in
+// different banks), and ldmatrix .trans turns them into the fragments of dZ^T (the A operand) and
+// of H read along its rows (the B operand): no transposing stores.
+constexpr int wg_out_cols(int out_w) { return out_w < 16 ? 16 : out_w; }  // A tiles are 16 rows high
+template <int kInW, int kOutW>
+constexpr int wgrad_smem_bytes() {
+    return kChunkRows * ((wg_out_cols(kOutW) + 8) + (kInW + 8)) * 2;
+}
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)),
+                 "l"(gmem)
+                 : "memory");
+}
+__device__ __forceinline__ void ldsm_x4_trans(uint32_t r[4], const void *smem_row) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"((uint32_t)__cvta_generic_to_shared(smem_row))
+                 : "memory");
+}
+
 template <int kInW, int kOutW>
 __device__ __forceinline__ void wgrad_layer(const WgradArgs &a, int l, long long n, uint16_t *sm) {
-    constexpr int kOutRows = kOutW < 16 ? 16 : kOutW;  // the A operand needs 16 rows per warp
-    uint16_t *dzt = sm;                                 // [kOutRows][kSubStride]
-    uint16_t *ht = sm + kOutRows * kSubStride;          // [kInW][kSubStride]
+    constexpr int kOutCols = wg_out_cols(kOutW);
+    constexpr int kZS = kOutCols + 8, kHS = kInW + 8;  // row strides (bf16) of the two tiles
+    uint16_t *dzs = sm;                                 // [kChunkRows][kZS]: dZ rows
+    uint16_t *hs = sm + kChunkRows * kZS;               // [kChunkRows][kHS]: H rows
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
     constexpr int kNT = kInW / 8;
+    static_assert(kNT % 2 == 0, "B fragments are loaded two n-tiles at a time");
+    const long long c0 = (long long)blockIdx.x * kChunkRows;
+    const long long c1 = c0 + kChunkRows < n ? c0 + kChunkRows : n;
+    const uint16_t *H = a.h[l];  // the pass's activations start at row 0 of the scratch
+    const uint16_t *DZ = a.dz[l];
+    // stage: 16-byte pieces of each row; rows past the chunk's end and the output layer's columns
+    // 8..15 are zero
+    constexpr int kZP = kOutW / 8, kHP = kInW / 8;  // 16-byte pieces per row
+    for (int i = threadIdx.x; i < kChunkRows * (kZP + kHP); i += blockDim.x) {
+        const int r = i / (kZP + kHP), q = i % (kZP + kHP);
+        const long long row = c0 + r;
+        uint16_t *dst = q < kZP ? dzs + r * kZS + 8 * q : hs + r * kHS + 8 * (q - kZP);
+        if (row < c1) {
+            const uint16_t *src = q < kZP ? DZ + row * kOutW + 8 * q : H + row * kInW + 8 * (q - kZP);
+            cp_async16(dst, src);
+        } else {
+            *reinterpret_cast<uint4 *>(dst) = make_uint4(0u, 0u, 0u, 0u);
+        }
+    }
+    if (kOutCols > kOutW)
+        for (int r = threadIdx.x; r < kChunkRows; r += blockDim.x)
+            *reinterpret_cast<uint4 *>(dzs + r * kZS + kOutW) = make_uint4(0u, 0u, 0u, 0u);
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    __syncthreads();
+    if (warp * 16 >= kOutCols) return;  // no output rows for this warp
     float acc[kNT][4];
 #pragma unroll
     for (int j = 0; j < kNT; j++) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
-    const long long c0 = (long long)blockIdx.x * kChunkRows;
-    const long long c1 = c0 + kChunkRows < n ? c0 + kChunkRows : n;
-    const bool active = warp * 16 < kOutW;
-    const uint16_t *H = a.h[l];  // the pass's activations start at row 0 of the scratch
-    const uint16_t *DZ = a.dz[l];
-    for (int i = threadIdx.x; i < kOutRows * kSubStride; i += blockDim.x) dzt[i] = 0;  // rows >= kOutW stay 0
-    for (long long s = c0; s < c1; s += kSub) {
-        __syncthreads();
-        // transposed staging: dzt[col][r] = dZ[s + r][col], ht[col][r] = H[s + r][col]
-        for (int i = threadIdx.x; i < kSub * kOutW; i += blockDim.x) {
-            const int r = i / kOutW, col = i % kOutW;
-            dzt[col * kSubStride + r] = s + r < c1 ? DZ[(s + r) * kOutW + col] : (uint16_t)0;
-        }
-        for (int i = threadIdx.x; i < kSub * kInW; i += blockDim.x) {
-            const int r = i / kInW, col = i % kInW;
-            ht[col * kSubStride + r] = s + r < c1 ? H[(s + r) * kInW + col] : (uint16_t)0;
-        }
-        __syncthreads();
-        if (active) {
+    const int m0 = 16 * warp, qm = lane >> 3, qi = lane & 7;
+#pragma unroll 2
+    for (int k0 = 0; k0 < kChunkRows; k0 += 16) {
+        // A = dZ^T (m = output, k = row): matrices (m0-7, k0-7), (m8-15, k0-7), (m0-7, k8-15), (m8-15, k8-15)
+        uint32_t af[4];
+        ldsm_x4_trans(af, dzs + (k0 + 8 * (qm >> 1) + qi) * kZS + m0 + 8 * (qm & 1));
 #pragma unroll
-            for (int kt = 0; kt < kSub / 16; kt++) {
-                const uint16_t *ar = dzt + (16 * warp + g) * kSubStride + 16 * kt + 2 * t;
-                uint32_t af[4];
-                af[0] = *reinterpret_cast<const uint32_t *>(ar);
-                af[1] = *reinterpret_cast<const uint32_t *>(ar + 8 * kSubStride);
-                af[2] = *reinterpret_cast<const uint32_t *>(ar + 8);
-                af[3] = *reinterpret_cast<const uint32_t *>(ar + 8 * kSubStride + 8);
-#pragma unroll
-                for (int j = 0; j < kNT; j++) {
-                    const uint16_t *br = ht + (8 * j + g) * kSubStride + 16 * kt + 2 * t;
-                    mma(acc[j], af, *reinterpret_cast<const uint32_t *>(br),
-                        *reinterpret_cast<const uint32_t *>(br + 8));
-                }
-            }
+        for (int j = 0; j < kNT; j += 2) {
+            // B = H (k = row, n = input): n-tiles j and j + 1, rows k0-7 and k8-15 of each
+            uint32_t bf[4];
+            ldsm_x4_trans(bf, hs + (k0 + 8 * (qm & 1) + qi) * kHS + 8 * j + 8 * (qm >> 1));
+            mma(acc[j], af, bf[0], bf[1]);
+            mma(acc[j + 1], af, bf[2], bf[3]);
         }
     }
-    if (!active) return;
     float *P = a.partial + (size_t)blockIdx.x * kParams + w_offset(l);
-    const int ra = 16 * warp + g, rb = ra + 8;
+    const int ra = m0 + g, rb = ra + 8;
 #pragma unroll
     for (int j = 0; j < kNT; j++) {
         const int col = 8 * j + 2 * t;
@@ -397,10 +421,12 @@ __device__ __forceinline__ void wgrad_layer(const WgradArgs &a, int l, long long
     }
 }
 
-constexpr int kWgradSmem = (64 * kSubStride + kIn * kSubStride) * 2;
+constexpr int kWgradSmem = wgrad_smem_bytes<kIn, kHidden>();  // the largest (layer 0)
+static_assert(wgrad_smem_bytes<kHidden, kHidden>() <= kWgradSmem &&
+                  wgrad_smem_bytes<kHidden, kOutPad>() <= kWgradSmem, "layer 0 needs the most");
 
 __global__ void __launch_bounds__(kThreads) k_mlp_wgrad(WgradArgs a) {
-    __shared__ __align__(16) uint16_t sm[kWgradSmem / 2];
+    extern __shared__ __align__(16) uint16_t sm[];
     long long n = a.n_host;
     if (a.n_dev) {
         n = (long long)*a.n_dev - a.off;
@@ -626,7 +652,7 @@ tt_status train_pass(tt_cache *c, const float *rec, const float *target, long lo
     w.off = n_dev ? off : 0;
     w.cap = cap;
     w.partial = c->partial;
-    k_mlp_wgrad<<<dim3(c->chunks, kLayers), kThreads, 0, s>>>(w);
+    k_mlp_wgrad<<<dim3(c->chunks, kLayers), kThreads, kWgradSmem, s>>>(w);
     AdamArgs ad;
     std::memset(&ad, 0, sizeof(ad));
     ad.partial = c->partial;
@@ -739,6 +765,8 @@ tt_status tt_cache_create(const tt_cache_params *p, tt_cache **out) {
         e = cudaFuncSetAttribute(k_mlp_forward<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kFwdSmem);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_mlp_backward, cudaFuncAttributeMaxDynamicSharedMemorySize, kWeightBytes);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_mlp_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, kWgradSmem);
     if (e != cudaSuccess) {
         delete c;
         return cuda_fail_c(e, "cache setup");
