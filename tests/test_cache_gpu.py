@@ -217,3 +217,29 @@ def test_trained_cache_beats_plain_tracing_at_equal_samples():
     e_cached = _relmse(cached.cpu().numpy().reshape(-1, 3) / spp, ref_img)
     e_plain = _relmse(plain.cpu().numpy().reshape(-1, 3) / spp, ref_img)
     assert np.isfinite(e_cached) and e_cached < e_plain, (e_cached, e_plain)
+
+
+def test_cached_renders_with_training_are_reproducible():
+    """Each training path owns a fixed record slot and the records reach the trainer in slot
+    order, so two runs of trained, cached frames with fresh caches of the same seed give the same
+    bits: images and weights (the queries' order does not matter: each path has at most one)."""
+    r, lo, hi = _scene()
+    cam = make_camera_meta(**CAM)
+    npx = 64 * 48 * 3
+    out = []
+    for _ in range(2):
+        cache = Cache(lo, hi, train_paths=1024, batch=256, steps=2, spread_c=0.01, seed=3)
+        acc = torch.zeros(npx, dtype=torch.float32, device="cuda")
+        for f in range(12):
+            r.render_cached(cache, cam, render_params(spp=2, sample_offset=2 * f, max_depth=10, rr_depth=4, seed=7),
+                            acc)
+        torch.cuda.synchronize()
+        r.check()
+        cache.check()
+        assert cache.steps > 0
+        out.append((acc.cpu().numpy(), cache.weights(0), cache.weights(1)))
+    (a0, w0, e0), (a1, w1, e1) = out
+    assert a0.max() > 0
+    assert np.array_equal(a0.view(np.uint32), a1.view(np.uint32))
+    assert np.array_equal(w0.view(np.uint32), w1.view(np.uint32))
+    assert np.array_equal(e0.view(np.uint32), e1.view(np.uint32))

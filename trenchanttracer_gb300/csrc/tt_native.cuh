@@ -76,12 +76,20 @@ struct CacheView {
     int *q_path;
     float *q_beta;            // 3 per query: throughput arriving at the query vertex
     float *q_rgb;             // 3 per query: the cache's radiance
-    float *t_rec;             // training records
+    float *t_rec;             // training records, compacted in slot order (k_cache_compact)
     int *t_path;
     float *t_L;               // 3 per record: the path's radiance up to the record vertex
     float *t_beta;            // 3 per record: throughput arriving at the record vertex
     float *t_target;          // 3 per record: measured radiance leaving the vertex
     int *counts;              // [0] queries, [1] training records
+    // Each training path of a wave owns slot (stream index + phase) / stride - train_slot0 of the
+    // slot arrays (path -1: no record), so the records' order does not depend on scheduling.
+    long long train_slot0;
+    int train_slots;
+    float *s_rec;
+    int *s_path;
+    float *s_L, *s_beta;
+    int *block_counts;        // filled slots per 1024-slot block
 };
 
 // Ordering of an extension queue (tt_reorder.cu): when order_built(state), k_extend reads the

@@ -358,12 +358,14 @@ __device__ __forceinline__ bool cache_vertex(const NativeArgs &a, int i, int dep
     if (!(PT_MUL(s_sum, s_sum) > PT_MUL(a.cache.spread_c, a.ps.a0[i]))) return false;
     if (flags & kFlagTrain) {
         flags |= kFlagRecorded;
-        const int s = append_active(a.cache.counts + 1);
-        if (s < a.cache.train_cap) {
-            cache_record(a.cache.t_rec + 16ll * s, p, wo, nl, m);
-            a.cache.t_path[s] = i;
-            st3(a.cache.t_L + 3ll * s, L);
-            st3(a.cache.t_beta + 3ll * s, beta);
+        const long long gid = a.view0.stream0 + a.wave_first + i;  // the path's stream index
+        const long long s = (gid + (long long)a.cache.train_phase) / (long long)a.cache.train_stride -
+                            a.cache.train_slot0;
+        if (s >= 0 && s < a.cache.train_slots) {
+            cache_record(a.cache.s_rec + 16ll * s, p, wo, nl, m);
+            a.cache.s_path[s] = i;
+            st3(a.cache.s_L + 3ll * s, L);
+            st3(a.cache.s_beta + 3ll * s, beta);
         }
         return false;
     }
@@ -372,6 +374,52 @@ __device__ __forceinline__ bool cache_vertex(const NativeArgs &a, int i, int dep
     a.cache.q_path[s] = i;
     st3(a.cache.q_beta + 3ll * s, beta);
     return true;
+}
+
+// Filled training slots per 1024-slot block.
+__global__ void __launch_bounds__(1024) k_cache_count(NativeArgs a) {
+    const int s = blockIdx.x * 1024 + threadIdx.x;
+    const int filled = __syncthreads_count(s < a.cache.train_slots && a.cache.s_path[s] >= 0);
+    if (threadIdx.x == 0) a.cache.block_counts[blockIdx.x] = filled;
+}
+
+// The filled training slots, in slot order, into the record arrays the targets and the training
+// read; counts[1] = their number.
+__global__ void __launch_bounds__(1024) k_cache_compact(NativeArgs a) {
+    __shared__ int s_base, s_warp[32];
+    const int s = blockIdx.x * 1024 + threadIdx.x, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (threadIdx.x == 0) {
+        int base = 0;
+        for (int b = 0; b < (int)blockIdx.x; b++) base += a.cache.block_counts[b];
+        s_base = base;
+    }
+    const int path = s < a.cache.train_slots ? a.cache.s_path[s] : -1;
+    const unsigned ballot = __ballot_sync(0xffffffffu, path >= 0);
+    if (lane == 0) s_warp[w] = __popc(ballot);
+    __syncthreads();
+    if (w == 0) {
+        int v = s_warp[lane], x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        s_warp[lane] = x - v;  // exclusive
+    }
+    __syncthreads();
+    const int dst = s_base + s_warp[w] + __popc(ballot & ((1u << lane) - 1u));
+    if (path >= 0) {
+        const float4 *src = reinterpret_cast<const float4 *>(a.cache.s_rec + 16ll * s);
+        float4 *out = reinterpret_cast<float4 *>(a.cache.t_rec + 16ll * dst);
+#pragma unroll
+        for (int k = 0; k < 4; k++) out[k] = src[k];
+        a.cache.t_path[dst] = path;
+        for (int c = 0; c < 3; c++) {
+            a.cache.t_L[3ll * dst + c] = a.cache.s_L[3ll * s + c];
+            a.cache.t_beta[3ll * dst + c] = a.cache.s_beta[3ll * s + c];
+        }
+    }
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 1023) a.cache.counts[1] = dst + (path >= 0 ? 1 : 0);
 }
 
 // Adds throughput x cache radiance of every query to its path.
@@ -419,6 +467,8 @@ __global__ void __launch_bounds__(kShadeBlockMax) k_raygen(NativeArgs a) {
             a.cache.counts[1] = 0;
         }
     }
+    if (a.cache.enabled)  // this wave's training slots start empty
+        for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < a.cache.train_slots; s += stride) a.cache.s_path[s] = -1;
     int cached = -1;
     ViewRec vw;
     V3 cam_pos, view, right, up;
@@ -1021,6 +1071,13 @@ static tt_status issue(NativeArgs a, long long total, const Launch &L, const Ord
             a.cache.train_stride = (unsigned)std::max<long long>(1, (a.wave_paths + tp - 1) / tp);
             a.cache.train_phase = (unsigned)((a.view0.stream0 / std::max(1, a.view0.npix) + done) * 7 %
                                              a.cache.train_stride);
+            // slots of the wave's training paths: stream indices g with (g + phase) % stride == 0
+            const long long st = (long long)a.cache.train_stride, ph = (long long)a.cache.train_phase;
+            const long long g0 = a.view0.stream0 + done, g1 = g0 + a.wave_paths - 1;
+            a.cache.train_slot0 = (g0 + ph + st - 1) / st;
+            a.cache.train_slots = (int)std::max<long long>(0, (g1 + ph) / st - a.cache.train_slot0 + 1);
+            if (a.cache.train_slots > a.cache.train_cap)
+                return fail(TT_ERR_INVALID, "cache: more training paths in a wave than training slots");
         }
         k_raygen<<<L.grid_shade, L.block, 0, s>>>(a);
         for (int b = 0; b < a.p.max_depth; b++) {
@@ -1049,7 +1106,14 @@ static tt_status issue(NativeArgs a, long long total, const Launch &L, const Ord
             if (st != TT_OK) return st;
             k_cache_resolve<<<L.grid_shade, L.block, 0, s>>>(a);
         }
-        if (cache && train) k_cache_targets<<<L.grid_shade, L.block, 0, s>>>(a);
+        if (cache && train) {
+            if (a.cache.train_slots > 0) {  // the records in slot order
+                const unsigned nb = (unsigned)((a.cache.train_slots + 1023) / 1024);
+                k_cache_count<<<nb, 1024, 0, s>>>(a);
+                k_cache_compact<<<nb, 1024, 0, s>>>(a);
+            }
+            k_cache_targets<<<L.grid_shade, L.block, 0, s>>>(a);
+        }
         if (accum) {
             if (f64) k_accumulate<double><<<L.grid_shade, L.block, 0, s>>>(a, (double *)accum);
             else k_accumulate<float><<<L.grid_shade, L.block, 0, s>>>(a, (float *)accum);
@@ -1067,7 +1131,8 @@ static tt_status issue(NativeArgs a, long long total, const Launch &L, const Ord
 static tt_status ensure_cache_buffers(tt_renderer *r, long long queries, long long records, CacheView &cv) {
     auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
     const size_t q = (size_t)queries, t = (size_t)records;
-    const size_t sizes[] = {64 * q, 4 * q, 12 * q, 12 * q, 64 * t, 4 * t, 12 * t, 12 * t, 12 * t, 256};
+    const size_t sizes[] = {64 * q, 4 * q, 12 * q, 12 * q, 64 * t, 4 * t, 12 * t, 12 * t, 12 * t, 256,
+                            64 * t, 4 * t, 12 * t, 12 * t, 4 * (t / 1024 + 1)};
     size_t total = 0;
     for (size_t s : sizes) total += al(s);
     if (r->cache_bytes < total || r->cache_queries < queries || r->cache_records < records) {
@@ -1097,6 +1162,11 @@ static tt_status ensure_cache_buffers(tt_renderer *r, long long queries, long lo
     cv.t_beta = (float *)take();
     cv.t_target = (float *)take();
     cv.counts = (int *)take();
+    cv.s_rec = (float *)take();
+    cv.s_path = (int *)take();
+    cv.s_L = (float *)take();
+    cv.s_beta = (float *)take();
+    cv.block_counts = (int *)take();
     cv.train_cap = (int)records;
     return TT_OK;
 }
