@@ -1,4 +1,5 @@
-"""Builds the reference's own code into oracle/_ref/ (git-ignored) for use as a checker.
+"""Builds the reference's own code into oracle/_ref/ (git-ignored), to check the oracle and the
+CUDA path against.
 
 Outputs:
   oracle/_ref/libttref_host.so   the reference's scene loader, SBVH builder, BVHCompact writer,

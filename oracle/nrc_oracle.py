@@ -1,7 +1,7 @@
 """CPU restatement of the learned radiance cache's network: encoding, forward pass, relative L2
 loss and its gradient, Adam.
 
-ORACLE — test infrastructure, used only by tests/ as the checker of the CUDA kernels
+ORACLE — test infrastructure, used only by tests/ to check the CUDA kernels
 (trenchanttracer_gb300/csrc/tt_nrc.cu). The reference has no learned component, so this is
 the project's own statement of the math, in FP64, with the same BF16 rounding points as the
 device code (weights, the encoding, every stored activation and pre-activation gradient):

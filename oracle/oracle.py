@@ -1,7 +1,7 @@
 """Build and ctypes access for the oracle's C restatement (oracle/tt_oracle.c).
 
 ORACLE — test infrastructure. Used only by tests/, __graft_entry__.smoke() and bench.py's CPU
-baseline leg, as the checker or the reported CPU baseline; the product never imports it.
+baseline leg, to check results or as the reported CPU baseline; the product never imports it.
 """
 from __future__ import annotations
 

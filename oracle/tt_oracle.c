@@ -4,7 +4,7 @@
  * A CPU restatement of the reference's ray traversal, intersect(ray, bvh, needClosestHit)
  * (include/geometry/IntersectKernel.cuh:78-296), over the compact BVH arrays read from a
  * bvh.cache (src/bvh/BVHCompact.cpp:319-375). Only tests/, __graft_entry__.smoke() and
- * bench.py's CPU-baseline leg use it, always as the checker or the reported CPU baseline.
+ * bench.py's CPU-baseline leg use it, always to check results or as the reported CPU baseline.
  *
  * Per ray it follows the reference's single-lane semantics: near-first order with the far
  * child pushed (:149-167), one postponed leaf, the warp vote reduced to this lane

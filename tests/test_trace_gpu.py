@@ -1,4 +1,4 @@
-"""Traversal kernels on the GPU, through the C ABI, against three checkers:
+"""Traversal kernels on the GPU, through the C ABI, checked three ways:
 
 1. the oracle's restatement in the reference kernel's arithmetic (small and medium cases);
 2. tests/golden/trace_gpu_golden.npz, outputs of the reference's own kernel on a GB300;
