@@ -200,10 +200,14 @@ __device__ __forceinline__ bool trav_node_step(TravState &s, Stack &stack, const
 template <bool kClosest, class Stack>
 __device__ __forceinline__ bool trav_leaf_phase(TravState &s, Stack &stack, const BvhView &bvh, uint32_t &err,
                                                 float tmax) {
+    bool stop = false;  // any hit: a triangle was accepted
     while (s.leaf < 0) {
         for (int tri = ~s.leaf;; tri += 3) {
             const float4 v0 = ldg4(bvh.verts + tri);
-            if (__float_as_int(v0.x) == (int)0x80000000) break;
+            // The any-hit stop is taken here, with the leaf terminator (the slot after an accepted
+            // triangle is another triangle or the terminator): a break at the acceptance itself
+            // made the any-hit build issue 10 % more warp instructions than the closest-hit one.
+            if (__float_as_int(v0.x) == (int)0x80000000 || (!kClosest && stop)) break;
             const float4 v1 = ldg4(bvh.verts + tri + 1);
             const float4 v2 = ldg4(bvh.verts + tri + 2);
             if (++s.iter > kMaxIterations) {
@@ -241,7 +245,7 @@ __device__ __forceinline__ bool trav_leaf_phase(TravState &s, Stack &stack, cons
                 s.v = v;
                 if (!kClosest) {
                     s.node = kEntrypointSentinel;
-                    break;
+                    stop = true;
                 }
             }
         }
