@@ -2,27 +2,31 @@
 // accumulator in tensor memory (TMEM), operands in shared memory, weights and feature records
 // brought in by bulk asynchronous copies (cp.async.bulk) that signal an mbarrier.
 //
-// One CTA per SM, three warpgroups of 128 threads sharing one copy of the network's weights
+// One CTA per SM, four warpgroups of 128 threads sharing one copy of the network's weights
 // (55.3 KB, loaded once per CTA). Each warpgroup owns its own stream of tiles of 128 rows (row r =
-// thread r of the group = TMEM lane r), its own A operand, its own 64 TMEM columns and two record
-// buffers, so three tiles are in flight per SM and a tile's records arrive while the previous tile
-// computes:
+// thread r of the group = TMEM lane r), its own 16 KB operand buffer, its own 64 TMEM columns and
+// two record buffers, so four tiles are in flight per SM and a tile's records arrive while the
+// previous tile computes:
 //   records  cp.async.bulk of the next tile's 128 x 64 B into the other record buffer
-//   encode   each thread builds its row's 160 BF16 inputs in the group's A buffer
+//   layer 0  the 160 encoded inputs go through the operand buffer as a ring of two 32-column
+//            slots: each thread encodes its row's 32 BF16 values of one slot, one thread issues
+//            that slot's two products (K = 16 each) and commits them to the slot's mbarrier, and
+//            the next slot is encoded while they run; a slot is refilled once its products have
+//            read it
 //   layers   one thread of the group issues the layer's tcgen05.mma (M = 128, N = 64 or 16, K = 16
 //            each) and a tcgen05.commit to the group's mbarrier; after the wait every warp of the
 //            group reads its 32 TMEM lanes (tcgen05.ld 32x32b), applies ReLU, rounds to BF16 and
-//            writes the next layer's A
+//            writes the next layer's A (the 64 hidden columns fill the whole buffer)
 //   output   exp of the first three columns of the last layer
-// A warpgroup synchronises on its own named barrier, so the three advance independently.
+// A warpgroup synchronises on its own named barrier, so the four advance independently.
 //
 // Operand layout: no swizzle, K-major, 8 x 16-byte core matrices. A (128 x K): core (m8, k8) at
 // byte (k8 * 16 + m8) * 128, so the stride between 8-row groups (SBO) is 128 and between the two
-// K halves of one instruction (LBO) 2048. Weights W_l (N x K): core (n8, k8) at (k8 * N/8 + n8) *
-// 128 from the layer's base: SBO 128, LBO N/8 * 128. Shared memory holds the three A buffers
-// first, then the weights, the records and the barriers, so that every operand address the
-// descriptors can form (with either of the two byte offsets applied along either dimension) lies
-// inside the CTA's own allocation.
+// K halves of one instruction (LBO) 2048; a ring slot holds k8 = 0..3 of its 32 columns. Weights
+// W_l (N x K): core (n8, k8) at (k8 * N/8 + n8) * 128 from the layer's base: SBO 128, LBO N/8 *
+// 128. Shared memory holds the four operand buffers first, then the weights, the records and
+// the barriers, so that every operand address the descriptors can form (with either of the two
+// byte offsets applied along either dimension) lies inside the CTA's own allocation.
 //
 // Every wait is bounded (a clock budget of about a second): one thread waits, the outcome goes
 // to all threads through shared memory and a block barrier, so a failure is uniform; it is
@@ -39,19 +43,26 @@ namespace tt {
 namespace nrc {
 
 constexpr int kTcRows = 128;
-constexpr int kTcGroups = 3;                         // warpgroups (tiles in flight) per CTA
+constexpr int kTcGroups = 4;                         // warpgroups (tiles in flight) per CTA
 constexpr int kTcThreads = 128 * kTcGroups;
-constexpr int kTmemCols = 256;                       // 64 per group, allocated as a power of two
-constexpr int kABytes = kTcRows * kIn * 2;           // 40960
+constexpr int kTmemCols = 256;                       // 64 per group
+constexpr int kFillCols = 32;                        // encoded columns per ring slot (two K = 16 steps)
+constexpr int kFills = kIn / kFillCols;              // 5 slot fills per tile
+constexpr int kSlotBytes = kTcRows * kFillCols * 2;  // 8192
+constexpr int kABytes = 2 * kSlotBytes;              // 16384: the ring, later the hidden activations
 constexpr int kRecBytes = kTcRows * kRec * 4;        // 8192
 constexpr long long kWaitCycles = 2000000000ll;      // ~1 s at 2 GHz
 constexpr unsigned kErrMlpWait = 8u;                 // error word bit: a tensor-core wait ran out
+static_assert(kIn % kFillCols == 0 && kFillCols % 8 == 0, "whole encoding chunks per slot");
+static_assert(kABytes == kTcRows * kHidden * 2, "the hidden activations fill the operand buffer");
 
 constexpr int kTcWeightBytes = kTcWeights * 2;        // 55296
-constexpr int kTcBarBytes = 128;  // weights barrier, per group 2 record + 1 product barriers, TMEM slot, flags
+// weights barrier; per group 2 record, 2 ring-slot and 1 product barriers; TMEM slot; flags
+constexpr int kTcBarBytes = 256;
 constexpr int kTcSmem = kTcGroups * (kABytes + 2 * kRecBytes) + kTcWeightBytes + kTcBarBytes;
 static_assert(kTcSmem <= 232448, "fits the 227 KB a CTA may use");
 static_assert(kTcWeightBytes % 16 == 0 && kABytes % 16 == 0 && kRecBytes % 16 == 0, "bulk copy sizes");
+static_assert(kTmemCols >= 64 * kTcGroups, "64 accumulator columns per group");
 
 
 // ---- PTX helpers ------------------------------------------------------------------------------
@@ -142,12 +153,31 @@ struct TcEncoding {
     float lo[3], inv_ext[3];
 };
 
-// the encoding of tt_nrc.cuh, one row, straight into the A operand: 20 chunks of 8 BF16 values,
-// each one 16-byte store (the 32 rows of a warp write 512 contiguous bytes per chunk)
-__device__ __forceinline__ void encode_row(const float *rec, const TcEncoding &e, __nv_bfloat16 *A, int r) {
-    const EncInputs in = enc_inputs(rec, e.lo, e.inv_ext);
+// Encoding values [32 f, 32 f + 32) of one row (tt_nrc.cuh) into ring slot S: four chunks of 8
+// BF16 values, each one 16-byte store (the 32 rows of a warp write 512 contiguous bytes per
+// chunk). f must be a compile-time constant after unrolling.
+__device__ __forceinline__ void encode_fill(const EncInputs &in, const float *rec, __nv_bfloat16 *S, int r, int f) {
 #pragma unroll
-    for (int c = 0; c < 20; c++) *reinterpret_cast<uint4 *>(A + a_offset(r, 8 * c)) = enc_chunk(in, rec, c);
+    for (int j = 0; j < kFillCols / 8; j++)
+        *reinterpret_cast<uint4 *>(S + a_offset(r, 8 * j)) = enc_chunk(in, rec, f * (kFillCols / 8) + j);
+}
+
+// ReLU of this thread's 64 accumulator columns, rounded to BF16, into its row of the next A.
+__device__ __forceinline__ void relu_to_operand(uint32_t lane_addr, __nv_bfloat16 *A, int r) {
+#pragma unroll
+    for (int c = 0; c < kHidden; c += 16) {
+        float v[16];
+        tmem_ld16(lane_addr + c, v);
+        tmem_wait_ld();
+        uint32_t w[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const __nv_bfloat162 b = __floats2bfloat162_rn(fmaxf(v[2 * j], 0.f), fmaxf(v[2 * j + 1], 0.f));
+            w[j] = *reinterpret_cast<const uint32_t *>(&b);
+        }
+        *reinterpret_cast<uint4 *>(A + a_offset(r, c)) = make_uint4(w[0], w[1], w[2], w[3]);
+        *reinterpret_cast<uint4 *>(A + a_offset(r, c + 8)) = make_uint4(w[4], w[5], w[6], w[7]);
+    }
 }
 
 struct TcArgs {
@@ -174,13 +204,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(TcArgs a) {
     float *R = reinterpret_cast<float *>(smem + kTcGroups * kABytes + kTcWeightBytes) +
                (size_t)group * 2 * kTcRows * kRec;  // this group's two record buffers
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kTcGroups * (kABytes + 2 * kRecBytes) + kTcWeightBytes);
-    uint64_t *bar_w = bars;                      // weights
-    uint64_t *bar_rec = bars + 1 + 3 * group;    // [0] [1]: the group's record buffers
-    uint64_t *bar_mma = bars + 3 + 3 * group;    // the group's products
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 1 + 3 * kTcGroups);
+    uint64_t *bar_w = bars;                        // weights
+    uint64_t *bar_rec = bars + 1 + 5 * group;      // [0] [1]: the group's record buffers
+    uint64_t *bar_ring = bar_rec + 2;              // [0] [1]: the products that read each ring slot
+    uint64_t *bar_mma = bar_rec + 4;               // the group's hidden and output layers
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 1 + 5 * kTcGroups);
     int *ok_w = reinterpret_cast<int *>(tmem_slot + 1);  // the weights arrived
     int *ok = ok_w + 1 + group;                          // this group's waits all ended
-    static_assert(8 * (1 + 3 * kTcGroups) + 4 + 4 * (1 + kTcGroups) <= kTcBarBytes, "barrier block");
+    static_assert(8 * (1 + 5 * kTcGroups) + 4 + 4 * (1 + kTcGroups) <= kTcBarBytes, "barrier block");
 
     long long n = a.n_host;
     if (a.n_dev) {
@@ -193,9 +224,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(TcArgs a) {
     if (tid == 0) {
         mbar_init(bar_w, 1);
         for (int g = 0; g < kTcGroups; g++) {
-            mbar_init(bars + 1 + 3 * g, 1);
-            mbar_init(bars + 2 + 3 * g, 1);
-            mbar_init(bars + 3 + 3 * g, 1);
+            for (int k = 0; k < 5; k++) mbar_init(bars + 1 + 5 * g + k, 1);
             ok_w[1 + g] = 1;
         }
         *ok_w = 1;
@@ -206,7 +235,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(TcArgs a) {
     // Asynchronous operations of this group, counted by its issuing thread (gt == 0): the k-th
     // completion of a barrier is awaited with parity k & 1, and whatever was issued and not yet
     // awaited is drained (bounded) before the block exits.
-    int rec_issued[2] = {0, 0}, rec_done[2] = {0, 0}, mma_issued = 0, mma_done = 0;
+    int rec_issued[2] = {0, 0}, rec_done[2] = {0, 0}, ring_issued[2] = {0, 0}, ring_done[2] = {0, 0};
+    int mma_issued = 0, mma_done = 0;
     const long long tstride = (long long)gridDim.x * kTcGroups;
     const long long first = (long long)blockIdx.x * kTcGroups + group;
     if (gt == 0 && first < ntiles) {  // the group's first records, while the weights come in
@@ -229,37 +259,90 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(TcArgs a) {
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot + (uint32_t)(group * 64);
-    if (!*ok_w && gt == 0) *ok = 0;
+    const uint32_t lane_addr = tmem + ((uint32_t)(warp_in_group * 32) << 16);
+    // *ok_w is not written after the block barrier above; *ok is read by the group only right after
+    // a group barrier that follows the issuing thread's write and precedes its next one
+    const bool weights_ok = *ok_w != 0;
+    if (!weights_ok && gt == 0) *ok = 0;
     group_sync(group);
     int buf = 0;
-    for (long long tile = first; *ok && tile < ntiles; tile += tstride) {
+    for (long long tile = first; weights_ok && tile < ntiles; tile += tstride) {
         const long long r0 = tile * kTcRows;
         const int rows = (int)((n - r0) < kTcRows ? (n - r0) : kTcRows);
-        float *Rb = R + buf * kTcRows * kRec;
+        const float *rec = R + buf * kTcRows * kRec + gt * kRec;
         if (gt == 0) {
             if (mbar_wait(bar_rec + buf, (uint32_t)(rec_done[buf] & 1), a.wait_cycles)) rec_done[buf]++;
             else *ok = 0;
         }
         group_sync(group);
         if (!*ok) break;
-        if (gt < rows) {
-            encode_row(Rb + gt * kRec, a.enc, A, gt);
-        } else {
-            for (int k = 0; k < kIn; k += 8)
-                *reinterpret_cast<uint4 *>(A + a_offset(gt, k)) = make_uint4(0u, 0u, 0u, 0u);
+        // layer 0 through the ring: encode a slot, issue its products, encode the other slot meanwhile
+        EncInputs in{};
+        if (gt < rows) in = enc_inputs(rec, a.enc.lo, a.enc.inv_ext);
+        bool failed = false;
+#pragma unroll
+        for (int f = 0; f < kFills; f++) {
+            const int slot = f & 1;
+            __nv_bfloat16 *S = A + slot * (kSlotBytes / 2);
+            if (f >= 2) {  // the slot's previous products have read it
+                if (gt == 0) {
+                    if (mbar_wait(bar_ring + slot, (uint32_t)(ring_done[slot] & 1), a.wait_cycles)) ring_done[slot]++;
+                    else *ok = 0;
+                }
+                group_sync(group);
+                if (!*ok) {
+                    failed = true;
+                    break;
+                }
+            }
+            if (gt < rows) {
+                encode_fill(in, rec, S, gt, f);
+            } else {
+                for (int k = 0; k < kFillCols; k += 8)
+                    *reinterpret_cast<uint4 *>(S + a_offset(gt, k)) = make_uint4(0u, 0u, 0u, 0u);
+            }
+            fence_async_smem();
+            tc_fence_before();
+            group_sync(group);  // the slot is encoded (after the last fill the records are free too)
+            tc_fence_after();
+            if (gt == 0) {
+                const uint32_t s0 = saddr(S), b0 = saddr(W + tc_offset(0));
+                constexpr int N = tc_out(0);
+                for (int k = 0; k < kFillCols / 16; k++) {
+                    const int ks = f * (kFillCols / 16) + k;  // K = 16 step of the layer
+                    umma(tmem, sdesc(s0 + k * 2 * 2048, 2048, 128), sdesc(b0 + ks * 2 * (N / 8) * 128, (N / 8) * 128, 128),
+                         idesc_bf16(kTcRows, N), ks > 0 ? 1u : 0u);
+                }
+                umma_commit(bar_ring + slot);
+                ring_issued[slot]++;
+            }
         }
+        if (failed) break;
+        if (gt == 0) {
+            if (tile + tstride < ntiles) {  // the next tile's records into the other buffer
+                const long long nr0 = (tile + tstride) * kTcRows;
+                const uint32_t bytes = (uint32_t)((n - nr0) < kTcRows ? (n - nr0) : kTcRows) * kRec * 4;
+                mbar_expect_tx(bar_rec + (buf ^ 1), bytes);
+                bulk_load(R + (buf ^ 1) * kTcRows * kRec, a.rec + nr0 * kRec, bytes, bar_rec + (buf ^ 1));
+                rec_issued[buf ^ 1]++;
+            }
+            // layer 0 is complete when the last fill of each slot is
+            for (int b = 0; b < 2; b++) {
+                if (ring_done[b] < ring_issued[b]) {
+                    if (mbar_wait(bar_ring + b, (uint32_t)(ring_done[b] & 1), a.wait_cycles)) ring_done[b]++;
+                    else *ok = 0;
+                }
+            }
+        }
+        group_sync(group);
+        tc_fence_after();
+        if (!*ok) break;
+        relu_to_operand(lane_addr, A, gt);  // the whole buffer: the ring is no longer read
         fence_async_smem();
         tc_fence_before();
-        group_sync(group);  // every row encoded: Rb is free again and A is ready
+        group_sync(group);
         tc_fence_after();
-        if (gt == 0 && tile + tstride < ntiles) {  // the next tile's records into the other buffer
-            const long long nr0 = (tile + tstride) * kTcRows;
-            const uint32_t bytes = (uint32_t)((n - nr0) < kTcRows ? (n - nr0) : kTcRows) * kRec * 4;
-            mbar_expect_tx(bar_rec + (buf ^ 1), bytes);
-            bulk_load(R + (buf ^ 1) * kTcRows * kRec, a.rec + nr0 * kRec, bytes, bar_rec + (buf ^ 1));
-            rec_issued[buf ^ 1]++;
-        }
-        for (int l = 0; l < kLayers; l++) {
+        for (int l = 1; l < kLayers; l++) {
             const int K = layer_in(l), N = tc_out(l);
             if (gt == 0) {
                 const uint32_t a0 = saddr(A), b0 = saddr(W + tc_offset(l));
@@ -275,22 +358,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(TcArgs a) {
             group_sync(group);
             tc_fence_after();
             if (!*ok) break;
-            const uint32_t lane_addr = tmem + ((uint32_t)(warp_in_group * 32) << 16);
             if (l < kLayers - 1) {
-#pragma unroll
-                for (int c = 0; c < kHidden; c += 16) {
-                    float v[16];
-                    tmem_ld16(lane_addr + c, v);
-                    tmem_wait_ld();
-                    uint32_t w[8];
-#pragma unroll
-                    for (int j = 0; j < 8; j++) {
-                        const __nv_bfloat162 b = __floats2bfloat162_rn(fmaxf(v[2 * j], 0.f), fmaxf(v[2 * j + 1], 0.f));
-                        w[j] = *reinterpret_cast<const uint32_t *>(&b);
-                    }
-                    *reinterpret_cast<uint4 *>(A + a_offset(gt, c)) = make_uint4(w[0], w[1], w[2], w[3]);
-                    *reinterpret_cast<uint4 *>(A + a_offset(gt, c + 8)) = make_uint4(w[4], w[5], w[6], w[7]);
-                }
+                relu_to_operand(lane_addr, A, gt);
                 fence_async_smem();
             } else {
                 float v[16];
@@ -312,8 +381,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(TcArgs a) {
     if (gt == 0) {
         if (!*ok) atomicOr(a.err, kErrMlpWait);
         // drain what this group issued and did not see complete (bounded again), before TMEM is freed
-        for (int b = 0; b < 2; b++)
+        for (int b = 0; b < 2; b++) {
             while (rec_done[b] < rec_issued[b] && mbar_wait(bar_rec + b, (uint32_t)(rec_done[b] & 1))) rec_done[b]++;
+            while (ring_done[b] < ring_issued[b] && mbar_wait(bar_ring + b, (uint32_t)(ring_done[b] & 1)))
+                ring_done[b]++;
+        }
         while (mma_done < mma_issued && mbar_wait(bar_mma, (uint32_t)(mma_done & 1))) mma_done++;
     }
     if (tid == 0 && w_pending) mbar_wait(bar_w, 0);  // the weights copy, if its wait ran out
@@ -370,7 +442,7 @@ tt_status tc_infer(const uint16_t *w_tc, const float *rec, long long n_host, con
     a.err = err;
     const long long rows = n_dev ? cap : n_host;
     const long long tiles = (rows + kTcRows - 1) / kTcRows;
-    const long long want = (tiles + kTcGroups - 1) / kTcGroups;  // blocks, each with three groups
+    const long long want = (tiles + kTcGroups - 1) / kTcGroups;  // blocks, each with kTcGroups groups
     const int grid = (int)(want < 1 ? 1 : (want < num_sms ? want : num_sms));
     k_mlp_forward_tc<<<grid, kTcThreads, kTcSmem, s>>>(a);
     const cudaError_t e = cudaGetLastError();
