@@ -43,14 +43,15 @@ namespace tt {
 namespace nrc {
 
 constexpr int kTcRows = 128;
-constexpr int kTcGroups = 4;                         // warpgroups (tiles in flight) per CTA
+constexpr int kTcGroups = 6;                         // warpgroups (tiles in flight) per CTA
 constexpr int kTcThreads = 128 * kTcGroups;
-constexpr int kTmemCols = 256;                       // 64 per group
+constexpr int kTmemCols = 512;                       // 64 per group, allocated as a power of two
 constexpr int kFillCols = 32;                        // encoded columns per ring slot (two K = 16 steps)
 constexpr int kFills = kIn / kFillCols;              // 5 slot fills per tile
 constexpr int kSlotBytes = kTcRows * kFillCols * 2;  // 8192
 constexpr int kABytes = 2 * kSlotBytes;              // 16384: the ring, later the hidden activations
 constexpr int kRecBytes = kTcRows * kRec * 4;        // 8192
+constexpr int kRecBufs = 1;                          // record buffers per group
 constexpr long long kWaitCycles = 2000000000ll;      // ~1 s at 2 GHz
 constexpr unsigned kErrMlpWait = 8u;                 // error word bit: a tensor-core wait ran out
 static_assert(kIn % kFillCols == 0 && kFillCols % 8 == 0, "whole encoding chunks per slot");
@@ -58,8 +59,8 @@ static_assert(kABytes == kTcRows * kHidden * 2, "the hidden activations fill the
 
 constexpr int kTcWeightBytes = kTcWeights * 2;        // 55296
 // weights barrier; per group 2 record, 2 ring-slot and 1 product barriers; TMEM slot; flags
-constexpr int kTcBarBytes = 256;
-constexpr int kTcSmem = kTcGroups * (kABytes + 2 * kRecBytes) + kTcWeightBytes + kTcBarBytes;
+constexpr int kTcBarBytes = 512;
+constexpr int kTcSmem = kTcGroups * (kABytes + kRecBufs * kRecBytes) + kTcWeightBytes + kTcBarBytes;
 static_assert(kTcSmem <= 232448, "fits the 227 KB a CTA may use");
 static_assert(kTcWeightBytes % 16 == 0 && kABytes % 16 == 0 && kRecBytes % 16 == 0, "bulk copy sizes");
 static_assert(kTmemCols >= 64 * kTcGroups, "64 accumulator columns per group");
@@ -202,8 +203,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(TcArgs a) {
     __nv_bfloat16 *A = reinterpret_cast<__nv_bfloat16 *>(smem + group * kABytes);
     uint16_t *W = reinterpret_cast<uint16_t *>(smem + kTcGroups * kABytes);
     float *R = reinterpret_cast<float *>(smem + kTcGroups * kABytes + kTcWeightBytes) +
-               (size_t)group * 2 * kTcRows * kRec;  // this group's two record buffers
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kTcGroups * (kABytes + 2 * kRecBytes) + kTcWeightBytes);
+               (size_t)group * kRecBufs * kTcRows * kRec;  // this group's record buffers
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kTcGroups * (kABytes + kRecBufs * kRecBytes) + kTcWeightBytes);
     uint64_t *bar_w = bars;                        // weights
     uint64_t *bar_rec = bars + 1 + 5 * group;      // [0] [1]: the group's record buffers
     uint64_t *bar_ring = bar_rec + 2;              // [0] [1]: the products that read each ring slot
@@ -319,12 +320,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(TcArgs a) {
         }
         if (failed) break;
         if (gt == 0) {
-            if (tile + tstride < ntiles) {  // the next tile's records into the other buffer
+            if (tile + tstride < ntiles) {  // the next tile's records (every encoding read is done)
+                const int nb = (buf + 1) % kRecBufs;
                 const long long nr0 = (tile + tstride) * kTcRows;
                 const uint32_t bytes = (uint32_t)((n - nr0) < kTcRows ? (n - nr0) : kTcRows) * kRec * 4;
-                mbar_expect_tx(bar_rec + (buf ^ 1), bytes);
-                bulk_load(R + (buf ^ 1) * kTcRows * kRec, a.rec + nr0 * kRec, bytes, bar_rec + (buf ^ 1));
-                rec_issued[buf ^ 1]++;
+                mbar_expect_tx(bar_rec + nb, bytes);
+                bulk_load(R + nb * kTcRows * kRec, a.rec + nr0 * kRec, bytes, bar_rec + nb);
+                rec_issued[nb]++;
             }
             // layer 0 is complete when the last fill of each slot is
             for (int b = 0; b < 2; b++) {
@@ -376,7 +378,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(TcArgs a) {
             group_sync(group);
             tc_fence_after();
         }
-        buf ^= 1;
+        buf = (buf + 1) % kRecBufs;
     }
     if (gt == 0) {
         if (!*ok) atomicOr(a.err, kErrMlpWait);
