@@ -59,11 +59,11 @@ METRIC = "Mrays/s closest-hit; time to relMSE 0.01, cached vs plain tracer, 1 GB
 UNIT = "Mrays/s"
 L2_FLUSH_BYTES = 256 << 20
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of the trace kernel of
-# this workload (the default, ray-ordered variant), the mean of the primary (292.0 MB) and
-# incoherent (327.0 MB) launches ncu captured of `bench.py --steps 2 --warmup 3` on a GB300; the
+# this workload (the default, ray-ordered variant), the mean of the primary (293.1 MB) and
+# incoherent (328.8 MB) launches ncu captured of `bench.py --steps 2 --warmup 3` on a GB300; the
 # ordering kernels around them add 8 MB (primary: the probe only) and 523 MB (incoherent: probe,
 # keys, scan, ordered copy, hit gather). bench.py cannot run ncu itself.
-TRACE_DRAM_BYTES_PER_LAUNCH = 309_500_000
+TRACE_DRAM_BYTES_PER_LAUNCH = 311_000_000
 # L2 of the same GB300 from one ncu capture of the incoherent trace launch: 95.84 sectors/ns were
 # 8.43 % of the sustained peak, i.e. 1,136.5 sectors/ns x 32 B; the launch's own L2 traffic was
 # that 8.4 % of it
