@@ -2,12 +2,13 @@
 // accumulator in tensor memory (TMEM), operands in shared memory, weights and feature records
 // brought in by bulk asynchronous copies (cp.async.bulk) that signal an mbarrier.
 //
-// One CTA per SM, four warpgroups of 128 threads sharing one copy of the network's weights
-// (55.3 KB, loaded once per CTA). Each warpgroup owns its own stream of tiles of 128 rows (row r =
-// thread r of the group = TMEM lane r), its own 16 KB operand buffer, its own 64 TMEM columns and
-// two record buffers, so four tiles are in flight per SM and a tile's records arrive while the
-// previous tile computes:
-//   records  cp.async.bulk of the next tile's 128 x 64 B into the other record buffer
+// One CTA per SM, six warpgroups of 128 threads (kTcGroups) sharing one copy of the network's
+// weights (55.3 KB, loaded once per CTA). Each warpgroup owns its own stream of tiles of 128 rows
+// (row r = thread r of the group = TMEM lane r), its own 16 KB operand buffer, its own 64 TMEM
+// columns and one record buffer (kRecBufs), so six tiles are in flight per SM and a tile's
+// records arrive while the previous tile's later layers compute:
+//   records  cp.async.bulk of the next tile's 128 x 64 B, issued once the current tile's records
+//            are encoded
 //   layer 0  the 160 encoded inputs go through the operand buffer as a ring of two 32-column
 //            slots: each thread encodes its row's 32 BF16 values of one slot, one thread issues
 //            that slot's two products (K = 16 each) and commits them to the slot's mbarrier, and
@@ -18,13 +19,13 @@
 //            group reads its 32 TMEM lanes (tcgen05.ld 32x32b), applies ReLU, rounds to BF16 and
 //            writes the next layer's A (the 64 hidden columns fill the whole buffer)
 //   output   exp of the first three columns of the last layer
-// A warpgroup synchronises on its own named barrier, so the four advance independently.
+// A warpgroup synchronises on its own named barrier, so the groups advance independently.
 //
 // Operand layout: no swizzle, K-major, 8 x 16-byte core matrices. A (128 x K): core (m8, k8) at
 // byte (k8 * 16 + m8) * 128, so the stride between 8-row groups (SBO) is 128 and between the two
 // K halves of one instruction (LBO) 2048; a ring slot holds k8 = 0..3 of its 32 columns. Weights
 // W_l (N x K): core (n8, k8) at (k8 * N/8 + n8) * 128 from the layer's base: SBO 128, LBO N/8 *
-// 128. Shared memory holds the four operand buffers first, then the weights, the records and
+// 128. Shared memory holds the groups' operand buffers first, then the weights, the records and
 // the barriers, so that every operand address the descriptors can form (with either of the two
 // byte offsets applied along either dimension) lies inside the CTA's own allocation.
 //
