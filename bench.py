@@ -141,6 +141,14 @@ class Clocks:
                 "samples": len(rows)}
 
 
+def trace_call_launches(dbvh) -> int:
+    """Kernels one DeviceBVH.intersect call launches: with the ray-ordered variants the ordering
+    probe, keys, scan and scatter, the trace and the hit gather (the ordering kernels return at
+    once when the probe finds the rays coherent, but they are still launched); otherwise the
+    trace alone."""
+    return 6 if dbvh.variant in (dbvh.VARIANT_SORTED, dbvh.VARIANT_SORTED_OCC) else 1
+
+
 def bytes_per_ray(counters: np.ndarray) -> float:
     """Algorithmic bytes per ray from the oracle's (node, leaf, tri, hit-update) counts."""
     c = counters.astype(np.float64).mean(axis=0)
@@ -406,7 +414,7 @@ def run_ours(args) -> None:
                          "sample": f"all {cpu['rays']:,} rays of both sets, {cpu['passes']} passes, "
                                    f"{cpu['seconds']:.1f} s"},
         "clocks": clocks,
-        "gpu_launches": 2 * args.steps,
+        "gpu_launches": 2 * args.steps * trace_call_launches(dbvh),
     }
     print(json.dumps(line), flush=True)
     if world > 1:

@@ -16,12 +16,14 @@
 //                         active at the vote depends on how the warp re-converges, so in float
 //                         corner cases (a leaf box whose entry rounds above a nearly equal hit
 //                         distance) the result can depend on the other rays of the warp.
-//   TT_VARIANT_SORTED     WARP_SH16 over the rays in the order of a counting sort by direction
-//                         cell and origin cell (tt_reorder.cu), or in their own order when a
+//   TT_VARIANT_SORTED     WARP_SH16 over the rays in the order of a counting sort by origin
+//                         cell and direction cell (tt_reorder.cu), or in their own order when a
 //                         sample finds them coherent; each hit still goes to its own ray's slot.
+//                         Compiled for 10 resident blocks per SM (48 registers, 8 bytes spilled;
+//                         without that bound it takes 61 registers and 8 blocks fit).
 //   TT_VARIANT_SH16_OCC,  WARP_SH16 and SORTED compiled for 12 resident blocks per SM (40
-//   TT_VARIANT_SORTED_OCC registers and a few spilled values instead of 54 registers), trading
-//                         spills for more warps to hide the node-fetch latency.
+//   TT_VARIANT_SORTED_OCC registers and a few spilled values), trading spills for more warps to
+//                         hide the node-fetch latency.
 // All but WARP_VOTE return the per-ray result of the reference's algorithm, bit for bit.
 #include <cuda_runtime.h>
 
