@@ -308,7 +308,7 @@ typedef struct tt_launch_shape {
     int32_t block;        /* threads per block: 64, 128 or 256 */
     int32_t stack_shared; /* traversal stack entries per thread kept in shared memory: 0, 8 or 16 */
     int32_t wave_paths;   /* paths in flight per wave (queue capacity): 1 .. 2^24 */
-    int32_t ordered;      /* 1: order each extension queue by direction and origin cell before
+    int32_t ordered;      /* 1: order each extension queue by origin and direction cell before
                              tracing it (coherent queues, e.g. camera rays, are left alone) */
     float ms;             /* tt_batch_autotune: the trial's time; otherwise 0 */
 } tt_launch_shape;

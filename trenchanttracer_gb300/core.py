@@ -297,7 +297,7 @@ class Renderer:
 
     def set_launch(self, block: int, stack_shared: int, wave_paths: int, ordered: int = 0) -> None:
         """Launch shape of the native kernels (include/tt.h, tt_launch_shape); ordered = 1 orders
-        each extension queue by direction and origin cell before tracing it."""
+        each extension queue by origin and direction cell before tracing it."""
         shape = _lib.LaunchShape(int(block), int(stack_shared), int(wave_paths), int(ordered), 0.0)
         check(lib().tt_renderer_set_launch(self._h, C.byref(shape)))
 

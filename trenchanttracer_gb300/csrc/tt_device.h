@@ -40,7 +40,7 @@ struct tt_renderer {
     int num_sms = 0;
     // launch shape of the native kernels (tt_renderer_set_launch, tt_batch_autotune)
     int launch_block = 128, launch_stack = 16, launch_wave = 1 << 22;
-    int launch_order = 0;  // order each extension queue by direction and origin cell before tracing
+    int launch_order = 0;  // order each extension queue by origin and direction cell before tracing
     float order_lo[3] = {-1.f, -1.f, -1.f}, order_hi[3] = {1.f, 1.f, 1.f};  // scene bounds
     size_t order_off = 0;       // byte offset of the ordering scratch inside `paths` (0: none)
     size_t order_state_at = 0;  // its state block, relative to the scratch
