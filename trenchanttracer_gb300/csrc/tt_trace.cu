@@ -625,33 +625,41 @@ tt_status tt_trace_host(const tt_dbvh *bvh, const tt_ray *h_rays, int64_t n, tt_
     // starts early and the later chunks are large enough for ordering to pay (measured on 4M
     // terrain rays: 2.04 ms against 2.32 ms for 1M chunks).
     const int64_t sched[4] = {n / 16, 3 * (n / 16), 6 * (n / 16), 0};
-    TT_CUDA(cudaEventRecord(d.pipe_start, s));
+    // The first failing call stops the issue, but every stream used is still drained before the
+    // return, so no copy of the caller's buffers is in flight once the call has returned.
     tt_status st = TT_OK;
+    auto cu = [&st](cudaError_t e, const char *what) {
+        if (e != cudaSuccess && st == TT_OK) st = cuda_fail(e, what);
+        return e == cudaSuccess;
+    };
     int used = 0;
-    for (int64_t off = 0, k = 0, m = 0; off < n && st == TT_OK; off += m, k++) {
-        if (n < (int64_t)(1 << 21)) m = n;
-        else if (coherent) m = (int64_t)(1 << 20);
-        else m = k < 3 ? sched[k] : n - off;
-        if (m > n - off) m = n - off;
-        const int p = (int)(k % 3);
-        cudaStream_t ps = d.pipe[p];
-        if (k < 3) {
-            TT_CUDA(cudaStreamWaitEvent(ps, d.pipe_start, 0));
-            used = (int)k + 1;
+    if (cu(cudaEventRecord(d.pipe_start, s), "cudaEventRecord(pipeline start)")) {
+        for (int64_t off = 0, k = 0, m = 0; off < n; off += m, k++) {
+            if (n < (int64_t)(1 << 21)) m = n;
+            else if (coherent) m = (int64_t)(1 << 20);
+            else m = k < 3 ? sched[k] : n - off;
+            if (m > n - off) m = n - off;
+            const int p = (int)(k % 3);
+            cudaStream_t ps = d.pipe[p];
+            if (k < 3) {
+                if (!cu(cudaStreamWaitEvent(ps, d.pipe_start, 0), "cudaStreamWaitEvent(pipeline start)")) break;
+                used = (int)k + 1;
+            }
+            if (!cu(cudaMemcpyAsync(dr + 32 * off, reinterpret_cast<const char *>(h_rays) + 32 * off, 32ull * m,
+                                    cudaMemcpyHostToDevice, ps),
+                    "cudaMemcpyAsync(rays to the device)"))
+                break;
+            st = launch_trace(d, dr + 32 * off, m, dh + 8 * off, closest != 0, false, ps, kScratchPipe + p,
+                              coherent && n >= (int64_t)(1 << 21));
+            if (st != TT_OK) break;
+            if (!cu(cudaMemcpyAsync(reinterpret_cast<char *>(h_hits) + 8 * off, dh + 8 * off, 8ull * m,
+                                    cudaMemcpyDeviceToHost, ps),
+                    "cudaMemcpyAsync(hits to the host)"))
+                break;
         }
-        TT_CUDA(cudaMemcpyAsync(dr + 32 * off, reinterpret_cast<const char *>(h_rays) + 32 * off, 32ull * m,
-                                cudaMemcpyHostToDevice, ps));
-        st = launch_trace(d, dr + 32 * off, m, dh + 8 * off, closest != 0, false, ps, kScratchPipe + p,
-                          coherent && n >= (int64_t)(1 << 21));
-        if (st == TT_OK)
-            TT_CUDA(cudaMemcpyAsync(reinterpret_cast<char *>(h_hits) + 8 * off, dh + 8 * off, 8ull * m,
-                                    cudaMemcpyDeviceToHost, ps));
     }
-    for (int p = 0; p < used; p++) {
-        TT_CUDA(cudaEventRecord(d.pipe_done[p], d.pipe[p]));
-        TT_CUDA(cudaStreamWaitEvent(s, d.pipe_done[p], 0));
-    }
-    TT_CUDA(cudaStreamSynchronize(s));
+    for (int p = 0; p < used; p++) cu(cudaStreamSynchronize(d.pipe[p]), "cudaStreamSynchronize(pipeline)");
+    cu(cudaStreamSynchronize(s), "cudaStreamSynchronize");
     if (st != TT_OK) return st;
     return read_error_word(d, s);
 }
@@ -699,11 +707,17 @@ tt_status tt_trace_host_noalloc(const void *d_nodes, const void *d_vertices, con
     // the header keeps the last call's contents: the error word must start at zero (the launch
     // itself zeroes the work counter)
     TT_CUDA(cudaMemsetAsync(nd.scratch + 8, 0, 8, s));
-    TT_CUDA(cudaMemcpyAsync(dr, h_rays, 32ull * n, cudaMemcpyHostToDevice, s));
-    st = launch_trace(d, dr, n, dh, closest != 0, false, s);
+    cudaError_t e = cudaMemcpyAsync(dr, h_rays, 32ull * n, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) st = cuda_fail(e, "cudaMemcpyAsync(rays to the device)");
+    if (st == TT_OK) st = launch_trace(d, dr, n, dh, closest != 0, false, s);
+    if (st == TT_OK) {
+        e = cudaMemcpyAsync(h_hits, dh, 8ull * n, cudaMemcpyDeviceToHost, s);
+        if (e != cudaSuccess) st = cuda_fail(e, "cudaMemcpyAsync(hits to the host)");
+    }
+    // drained on failure too: no copy of the caller's buffers stays in flight after the return
+    e = cudaStreamSynchronize(s);
     if (st != TT_OK) return st;
-    TT_CUDA(cudaMemcpyAsync(h_hits, dh, 8ull * n, cudaMemcpyDeviceToHost, s));
-    TT_CUDA(cudaStreamSynchronize(s));
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
     return read_error_word(d, s);
 }
 
