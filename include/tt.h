@@ -227,6 +227,14 @@ tt_status tt_trace_host(const tt_dbvh *bvh, const tt_ray *h_rays, int64_t n, tt_
  * if a traversal reached its iteration cap (a corrupt BVH), TT_OK otherwise. Rays that fail
  * this way are reported as misses. */
 tt_status tt_dbvh_check(const tt_dbvh *bvh, void *stream);
+/* The key the ordered variants (TT_VARIANT_SORTED, TT_VARIANT_SORTED_OCC) sort a ray set by,
+ * computed on the host; no counterpart in the reference. keys[i] holds ray i's origin cell above
+ * its 8-bit direction cell (a 16 x 16 octahedral map); the origin cell indexes a grid over the
+ * scene bounds lo..hi whose bits go to the longest remaining cell side first, 13 bits for 2^22
+ * rays or more and 2 fewer per quartering of n (6 at least). *key_bits receives the key width.
+ * A caller may sort its rays by these keys on the host to trace them coherently. */
+tt_status tt_ray_order_keys(const tt_ray *rays, int64_t n, const float lo[3], const float hi[3], uint32_t *keys,
+                            int32_t *key_bits);
 
 /* Allocation-free tracing with HOST ray and hit buffers. No counterpart in the reference: it is
  * an addition for callers that cannot allocate device memory, such as a host application whose

@@ -460,6 +460,19 @@ def render_params(**kw) -> _lib.RenderParams:
     return p
 
 
+def ray_order_keys(rays: np.ndarray, lo, hi) -> tuple[np.ndarray, int]:
+    """The key the ordered trace variants sort rays (n, 8) float32 by, and its width in bits
+    (include/tt.h, tt_ray_order_keys)."""
+    rays = np.ascontiguousarray(rays, dtype=np.float32)
+    assert rays.ndim == 2 and rays.shape[1] == 8
+    keys = np.empty(rays.shape[0], np.uint32)
+    lo_a = np.ascontiguousarray(lo, dtype=np.float32)
+    hi_a = np.ascontiguousarray(hi, dtype=np.float32)
+    bits = C.c_int32()
+    check(lib().tt_ray_order_keys(_ptr(rays), rays.shape[0], _ptr(lo_a), _ptr(hi_a), _ptr(keys), C.byref(bits)))
+    return keys, bits.value
+
+
 def hits_to_numpy(hits: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
     """(n, 2) int32 [id, t bits] -> (ids int32, t float32)."""
     h = np.ascontiguousarray(hits).view(np.int32).reshape(-1, 2)

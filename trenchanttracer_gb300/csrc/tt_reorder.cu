@@ -391,3 +391,17 @@ tt_status reorder_unpermute(const OrderOut &out, int64_t n, void *hits, size_t h
 }
 
 }  // namespace tt
+
+extern "C" tt_status tt_ray_order_keys(const tt_ray *rays, int64_t n, const float lo[3], const float hi[3],
+                                       uint32_t *keys, int32_t *key_bits) {
+    if (n < 0) return tt::fail(TT_ERR_INVALID, "tt_ray_order_keys: n < 0");
+    if (!lo || !hi || !key_bits || (n > 0 && (!rays || !keys)))
+        return tt::fail(TT_ERR_INVALID, "tt_ray_order_keys: null argument");
+    const int ob = tt::order_origin_bits(n);
+    *key_bits = tt::kOrderDirBits + ob;
+    const tt::OrderGrid g = tt::order_grid(lo, hi, ob);
+    const float *r = reinterpret_cast<const float *>(rays);
+    for (int64_t i = 0; i < n; i++, r += 8)
+        keys[i] = tt::order_key(make_float4(r[0], r[1], r[2], r[3]), make_float4(r[4], r[5], r[6], r[7]), g);
+    return TT_OK;
+}
