@@ -16,6 +16,8 @@
 #include <bvh/SAHHelper.h>
 #include <core/Camera.h>
 #include <core/Scene.h>
+#include <hdr/HDRImage.h>
+#include <loader/HDRLoader.h>
 #include <loader/SceneLoader.h>
 #include <util/Config.h>
 #include <util/WangHash.h>
@@ -118,6 +120,32 @@ int ref_intersect_host(const char *cache_path, const float *rays, long long n, i
         return 0;
     } catch (const std::exception &e) {
         fprintf(stderr, "ref_intersect_host: %s\n", e.what());
+        return -1;
+    }
+}
+
+// HDRLoader::load (src/loader/HDRLoader.cpp:5-62): the decoded picture as the reference keeps it,
+// rows in file order, 3 floats per texel (read back from the HDRImage's float4 array, which the
+// cudart stub holds in host memory). Returns -1 when the loader throws or the picture exceeds cap
+// floats.
+int ref_load_hdr(const char *path, int *w, int *h, float *rgb, long long cap) {
+    try {
+        HDRLoader loader;
+        HDRImage *img = loader.load(path);
+        const long long n = (long long)img->width * img->height;
+        *w = img->width;
+        *h = img->height;
+        if (3 * n > cap) {
+            delete img;
+            return -1;
+        }
+        const float *src = reinterpret_cast<const float *>(img->hdrEnv);
+        for (long long i = 0; i < n; i++)
+            for (int c = 0; c < 3; c++) rgb[3 * i + c] = src[4 * i + c];
+        delete img;
+        return 0;
+    } catch (const std::exception &e) {
+        fprintf(stderr, "ref_load_hdr: %s\n", e.what());
         return -1;
     }
 }

@@ -38,6 +38,8 @@ def _load():
         h.ref_camera_meta.argtypes = [C.c_char_p, C.c_float, C.c_void_p]
         h.ref_wang_hash.restype = C.c_uint
         h.ref_wang_hash.argtypes = [C.c_uint]
+        h.ref_load_hdr.restype = C.c_int
+        h.ref_load_hdr.argtypes = [C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_void_p, C.c_longlong]
         h.ref_intersect_host.restype = C.c_int
         h.ref_intersect_host.argtypes = [C.c_char_p, C.c_void_p, C.c_longlong, C.c_int, C.c_void_p, C.c_void_p,
                                          C.c_void_p, C.c_void_p, C.c_int]
@@ -85,3 +87,12 @@ def intersect(cache: str, rays: np.ndarray, closest: bool, threads: int = 0) -> 
     if rc != 0:
         raise RuntimeError("reference intersect failed")
     return out
+
+
+def load_hdr(path: str, max_texels: int = 1 << 22) -> np.ndarray:
+    """The reference's HDRLoader on an RGBE file: (height, width, 3) float32."""
+    buf = np.zeros(3 * max_texels, np.float32)
+    w, h = C.c_int(0), C.c_int(0)
+    if _load().ref_load_hdr(os.fsencode(path), C.byref(w), C.byref(h), buf.ctypes.data, buf.size) != 0:
+        raise RuntimeError(f"reference HDRLoader failed on {path}")
+    return buf[:3 * w.value * h.value].reshape(h.value, w.value, 3).copy()

@@ -598,107 +598,124 @@ static tt_status load_obj(const std::string &file, const M4 &xf, Scene &sc) {
 }
 
 // ---- RGBE .hdr ------------------------------------------------------------------------------
-static bool old_decrunch(unsigned char (*scan)[4], int len, FILE *f) {
-    int rshift = 0;
-    while (len > 0) {
-        for (int c = 0; c < 4; c++) scan[0][c] = (unsigned char)fgetc(f);
-        if (feof(f)) return false;
-        if (scan[0][0] == 1 && scan[0][1] == 1 && scan[0][2] == 1) {
-            for (int i = scan[0][3] << rshift; i > 0 && len > 0; i--) {
-                memcpy(scan[0], scan[-1], 4);
-                scan++;
-                len--;
+// A Radiance picture (src/loader/HDRLoader.cpp reads the same files): "#?RADIANCE", header lines
+// up to an empty line, a "-Y <height> +X <width>" line, then `height` scanlines of `width` RGBE
+// pixels (8-bit mantissas sharing an exponent biased by 128). A scanline is stored in one of two
+// codings:
+//   flat            4-byte R,G,B,E pixels. A pixel (1, 1, 1, n) stands for n copies of the pixel
+//                   before it; each repeat pixel that directly follows another multiplies its
+//                   count by 256 (the older run-length form of the format).
+//   adaptive RLE    widths 8..32767 only: the bytes 2, 2, width >> 8, width & 255, then the R, G, B
+//                   and E components one after another, each as packets: a count byte c > 128 is
+//                   followed by one byte repeated c - 128 times, any other c by c literal bytes.
+// The decoder works on the file's bytes in memory. A scanline that runs past the end of the data
+// ends the picture; it and the rows after it stay zero.
+namespace {
+
+struct ByteCursor {
+    const unsigned char *p, *end;
+    bool overrun = false;
+    size_t left() const { return (size_t)(end - p); }
+    // the next byte, or 0 (recorded as an overrun) past the end
+    unsigned char take() {
+        if (p < end) return *p++;
+        overrun = true;
+        return 0;
+    }
+};
+
+enum class ScanlineCoding { Flat, AdaptiveRle };
+
+ScanlineCoding scanline_coding(const ByteCursor &in, long width) {
+    if (width < 8 || width > 0x7fff || in.left() < 4) return ScanlineCoding::Flat;
+    // a flat scanline cannot start with these bytes unless its first pixel has a 2,2 red/green
+    // mantissa pair and a blue mantissa below 128, which the format reserves for the RLE marker
+    return (in.p[0] == 2 && in.p[1] == 2 && (in.p[2] & 0x80) == 0) ? ScanlineCoding::AdaptiveRle
+                                                                  : ScanlineCoding::Flat;
+}
+
+// One scanline into `px` (width x 4 bytes). Returns false when the data ends inside it.
+bool decode_scanline(ByteCursor &in, long width, unsigned char *px) {
+    if (scanline_coding(in, width) == ScanlineCoding::AdaptiveRle) {
+        in.p += 4;  // 2, 2 and the width, which the pixel count already gives
+        for (int comp = 0; comp < 4; comp++) {
+            long x = 0;
+            while (x < width) {
+                if (!in.left()) return false;
+                const int count = in.take();
+                if (count > 128) {
+                    const unsigned char value = in.take();
+                    for (int k = count - 128; k > 0 && x < width; k--) px[4 * x++ + comp] = value;
+                } else {
+                    for (int k = count; k > 0 && x < width; k--) px[4 * x++ + comp] = in.take();
+                }
             }
-            rshift += 8;
+        }
+        return !in.overrun;
+    }
+    unsigned char prev[4] = {0, 0, 0, 0};  // the pixel a repeat at the start of a scanline copies
+    int shift = 0;
+    long x = 0;
+    while (x < width) {
+        if (in.left() < 4) return false;
+        const unsigned char *q = in.p;
+        in.p += 4;
+        if (q[0] == 1 && q[1] == 1 && q[2] == 1) {
+            long repeat = shift < 32 ? (long)q[3] << shift : (q[3] ? width : 0);
+            for (; repeat > 0 && x < width; repeat--, x++) memcpy(px + 4 * x, prev, 4);
+            shift += 8;
         } else {
-            scan++;
-            len--;
-            rshift = 0;
+            memcpy(px + 4 * x, q, 4);
+            memcpy(prev, q, 4);
+            x++;
+            shift = 0;
         }
     }
     return true;
 }
 
-static bool decrunch(unsigned char (*scan)[4], int len, FILE *f) {
-    if (len < 8 || len > 0x7fff) return old_decrunch(scan, len, f);
-    int i = fgetc(f);
-    if (i != 2) {
-        fseek(f, -1, SEEK_CUR);
-        return old_decrunch(scan, len, f);
-    }
-    scan[0][1] = (unsigned char)fgetc(f);
-    scan[0][2] = (unsigned char)fgetc(f);
-    i = fgetc(f);
-    if (scan[0][1] != 2 || (scan[0][2] & 128)) {
-        scan[0][0] = 2;
-        scan[0][3] = (unsigned char)i;
-        return old_decrunch(scan + 1, len - 1, f);
-    }
-    for (int c = 0; c < 4; c++) {
-        for (int j = 0; j < len;) {
-            int code = fgetc(f);
-            if (code == EOF) return false;
-            if (code > 128) {
-                code &= 127;
-                int val = fgetc(f);
-                while (code-- && j < len) scan[j++][c] = (unsigned char)val;
-            } else {
-                while (code-- && j < len) scan[j++][c] = (unsigned char)fgetc(f);
-            }
-        }
-    }
-    return feof(f) == 0;
-}
+}  // namespace
 
 tt_status load_hdr(const std::string &path, int32_t &w_out, int32_t &h_out, std::vector<float> &rgb) {
-    FILE *f = fopen(path.c_str(), "rb");
-    if (!f) return fail(TT_ERR_IO, "HDR environment map not found: " + path);
-    char magic[10];
-    if (fread(magic, 10, 1, f) != 1 || memcmp(magic, "#?RADIANCE", 10) != 0) {
+    std::vector<unsigned char> bytes;
+    {
+        FILE *f = fopen(path.c_str(), "rb");
+        if (!f) return fail(TT_ERR_IO, "HDR environment map not found: " + path);
+        unsigned char chunk[1 << 16];
+        size_t got;
+        while ((got = fread(chunk, 1, sizeof(chunk), f)) > 0) bytes.insert(bytes.end(), chunk, chunk + got);
         fclose(f);
+    }
+    ByteCursor in{bytes.data(), bytes.data() + bytes.size()};
+    if (in.left() < 11 || memcmp(in.p, "#?RADIANCE", 10) != 0)
         return fail(TT_ERR_FORMAT, path + ": not a RADIANCE file");
-    }
-    fseek(f, 1, SEEK_CUR);
+    in.p += 11;  // the magic and the byte after it
     // header lines end at an empty line
-    int c = 0, oldc = 0, guard = 0;
-    while (true) {
-        oldc = c;
-        c = fgetc(f);
-        if (c == EOF || ++guard > 65536) {
-            fclose(f);
-            return fail(TT_ERR_FORMAT, path + ": header not terminated");
-        }
-        if (c == '\n' && oldc == '\n') break;
+    for (unsigned char prev = 0;;) {
+        if (!in.left()) return fail(TT_ERR_FORMAT, path + ": header not terminated");
+        const unsigned char c = in.take();
+        if (c == '\n' && prev == '\n') break;
+        prev = c;
     }
-    char reso[256];
-    int n = 0;
-    while (n < 255) {
-        c = fgetc(f);
-        if (c == EOF) break;
-        reso[n++] = (char)c;
+    std::string reso;
+    while (in.left() && reso.size() < 255) {
+        const char c = (char)in.take();
+        reso.push_back(c);
         if (c == '\n') break;
     }
-    reso[n] = 0;
     long w = 0, h = 0;
-    if (sscanf(reso, "-Y %ld +X %ld", &h, &w) != 2 || w <= 0 || h <= 0 || w * h > (1L << 28)) {
-        fclose(f);
+    if (sscanf(reso.c_str(), "-Y %ld +X %ld", &h, &w) != 2 || w <= 0 || h <= 0 || w * h > (1L << 28))
         return fail(TT_ERR_FORMAT, path + ": bad resolution line");
-    }
     rgb.assign((size_t)w * h * 3, 0.0f);
-    std::vector<unsigned char> line((size_t)(w + 1) * 4, 0);
-    unsigned char (*scan)[4] = reinterpret_cast<unsigned char (*)[4]>(line.data() + 4);
+    std::vector<unsigned char> px((size_t)w * 4);
     for (long y = 0; y < h; y++) {
-        if (!decrunch(scan, (int)w, f)) break;
+        if (!decode_scanline(in, w, px.data())) break;
         float *dst = rgb.data() + (size_t)y * w * 3;
         for (long x = 0; x < w; x++) {
-            int e = (int)scan[x][3] - 128;
-            float d = ldexpf(1.0f, e);
-            dst[3 * x + 0] = (scan[x][0] / 256.0f) * d;
-            dst[3 * x + 1] = (scan[x][1] / 256.0f) * d;
-            dst[3 * x + 2] = (scan[x][2] / 256.0f) * d;
+            const float scale = ldexpf(1.0f, (int)px[4 * x + 3] - 128);
+            for (int c = 0; c < 3; c++) dst[3 * x + c] = (px[4 * x + c] / 256.0f) * scale;
         }
     }
-    fclose(f);
     w_out = (int32_t)w;
     h_out = (int32_t)h;
     return TT_OK;
