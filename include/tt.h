@@ -280,6 +280,43 @@ tt_status tt_render_compat(tt_renderer *renderer, const tt_camera_meta *cam, con
 /* Synchronises `stream` and reports traversal errors of the renderer's launches. */
 tt_status tt_renderer_check(tt_renderer *renderer, void *stream);
 
+/* One material interaction of the reference's path loop (src/core/RenderKernel.cu:64-91): the
+ * ray that hit, the Hit record renderKernel built (raw interpolated normal and distance, then
+ * n / nl from normalize() and point from hitPoint(), include/geometry/IntersectKernel.cuh:62-76),
+ * the throughput mask and the curand XORWOW state (48 bytes) going in; the next ray, mask and
+ * state coming out of the material's sampler (include/material/{Diff,Metal,Spec,Refr,Coat}Impl.cuh);
+ * u0 is the first uniform the incoming state yields. `kind` is the reference's MaterialType
+ * (0 DIFF, 1 METAL, 2 SPEC, 3 REFR, 4 COAT), `material` the index into the scene's materials.
+ * 256 bytes. */
+typedef struct tt_compat_interaction {
+    int32_t kind, thread, material, seq;
+    float o[3], d[3], tmin, tmax;
+    float normal[3], distance;
+    float n[3], nl[3], point[3];
+    float mask[3];
+    uint32_t rng[12];
+    float out_o[3], out_d[3], out_mask[3];
+    uint32_t out_rng[12];
+    float u0;
+    int32_t pad[2];
+} tt_compat_interaction;
+/* Diagnostic (no counterpart in the reference): re-runs recorded interactions through
+ * tt_render_compat's own per-hit arithmetic. For each of the n device records of d_in, d_out gets
+ * a copy whose n / nl / point are recomputed by this renderer from (o, d, normal, distance), and
+ * whose out_* fields and u0 come from this renderer's sampler of `kind` run on the record's
+ * incoming ray, hit (n, nl, point as recorded), mask and curand state. Two more kinds:
+ *   5  an environment lookup at a path's miss (hdrSample, include/hdr/HDRKernel.cuh:6-42):
+ *      out_mask gets the radiance this renderer looks up for direction d;
+ *   6  a sample's primary ray (src/core/RenderKernel.cu:131-197) for the pixel that thread
+ *      `thread` of tt_render_compat's launch over `cam` renders: out_o / out_d / tmin / tmax get
+ *      the ray, out_rng the curand state after its draws; the state going in is `rng`, or, with
+ *      seq < 0, the one the frame seeds for that thread (WangHash(frame) + thread).
+ * Lets a caller holding interactions recorded inside the reference's own kernel compare one
+ * bounce at a time instead of whole frames. Launch only. */
+tt_status tt_compat_replay(const tt_renderer *renderer, const tt_camera_meta *cam, const tt_render_meta *meta,
+                           const tt_compat_interaction *d_in, int64_t n, tt_compat_interaction *d_out,
+                           void *stream);
+
 /* Parameters of the native path tracer (no counterpart in the reference, which always runs 10
  * bounces with curand streams). */
 typedef struct tt_render_params {

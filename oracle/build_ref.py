@@ -173,6 +173,11 @@ def build(ref: Path = DEFAULT_REF, quiet: bool = True) -> bool:
         _run([str(cuda / "bin" / "nvcc"), "-cubin", "-gencode=arch=compute_103a,code=sm_103a", "-w",
               "-I" + str(tmp / "gpu"), "-I" + str(ref / "include"), "-I" + str(ref / "lib" / "include"),
               "-I" + str(ref), str(HERE / "ref" / "ref_render_harness.cu"), "-o", str(OUT / "ref_render.cubin")])
+        # the same kernel with every material interaction recorded (ref_render_probe.cu)
+        _run([str(cuda / "bin" / "nvcc"), "-cubin", "-gencode=arch=compute_103a,code=sm_103a", "-w",
+              "-I" + str(tmp / "gpu"), "-I" + str(ref / "include"), "-I" + str(ref / "lib" / "include"),
+              "-I" + str(ref), str(HERE / "ref" / "ref_render_probe.cu"), "-o",
+              str(OUT / "ref_render_probe.cubin")])
     if not quiet:
         print(f"built {OUT}/libttref_host.so and ref_intersect.cubin", file=sys.stderr)
     return True

@@ -147,12 +147,19 @@ done:
 // given as flat arrays (see ref_render_harness.cu for geo_data / mat_data). accum (W*H*3 floats)
 // is the accumulation buffer: read as the kernel's starting contents, written with its result.
 // The kernel launches with the reference's own shape (16x16 blocks, grid (W/16, H/16)).
-int ref_gpu_render(const char *cubin_path, const void *nodes, uint32_t n_nodes, const void *verts, uint32_t n_verts,
-                   const void *norms, const int32_t *tri_idx, const uint32_t *mat_idx, const float *geo_data,
-                   const int32_t *geo_mat, int ngeo, const float *mat_data, int nmat, const float *env_rgb, int env_w,
-                   int env_h, const float *cam13, int width, int height, int frame, unsigned hashed, int samples,
-                   float pi, float two_pi, float *accum, float *ms_out) {
+// With probe_records non-null the cubin is the probe build (ref_render_probe.cu): every material
+// interaction is recorded (256 bytes each); the first ones (all of them when they fit in
+// probe_capacity, else probe_capacity - 1) are copied to probe_records, and *probe_count receives
+// how many the frame made.
+static int render_impl(const char *cubin_path, const void *nodes, uint32_t n_nodes, const void *verts, uint32_t n_verts,
+                       const void *norms, const int32_t *tri_idx, const uint32_t *mat_idx, const float *geo_data,
+                       const int32_t *geo_mat, int ngeo, const float *mat_data, int nmat, const float *env_rgb,
+                       int env_w, int env_h, const float *cam13, int width, int height, int frame, unsigned hashed,
+                       int samples, float pi, float two_pi, float *accum, float *ms_out, void *probe_records,
+                       uint64_t probe_capacity, uint64_t *probe_count) {
     int rc = -1;
+    void *d_probe = nullptr;
+    unsigned long long *d_probe_n = nullptr;
     CUmodule mod = nullptr;
     CUfunction f_sizes = nullptr, f_scene = nullptr, f_meta = nullptr, f_pt = nullptr;
     void *d_nodes = nullptr, *d_verts = nullptr, *d_norms = nullptr, *d_tri = nullptr, *d_mat = nullptr;
@@ -248,6 +255,14 @@ int ref_gpu_render(const char *cubin_path, const void *nodes, uint32_t n_nodes, 
         CK(cudaMalloc(&d_out, 12 * npx));
         CK(cudaMemcpy(d_accum, accum, 12 * npx, cudaMemcpyHostToDevice));
         void *pargs[] = {&d_out, &d_accum, &p_hdr, &p_rm, &p_cm, &p_bvh, &p_geo, &p_matc};
+        if (probe_records) {
+            CUfunction f_setup = nullptr;
+            CKD(cuModuleGetFunction(&f_setup, mod, "ref_probe_setup"));
+            CK(cudaMalloc(&d_probe, 256ull * (probe_capacity ? probe_capacity : 1)));
+            unsigned long long cap = probe_capacity ? probe_capacity : 1;
+            void *qargs[] = {&d_probe, &cap};
+            CKD(cuLaunchKernel(f_setup, 1, 1, 1, 1, 1, 1, 0, nullptr, qargs, nullptr));
+        }
         CK(cudaEventCreate(&ev[0]));
         CK(cudaEventCreate(&ev[1]));
         CK(cudaEventRecord(ev[0], 0));
@@ -259,8 +274,23 @@ int ref_gpu_render(const char *cubin_path, const void *nodes, uint32_t n_nodes, 
     }
     CK(cudaGetLastError());
     CK(cudaMemcpy(accum, d_accum, 12 * npx, cudaMemcpyDeviceToHost));
+    if (probe_records) {
+        CUfunction f_count = nullptr;
+        unsigned long long made = 0;
+        CKD(cuModuleGetFunction(&f_count, mod, "ref_probe_count"));
+        CK(cudaMalloc(&d_probe_n, sizeof(made)));
+        void *cargs[] = {&d_probe_n};
+        CKD(cuLaunchKernel(f_count, 1, 1, 1, 1, 1, 1, 0, nullptr, cargs, nullptr));
+        CK(cudaMemcpy(&made, d_probe_n, sizeof(made), cudaMemcpyDeviceToHost));
+        *probe_count = made;
+        // past the capacity the last slot took every further record: keep the slots before it
+        const uint64_t kept = made <= probe_capacity ? made : (probe_capacity ? probe_capacity - 1 : 0);
+        if (kept) CK(cudaMemcpy(probe_records, d_probe, 256ull * kept, cudaMemcpyDeviceToHost));
+    }
     rc = 0;
 done:
+    if (d_probe) cudaFree(d_probe);
+    if (d_probe_n) cudaFree(d_probe_n);
     delete[] env4;
     for (auto &t : tex)
         if (t) cudaDestroyTextureObject(t);
@@ -271,6 +301,31 @@ done:
         if (p) cudaFree(p);
     if (mod) cuModuleUnload(mod);
     return rc;
+}
+
+int ref_gpu_render(const char *cubin_path, const void *nodes, uint32_t n_nodes, const void *verts, uint32_t n_verts,
+                   const void *norms, const int32_t *tri_idx, const uint32_t *mat_idx, const float *geo_data,
+                   const int32_t *geo_mat, int ngeo, const float *mat_data, int nmat, const float *env_rgb, int env_w,
+                   int env_h, const float *cam13, int width, int height, int frame, unsigned hashed, int samples,
+                   float pi, float two_pi, float *accum, float *ms_out) {
+    return render_impl(cubin_path, nodes, n_nodes, verts, n_verts, norms, tri_idx, mat_idx, geo_data, geo_mat, ngeo,
+                       mat_data, nmat, env_rgb, env_w, env_h, cam13, width, height, frame, hashed, samples, pi, two_pi,
+                       accum, ms_out, nullptr, 0, nullptr);
+}
+
+int ref_gpu_render_probe(const char *cubin_path, const void *nodes, uint32_t n_nodes, const void *verts,
+                         uint32_t n_verts, const void *norms, const int32_t *tri_idx, const uint32_t *mat_idx,
+                         const float *geo_data, const int32_t *geo_mat, int ngeo, const float *mat_data, int nmat,
+                         const float *env_rgb, int env_w, int env_h, const float *cam13, int width, int height,
+                         int frame, unsigned hashed, int samples, float pi, float two_pi, float *accum,
+                         void *probe_records, uint64_t probe_capacity, uint64_t *probe_count) {
+    if (!probe_records || !probe_count) {
+        g_err = "probe buffers required";
+        return -1;
+    }
+    return render_impl(cubin_path, nodes, n_nodes, verts, n_verts, norms, tri_idx, mat_idx, geo_data, geo_mat, ngeo,
+                       mat_data, nmat, env_rgb, env_w, env_h, cam13, width, height, frame, hashed, samples, pi, two_pi,
+                       accum, nullptr, probe_records, probe_capacity, probe_count);
 }
 
 }  // extern "C"

@@ -60,19 +60,8 @@ def render_available() -> bool:
     return RENDER_CUBIN.exists() and LIB.exists()
 
 
-def render(bvh_arrays: dict, materials: list, geometries: list, env: np.ndarray | None, cam, meta,
-           accum: np.ndarray) -> tuple[np.ndarray, float]:
-    """One frame of the reference's own pathTracingKernel. materials / geometries: the
-    tt_material / tt_geometry records of the scene; cam / meta: CameraMeta / RenderMeta;
-    accum: (W*H*3,) float32 starting contents. Returns (accumulation buffer, kernel ms)."""
-    h = _load()
-    if not hasattr(h, "_render_ready"):
-        h.ref_gpu_render.restype = C.c_int
-        h.ref_gpu_render.argtypes = [C.c_char_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p,
-                                     C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int,
-                                     C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_uint,
-                                     C.c_int, C.c_float, C.c_float, C.c_void_p, C.c_void_p]
-        h._render_ready = True
+def _render_args(bvh_arrays: dict, materials: list, geometries: list, env: np.ndarray | None, cam) -> tuple:
+    """The scene as the flat arrays ref_gpu_render takes (kept alive by the returned tuple)."""
     a = {k: np.ascontiguousarray(bvh_arrays[k]) for k in ["nodes", "vertices", "normals", "tri_indices",
                                                          "mat_indices"]}
     geo = np.zeros((max(1, len(geometries)), 16), np.float32)
@@ -97,17 +86,70 @@ def render(bvh_arrays: dict, materials: list, geometries: list, env: np.ndarray 
         eh, ew = env_a.shape[0], env_a.shape[1]
     cam13 = np.array(list(cam.position) + list(cam.view) + list(cam.up) + list(cam.fov) + [cam.aperture, cam.focal],
                      np.float32)
+    keep = (a, geo, geo_mat, mat, env_a, cam13)
+    args = (a["nodes"].ctypes.data, a["nodes"].shape[0], a["vertices"].ctypes.data, a["vertices"].shape[0],
+            a["normals"].ctypes.data, a["tri_indices"].ctypes.data, a["mat_indices"].ctypes.data, geo.ctypes.data,
+            geo_mat.ctypes.data, len(geometries), mat.ctypes.data, len(materials), env_a.ctypes.data, ew, eh,
+            cam13.ctypes.data, cam.width, cam.height)
+    return keep, args
+
+
+_SCENE_ARGTYPES = [C.c_char_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p,
+                   C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p,
+                   C.c_int, C.c_int, C.c_int, C.c_uint, C.c_int, C.c_float, C.c_float, C.c_void_p]
+
+
+def render(bvh_arrays: dict, materials: list, geometries: list, env: np.ndarray | None, cam, meta,
+           accum: np.ndarray) -> tuple[np.ndarray, float]:
+    """One frame of the reference's own pathTracingKernel. materials / geometries: the
+    tt_material / tt_geometry records of the scene; cam / meta: CameraMeta / RenderMeta;
+    accum: (W*H*3,) float32 starting contents. Returns (accumulation buffer, kernel ms)."""
+    h = _load()
+    if not hasattr(h, "_render_ready"):
+        h.ref_gpu_render.restype = C.c_int
+        h.ref_gpu_render.argtypes = _SCENE_ARGTYPES + [C.c_void_p]
+        h._render_ready = True
+    keep, args = _render_args(bvh_arrays, materials, geometries, env, cam)
     out = np.ascontiguousarray(accum, dtype=np.float32).copy()
     ms = C.c_float(0.0)
-    rc = h.ref_gpu_render(str(RENDER_CUBIN).encode(), a["nodes"].ctypes.data, a["nodes"].shape[0],
-                          a["vertices"].ctypes.data, a["vertices"].shape[0], a["normals"].ctypes.data,
-                          a["tri_indices"].ctypes.data, a["mat_indices"].ctypes.data, geo.ctypes.data,
-                          geo_mat.ctypes.data, len(geometries), mat.ctypes.data, len(materials), env_a.ctypes.data,
-                          ew, eh, cam13.ctypes.data, cam.width, cam.height, meta.frame_number, meta.hashed_frame,
-                          meta.samples, meta.pi, meta.two_pi, out.ctypes.data, C.byref(ms))
+    rc = h.ref_gpu_render(str(RENDER_CUBIN).encode(), *args, meta.frame_number, meta.hashed_frame, meta.samples,
+                          meta.pi, meta.two_pi, out.ctypes.data, C.byref(ms))
+    del keep
     if rc != 0:
         raise RuntimeError("reference GPU render failed: " + h.ref_gpu_error().decode())
     return out, float(ms.value)
+
+
+PROBE_CUBIN = HERE / "_ref" / "ref_render_probe.cubin"
+
+
+def probe_available() -> bool:
+    return PROBE_CUBIN.exists() and LIB.exists()
+
+
+def render_probe(bvh_arrays: dict, materials: list, geometries: list, env: np.ndarray | None, cam, meta,
+                 accum: np.ndarray, capacity: int) -> tuple[np.ndarray, np.ndarray, int]:
+    """One frame of the reference's pathTracingKernel built with recording samplers
+    (ref_render_probe.cu): every material interaction is recorded (field 0 of a record is the
+    reference's MaterialType: DIFF, METAL, SPEC, REFR, COAT). Returns (accumulation buffer, the
+    first records as a (m, 64) uint32 array, m <= capacity, the number of interactions the frame
+    made)."""
+    h = _load()
+    if not hasattr(h, "_probe_ready"):
+        h.ref_gpu_render_probe.restype = C.c_int
+        h.ref_gpu_render_probe.argtypes = _SCENE_ARGTYPES + [C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64)]
+        h._probe_ready = True
+    keep, args = _render_args(bvh_arrays, materials, geometries, env, cam)
+    out = np.ascontiguousarray(accum, dtype=np.float32).copy()
+    recs = np.zeros((max(1, capacity), 64), np.uint32)
+    made = C.c_uint64(0)
+    rc = h.ref_gpu_render_probe(str(PROBE_CUBIN).encode(), *args, meta.frame_number, meta.hashed_frame, meta.samples,
+                                meta.pi, meta.two_pi, out.ctypes.data, recs.ctypes.data, capacity, C.byref(made))
+    del keep
+    if rc != 0:
+        raise RuntimeError("reference GPU probe render failed: " + h.ref_gpu_error().decode())
+    kept = made.value if made.value <= capacity else capacity - 1
+    return out, recs[:kept], int(made.value)
 
 
 def intersect(bvh_arrays: dict, rays: np.ndarray, closest: bool, reps: int = 1) -> dict:

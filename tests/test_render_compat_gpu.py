@@ -33,7 +33,7 @@ def _render_both(scene: Scene, cam, samples: int, frame: int = 1, leaf_max: int 
     return mine, ref
 
 
-def _compare(mine, ref, w, h, what, max_beyond=1e-3, mean_rel=1e-4):
+def _compare(mine, ref, w, h, what, max_beyond=0.0, mean_rel=1e-4, bit_identical=False):
     covered = np.zeros((h, w), bool)
     covered[h - (h // 16) * 16:, :(w // 16) * 16] = True  # the reference renders whole 16x16 blocks only
     m = mine.reshape(h, w, 3)[covered]
@@ -47,6 +47,8 @@ def _compare(mine, ref, w, h, what, max_beyond=1e-3, mean_rel=1e-4):
           f"mean radiance {mean_m:.6f} vs {mean_r:.6f} (relative {abs(mean_m - mean_r) / max(abs(mean_r), 1e-6):.2e})")
     assert r.max() > 0
     assert bad.mean() <= max_beyond, f"{what}: {bad.sum()} of {bad.size} pixels differ by more than 1e-4 relative"
+    if bit_identical:
+        assert exact.all(), f"{what}: {int((~exact).sum())} of {exact.size} pixels are not bit-identical"
     assert abs(mean_m - mean_r) <= mean_rel * max(abs(mean_r), 1e-6) + 1e-6
 
 
@@ -56,7 +58,7 @@ def test_cornell_box_matches_reference_kernel():
     sc = Scene.from_mesh(mesh)
     cam = make_camera_meta(96, 80, [0.0, 0.0, 1.55], [0.0, 0.0, -1.0], fov=(45.0, 38.0), aperture=0.0, focal=1.0)
     mine, ref = _render_both(sc, cam, samples=4)
-    _compare(mine, ref, 96, 80, "cornell")
+    _compare(mine, ref, 96, 80, "cornell", bit_identical=True)
 
 
 @needs_ref
@@ -144,12 +146,10 @@ def test_render_speed_beside_reference_kernel():
     assert compat_ms < 2.0 * ref_ms
 
 
-@needs_ref
-def test_multi_material_speed_and_parity_beside_reference_kernel():
-    """The bench's multi-material view (8,192,002 triangles, 2048 x 1024 sky with sun, 1920 x
-    1080) with its GGX and dielectric spheres given the reference's Metal and Refr kinds: the
-    reference's own pathTracingKernel and tt_render_compat (its algorithm) on the same GB300, 4
-    samples per pixel, parity within 1e-4 and the time of each printed."""
+def _multi_material_reference_kinds():
+    """The bench's multi-material scene (8,192,002 triangles, 2048 x 1024 sky with a 5e4 sun) with
+    its GGX and dielectric spheres given the reference's Metal and Refr kinds, and its 1920 x 1080
+    view."""
     import math
     mesh = scenes.multi_material(400, 5)
     mats = []
@@ -167,6 +167,136 @@ def test_multi_material_speed_and_parity_beside_reference_kernel():
     fy = 2.0 * math.degrees(math.atan(math.tan(math.radians(30.0)) * h / w))
     cam = make_camera_meta(w, h, [0.0, 14.0, 34.0], [0.0, -12.0, -34.0], fov=(60.0, fy))
     bvh = BVHCompact.build(sc, 1e-5, 1, 8)
+    return sc, bvh, cam
+
+
+@pytest.fixture(scope="module")
+def multi_material():
+    return _multi_material_reference_kinds()
+
+
+# fields of a tt_compat_interaction record (32-bit word ranges)
+_REC_FIELDS = {"n": (16, 19), "nl": (19, 22), "point": (22, 25), "out_o": (40, 43), "out_d": (43, 46),
+               "out_mask": (46, 49), "out_rng": (49, 61), "u0": (61, 62)}
+
+
+@pytest.mark.skipif(not refgpu.probe_available(), reason="reference probe cubin not built")
+def test_every_material_interaction_bit_identical_to_reference_kernel(multi_material):
+    """Single-bounce parity inside the reference's own kernel. The probe build of
+    pathTracingKernel (oracle/ref/ref_render_probe.cu) records every material interaction of one
+    frame of the multi-material view at 4 spp (the ray, the hit record renderKernel built, the mask
+    and the curand state going in, and what the reference's Diff / Metal / Refr sampler returned)
+    and every environment lookup at a miss. Its frame must equal the plain build's bit for bit
+    (the recording does not change the reference's arithmetic). Then tt_compat_replay re-runs each
+    record through tt_render_compat's own arithmetic: hit frame (n, nl, point), next ray, mask,
+    curand state and looked-up radiance must all be bit-identical, over more than 10^6 glass (Refr)
+    interactions and as many Metal ones. This project's traversal must also return the
+    reference's own hit (distance and interpolated normal) for every recorded ray, and a miss for
+    every ray that missed."""
+    sc, bvh, cam = multi_material
+    dbvh = DeviceBVH(bvh)
+    r = Renderer(dbvh, sc)
+    meta = render_meta(1, 4)
+    init = np.zeros(3 * cam.width * cam.height, np.float32)
+    args = (bvh.arrays(), sc.materials_raw(), sc.geometries_raw(), sc.env(), cam, meta, init)
+    plain, _ = refgpu.render(*args)
+    probed, recs, made = refgpu.render_probe(*args, capacity=24_000_000)
+    assert np.array_equal(plain.view(np.uint32), probed.view(np.uint32)), "the probe changed the reference's frame"
+    assert recs.shape[0] == made
+    kinds = recs[:, 0].view(np.int32)
+    counts = np.bincount(kinds, minlength=6)
+    print(f"\n{made:,} records: Diff {counts[0]:,}, Metal {counts[1]:,}, Refr {counts[3]:,}, "
+          f"environment lookups {counts[5]:,}")
+    assert counts[3] >= 1_000_000 and counts[1] >= 1_000_000 and counts[5] > 0
+    out = np.empty_like(recs)
+    t = np.empty(recs.shape[0], np.float32)
+    ids = np.empty(recs.shape[0], np.int32)
+    normal = np.empty((recs.shape[0], 3), np.float32)
+    step = 1 << 21
+    for a in range(0, recs.shape[0], step):
+        din = torch.from_numpy(recs[a:a + step].view(np.int32)).cuda()
+        dout = torch.empty_like(din)
+        r.compat_replay(cam, meta, din, dout)
+        # the recorded rays through this project's traversal: (o, d, tmin, tmax) are words 4..11
+        rays = din[:, 4:12].contiguous().view(torch.float32)
+        hits = torch.empty((rays.shape[0], 6), dtype=torch.int32, device="cuda")
+        dbvh.intersect(rays, hits, closest=True, ext=True)
+        torch.cuda.synchronize()
+        out[a:a + step] = dout.cpu().numpy().view(np.uint32)
+        h = hits.cpu().numpy()
+        ids[a:a + step] = h[:, 0]
+        t[a:a + step] = h[:, 2].view(np.float32)
+        normal[a:a + step] = h[:, 3:6].view(np.float32)
+    dbvh.check()
+    bad = {}
+    for name, (i, j) in _REC_FIELDS.items():
+        diff = (out[:, i:j] != recs[:, i:j]).any(axis=1)
+        bad[name] = {k: int(diff[kinds == k].sum()) for k in (0, 1, 3, 5)}
+    hit = kinds != 5
+    bad["trace_t"] = int((t[hit].view(np.uint32) != recs[hit, 15]).sum())
+    bad["trace_normal"] = int((normal[hit].view(np.uint32) != recs[hit, 12:15]).any(axis=1).sum())
+    bad["trace_miss"] = int((ids[~hit] != -1).sum())
+    cam_bad, n_cam = _camera_rays_against_reference(r, cam, meta, recs)
+    bad["camera_ray"] = cam_bad
+    print(f"differing records per field and kind ({n_cam:,} primary rays replayed):", bad)
+    assert all(v == 0 for per in bad.values() for v in (per.values() if isinstance(per, dict) else [per]))
+
+
+def _camera_rays_against_reference(r, cam, meta, recs):
+    """The primary rays in the records (those starting at the camera position: the view has no
+    aperture) replayed as kind-6 records: ray and curand state after the camera's draws must be
+    the reference's. A sample's camera draws start from the thread's seed (its first sample) or
+    from the state its previous sample's last interaction left."""
+    f = recs.view(np.float32)
+    kinds = recs[:, 0].view(np.int32)
+    threads = recs[:, 1].view(np.int32)
+    order = np.argsort(threads, kind="stable")  # per thread, in the order the records were made
+    th = threads[order]
+    pos = np.asarray(cam.position, np.float32).view(np.uint32)
+    start = (recs[order, 4:7] == pos).all(axis=1)
+    first = np.r_[True, th[1:] != th[:-1]]
+    assert start[first].all(), "every thread's first record is a primary ray"
+    idx = np.arange(order.size)
+    # index (in `order`) of the latest interaction record at or before each position, per thread
+    inter = np.where(kinds[order] != 5, idx, -1)
+    last_inter = np.maximum.accumulate(inter)
+    group_start = np.maximum.accumulate(np.where(first, idx, 0))
+    prev_start = np.maximum.accumulate(np.where(start, idx, -1))
+    prev_start_before = np.r_[-1, prev_start[:-1]]  # the sample start before this position
+    li = np.r_[-1, last_inter[:-1]]
+    cand = start & (first | ((li >= group_start) & (li > prev_start_before)))
+    sel = np.where(cand)[0]
+    q = np.zeros((sel.size, 64), np.uint32)
+    q[:, 0] = 6
+    q[:, 1] = recs[order[sel], 1]
+    q[:, 3] = np.where(first[sel], np.uint32(0xFFFFFFFF), 0)  # seq < 0: the thread's seeded state
+    later = ~first[sel]
+    q[later, 28:40] = recs[order[li[sel][later]], 49:61]  # the previous interaction's state out
+    out = np.empty_like(q)
+    step = 1 << 21
+    for a in range(0, q.shape[0], step):
+        din = torch.from_numpy(q[a:a + step].view(np.int32)).cuda()
+        dout = torch.empty_like(din)
+        r.compat_replay(cam, meta, din, dout)
+        torch.cuda.synchronize()
+        out[a:a + step] = dout.cpu().numpy().view(np.uint32)
+    ref = recs[order[sel]]
+    bad = (out[:, 40:46] != ref[:, 4:10]).any(axis=1)
+    # an interaction's incoming state is the camera's outgoing one: the XORWOW words d, v[5] and the
+    # two Box-Muller flags (the Box-Muller scratch values after them are never set by curand_init
+    # and never read here)
+    is_inter = kinds[order[sel]] != 5
+    bad |= is_inter & (out[:, 49:57] != ref[:, 28:36]).any(axis=1)
+    return int(bad.sum()), int(sel.size)
+
+
+@needs_ref
+def test_multi_material_speed_and_parity_beside_reference_kernel(multi_material):
+    """The multi-material view with the reference's kinds: the reference's own pathTracingKernel
+    and tt_render_compat (its algorithm) on the same GB300, 4 samples per pixel, parity within 1e-4
+    and the time of each printed."""
+    sc, bvh, cam = multi_material
+    w, h = cam.width, cam.height
     r = Renderer(DeviceBVH(bvh), sc)
     meta = render_meta(1, 4)
     init = np.zeros(3 * w * h, np.float32)
@@ -185,12 +315,9 @@ def test_multi_material_speed_and_parity_beside_reference_kernel():
         torch.cuda.synchronize()
         best = min(best, e0.elapsed_time(e1))
     r.check()
-    # 96 % of pixels come out bit-identical. The rest carry a 1-2 ulp difference in a refracted
-    # direction (the two compilers contract the Refr arithmetic differently) that a later bounce
-    # turns into a different path; seen through glass with a 5e4-radiance sun behind it, such a
-    # path moves its pixel far, so up to 2 % of pixels may lie beyond 1e-4 while the image mean
-    # still agrees within 1e-4.
-    _compare(acc.cpu().numpy(), ref, w, h, "multi-material (reference kinds)", max_beyond=0.02)
+    # every pixel bit-identical: camera rays, each material interaction, traversal and environment
+    # lookups all follow the reference's own rounding (test_every_material_interaction_...)
+    _compare(acc.cpu().numpy(), ref, w, h, "multi-material (reference kinds)", bit_identical=True)
     rate = lambda ms: 4 * w * h / ms / 1e3
     print(f"multi-material 1920x1080 x 4 spp, Msamples/s: reference pathTracingKernel {rate(ref_ms):.1f} "
           f"({ref_ms:.1f} ms), tt_render_compat {rate(best):.1f} ({best:.1f} ms)")

@@ -283,6 +283,17 @@ class Renderer:
         check(lib().tt_render_compat(self._h, C.byref(cam), C.byref(meta), C.c_void_p(accum.data_ptr()),
                                      C.c_void_p(stream)))
 
+    def compat_replay(self, cam: _lib.CameraMeta, meta: _lib.RenderMeta, records_in, records_out,
+                      stream: int = 0) -> None:
+        """Re-runs recorded material interactions, environment lookups and primary rays (CUDA
+        int32 tensors of shape (n, 64), the tt_compat_interaction layout) through tt_render_compat's
+        own arithmetic into records_out."""
+        if records_in.shape != records_out.shape or records_in.shape[-1] != 64:
+            raise ValueError("records must be (n, 64) 32-bit words, in and out of the same shape")
+        check(lib().tt_compat_replay(self._h, C.byref(cam), C.byref(meta), C.c_void_p(records_in.data_ptr()),
+                                     int(records_in.shape[0]), C.c_void_p(records_out.data_ptr()),
+                                     C.c_void_p(stream)))
+
     def render_native(self, cam: _lib.CameraMeta, params: _lib.RenderParams, accum, stream: int = 0) -> None:
         """Native wavefront path tracer: adds spp samples per pixel to accum (CUDA tensor W*H*3,
         float32, or float64 with the RENDER_ACCUM_F64 flag; row 0 = top)."""

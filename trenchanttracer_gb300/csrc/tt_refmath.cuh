@@ -47,6 +47,17 @@ __device__ __forceinline__ V3 r_normalize(const V3 &a) {
     const float n = __fsqrt_rn(__fmaf_rn(a.z, a.z, __fmaf_rn(a.x, a.x, __fmul_rn(a.y, a.y))));
     return V3(__fdiv_rn(a.x, n), __fdiv_rn(a.y, n), __fdiv_rn(a.z, n));
 }
+// The same two Vec3f expressions where nvcc contracts them the other way round, as it does inside
+// the reference's refrSample (measured on interactions recorded in the reference's own kernel):
+// dot(n, d) in `d - n * 2.0f * dot(n, d)` -> fma(y, y', x*x') + z*z' (the last product unfused),
+// and Vec3f::normalize -> sqrtf(fma(z, z, fma(y, y, x*x))).
+__device__ __forceinline__ float r_dot_yx(const V3 &a, const V3 &b) {
+    return __fadd_rn(__fmaf_rn(a.y, b.y, __fmul_rn(a.x, b.x)), __fmul_rn(a.z, b.z));
+}
+__device__ __forceinline__ V3 r_normalize_yx(const V3 &a) {
+    const float n = __fsqrt_rn(__fmaf_rn(a.z, a.z, __fmaf_rn(a.y, a.y, __fmul_rn(a.x, a.x))));
+    return V3(__fdiv_rn(a.x, n), __fdiv_rn(a.y, n), __fdiv_rn(a.z, n));
+}
 // Vec3f::length
 __device__ __forceinline__ float r_length(const V3 &a) {
     return __fsqrt_rn(__fmaf_rn(a.z, a.z, __fmaf_rn(a.x, a.x, __fmul_rn(a.y, a.y))));

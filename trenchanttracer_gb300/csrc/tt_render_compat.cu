@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 #include <curand_kernel.h>
 
+#include <algorithm>
 #include <string>
 
 #include "tt_device.h"
@@ -144,11 +145,19 @@ __device__ __forceinline__ V3 lobe_dir(const V3 &u, const V3 &v, const V3 &w, fl
     return r;
 }
 
-// d - n * 2.0f * dot(n, d)
+// `d - n * 2.0f * dot(n, d)` (MetalImpl.cuh:25, CoatImpl.cuh:12-14, RefrImpl.cuh:24,43): inside the
+// reference's kernel dot(n, d) rounds as r_dot_yx in all three samplers; Metal and Refr fuse the
+// n * 2 * k product into the subtraction, Coat's reflect() keeps it rounded (both measured on
+// interactions recorded in the reference's own kernel, oracle/ref/ref_render_probe.cu).
 __device__ __forceinline__ V3 reflect_ref(const V3 &d, const V3 &n) {
-    const float k = r_dot(n, d);
+    const float k = r_dot_yx(n, d);
     return V3(__fmaf_rn(-__fmul_rn(n.x, 2.0f), k, d.x), __fmaf_rn(-__fmul_rn(n.y, 2.0f), k, d.y),
               __fmaf_rn(-__fmul_rn(n.z, 2.0f), k, d.z));
+}
+__device__ __forceinline__ V3 reflect_ref_rounded(const V3 &d, const V3 &n) {
+    const float k = r_dot_yx(n, d);
+    return V3(__fsub_rn(d.x, __fmul_rn(__fmul_rn(n.x, 2.0f), k)), __fsub_rn(d.y, __fmul_rn(__fmul_rn(n.y, 2.0f), k)),
+              __fsub_rn(d.z, __fmul_rn(__fmul_rn(n.z, 2.0f), k)));
 }
 
 struct RRay {
@@ -194,7 +203,14 @@ __device__ __forceinline__ void spec_sample(const MaterialRec &m, RRay &ray, con
     mask = r_mul(mask, V3(m.color[0], m.color[1], m.color[2]));
 }
 
-// refrSample (include/material/RefrImpl.cuh:12-61): IOR 1.4, Schlick weights, reflect p = 0.2
+// refrSample (include/material/RefrImpl.cuh:12-61): IOR 1.4, Schlick weights, reflect p = 0.2.
+// The rounding of every expression was pinned against interactions recorded inside the reference's
+// own kernel (oracle/ref/ref_render_probe.cu): the reflected direction is normalised as
+// r_normalize_yx, and so is the transmitted one the second time round.
+__device__ __forceinline__ V3 refr_reflect(const V3 &d, const V3 &n) {
+    return r_normalize_yx(reflect_ref(d, n));
+}
+
 __device__ __forceinline__ void refr_sample(curandState *rs, RRay &ray, const RHit &h, V3 &mask) {
     const bool into = r_dot(h.n, h.nl) > 0;
     const float nc = 1.0f, nt = 1.4f;
@@ -202,14 +218,12 @@ __device__ __forceinline__ void refr_sample(curandState *rs, RRay &ray, const RH
     const float ddn = r_dot(ray.d, h.nl);
     const float cos2t = __fmaf_rn(-__fmul_rn(nnt, nnt), __fmaf_rn(-ddn, ddn, 1.f), 1.0f);
     if (cos2t < 0.0f) {
-        ray.d = r_normalize(reflect_ref(ray.d, h.n));
+        ray.d = refr_reflect(ray.d, h.n);
         ray.o = r_madd(h.nl, 0.001f, h.point);
         return;
     }
     const float k = __fmul_rn((float)(into ? 1 : -1), __fmaf_rn(ddn, nnt, __fsqrt_rn(cos2t)));
-    // `tdir = d * nnt; tdir -= n * k;`: the compiled reference keeps d * nnt rounded and fuses n * k
-    // into the subtraction (the other fusion matches 96.8 % of the showcase's glass pixels, this one
-    // 99.2 %)
+    // `tdir = d * nnt; tdir -= n * k;`: d * nnt stays rounded and n * k is fused into the subtraction
     V3 tdir(__fmaf_rn(-h.n.x, k, __fmul_rn(ray.d.x, nnt)), __fmaf_rn(-h.n.y, k, __fmul_rn(ray.d.y, nnt)),
             __fmaf_rn(-h.n.z, k, __fmul_rn(ray.d.z, nnt)));
     tdir = r_normalize(tdir);
@@ -224,10 +238,10 @@ __device__ __forceinline__ void refr_sample(curandState *rs, RRay &ray, const RH
     const float TP = __fdiv_rn(Tr, __fsub_rn(1.f, P));
     if ((double)curand_uniform(rs) < 0.2) {
         mask = r_mul(mask, RP);
-        ray.d = r_normalize(reflect_ref(ray.d, h.n));
+        ray.d = refr_reflect(ray.d, h.n);
     } else {
         mask = r_mul(mask, TP);
-        ray.d = r_normalize(tdir);
+        ray.d = r_normalize_yx(tdir);  // `nextRay.direction = tdir; nextRay.direction.normalize();`
     }
     ray.o = r_madd(h.nl, 0.001f, h.point);
 }
@@ -256,7 +270,7 @@ __device__ __forceinline__ float coat_fresnel(const RRay &ray, const RHit &h, fl
 // coatSample (include/material/CoatImpl.cuh:68-116)
 __device__ __forceinline__ void coat_sample(const MaterialRec &m, curandState *rs, RRay &ray, const RHit &h,
                                             V3 &mask) {
-    const V3 refl = reflect_ref(ray.d, h.n);
+    const V3 refl = reflect_ref_rounded(ray.d, h.n);
     const float roulette = curand_uniform(rs);
     const float n_air = (float)1.000293, n_coat = (float)1.291;  // double literals, as written
     const V3 refr = coat_refract(ray, h, n_air, n_coat);
@@ -275,6 +289,26 @@ __device__ __forceinline__ void coat_sample(const MaterialRec &m, curandState *r
         ray.d = r_normalize(lobe_dir(u, v, w, cosf(r1), sinf(r1), r2s, __fsqrt_rn(__fsub_rn(1.f, r2))));
         ray.o = r_madd(h.nl, 0.001f, h.point);
         mask = r_mul(mask, V3(m.color[0], m.color[1], m.color[2]));
+    }
+}
+
+// normalize(hit, ray) + hitPoint(hit, ray) (include/geometry/IntersectKernel.cuh:62-76)
+__device__ __forceinline__ void hit_frame(RHit &hit, const RRay &ray) {
+    hit.n = r_normalize(hit.normal);
+    hit.nl = r_dot(hit.n, ray.d) < 0 ? hit.n : r_mul(hit.n, -1.0f);
+    hit.point = r_madd(ray.d, hit.distance, ray.o);
+}
+
+// the sampler switch of renderKernel (src/core/RenderKernel.cu:75-91)
+__device__ __forceinline__ void sample_material(const MaterialRec &m, int kind, curandState *rs, RRay &ray,
+                                                const RHit &hit, V3 &mask) {
+    switch (kind) {
+        case MAT_COAT: coat_sample(m, rs, ray, hit, mask); break;
+        case MAT_DIFF: diff_sample(m, rs, ray, hit, mask); break;
+        case MAT_METAL: metal_sample(m, rs, ray, hit, mask); break;
+        case MAT_SPEC: spec_sample(m, ray, hit, mask); break;
+        case MAT_REFR: refr_sample(rs, ray, hit, mask); break;
+        default: break;  // materials the reference does not know leave the ray unchanged
     }
 }
 
@@ -315,22 +349,57 @@ __device__ V3 radiance(const CompatArgs &a, curandState *rs, RRay ray, uint32_t 
             acc = r_madd(mask, env_lookup(a, ray.d), acc);
             return acc;
         }
-        hit.n = r_normalize(hit.normal);
-        hit.nl = r_dot(hit.n, ray.d) < 0 ? hit.n : r_mul(hit.n, -1.0f);
-        hit.point = r_madd(ray.d, hit.distance, ray.o);
+        hit_frame(hit, ray);
         if (hit.mat < 0 || hit.mat >= a.num_materials) return acc;  // no material: stop the path
         const MaterialRec m = a.materials[hit.mat];
         acc = r_madd(mask, V3(m.emission[0], m.emission[1], m.emission[2]), acc);
-        switch (m.kind) {
-            case MAT_COAT: coat_sample(m, rs, ray, hit, mask); break;
-            case MAT_DIFF: diff_sample(m, rs, ray, hit, mask); break;
-            case MAT_METAL: metal_sample(m, rs, ray, hit, mask); break;
-            case MAT_SPEC: spec_sample(m, ray, hit, mask); break;
-            case MAT_REFR: refr_sample(rs, ray, hit, mask); break;
-            default: break;  // materials the reference does not know leave the ray unchanged
-        }
+        sample_material(m, m.kind, rs, ray, hit, mask);
     }
     return acc;
+}
+
+// The primary ray of one sample (src/core/RenderKernel.cu:131-197): jitter and, with an aperture,
+// a lens point drawn from rs; pixel_y counts from the image's bottom row.
+__device__ __forceinline__ RRay camera_ray(const CompatArgs &a, int pixel_x, int pixel_y, curandState *rs) {
+    const int width = a.cam.width;
+    const int height = a.cam.height;
+    const V3 cam_pos(a.cam.position[0], a.cam.position[1], a.cam.position[2]);
+    const V3 view = r_normalize(V3(a.cam.view[0], a.cam.view[1], a.cam.view[2]));
+    const V3 up = r_normalize(V3(a.cam.up[0], a.cam.up[1], a.cam.up[2]));
+    const V3 haxis = r_normalize(r_cross(view, up));
+    const V3 vaxis = r_normalize(r_cross(haxis, view));
+    const V3 middle = r_add(cam_pos, view);
+    const float deg = __fdiv_rn(a.meta.pi, 180.0f);
+    const V3 horizontal = r_mul(haxis, tanf(__fmul_rn(__fmul_rn(a.cam.fov[0], 0.5f), deg)));
+    const V3 vertical = r_mul(vaxis, tanf(__fmul_rn(__fmul_rn(-a.cam.fov[1], 0.5f), deg)));
+    const float jx = __fsub_rn(curand_uniform(rs), 0.5f);
+    const float jy = __fsub_rn(curand_uniform(rs), 0.5f);
+    const float sx = __fdiv_rn(__fadd_rn(jx, (float)pixel_x), (float)(width - 1));
+    const float sy = __fdiv_rn(__fadd_rn(jy, (float)pixel_y), (float)(height - 1));
+    const float ax = __fmaf_rn(2.0f, sx, -1.0f);
+    const float ay = __fmaf_rn(2.0f, sy, -1.0f);
+    const V3 point = r_madd(vertical, ay, r_madd(horizontal, ax, middle));
+    const V3 on_plane = r_madd(r_sub(point, cam_pos), a.cam.focal, cam_pos);
+    V3 aperture_point = cam_pos;
+    if ((double)a.cam.aperture > 0.00001) {
+        const float rnd1 = curand_uniform(rs);
+        const float rnd2 = curand_uniform(rs);
+        const float angle = __fmul_rn(a.meta.two_pi, rnd1);
+        const float dist = __fmul_rn(a.cam.aperture, __fsqrt_rn(rnd2));
+        const float apx = __fmul_rn(cosf(angle), dist);
+        const float apy = __fmul_rn(sinf(angle), dist);
+        aperture_point = r_madd(vaxis, apy, r_madd(haxis, apx, cam_pos));
+    }
+    // apertureToImagePlane.normalize() rounds as r_normalize_yx, the second normalize as
+    // r_normalize (measured on primary rays recorded in the reference's own kernel)
+    V3 dir = r_normalize_yx(r_sub(on_plane, aperture_point));
+    dir = r_normalize(dir);
+    RRay ray;
+    ray.o = aperture_point;
+    ray.d = dir;
+    ray.tmin = 0.01f;  // tMin, tMax of pathTracingKernel (:110-111)
+    ray.tmax = 1e20f;
+    return ray;
 }
 
 // pathTracingKernel (src/core/RenderKernel.cu:97-206): one thread per pixel, 16x16 blocks.
@@ -339,52 +408,17 @@ __global__ void __launch_bounds__(256) render_compat_kernel(CompatArgs a) {
     const unsigned y = blockIdx.y * blockDim.y + threadIdx.y;
     const int width = a.cam.width;
     const int height = a.cam.height;
-    const float tmin = 0.01f;
-    const float tmax = 1e20f;
     const int thread_id = (int)((blockIdx.x + blockIdx.y * gridDim.x) * (blockDim.x * blockDim.y) +
                                 (threadIdx.y * blockDim.x) + threadIdx.x);
     curandState rs;
     curand_init((unsigned long long)(a.meta.hashed_frame + (unsigned)thread_id), 0, 0, &rs);
     uint32_t err = 0;
     V3 final_color(0.0f, 0.0f, 0.0f);
-    const V3 cam_pos(a.cam.position[0], a.cam.position[1], a.cam.position[2]);
     const int i = (int)((unsigned)(height - (int)y - 1) * (unsigned)width + x);
     const int pixel_x = (int)x;
     const int pixel_y = height - (int)y - 1;
     for (int s = 0; s < a.meta.samples; s++) {
-        const V3 view = r_normalize(V3(a.cam.view[0], a.cam.view[1], a.cam.view[2]));
-        const V3 up = r_normalize(V3(a.cam.up[0], a.cam.up[1], a.cam.up[2]));
-        const V3 haxis = r_normalize(r_cross(view, up));
-        const V3 vaxis = r_normalize(r_cross(haxis, view));
-        const V3 middle = r_add(cam_pos, view);
-        const float deg = __fdiv_rn(a.meta.pi, 180.0f);
-        const V3 horizontal = r_mul(haxis, tanf(__fmul_rn(__fmul_rn(a.cam.fov[0], 0.5f), deg)));
-        const V3 vertical = r_mul(vaxis, tanf(__fmul_rn(__fmul_rn(-a.cam.fov[1], 0.5f), deg)));
-        const float jx = __fsub_rn(curand_uniform(&rs), 0.5f);
-        const float jy = __fsub_rn(curand_uniform(&rs), 0.5f);
-        const float sx = __fdiv_rn(__fadd_rn(jx, (float)pixel_x), (float)(width - 1));
-        const float sy = __fdiv_rn(__fadd_rn(jy, (float)pixel_y), (float)(height - 1));
-        const float ax = __fmaf_rn(2.0f, sx, -1.0f);
-        const float ay = __fmaf_rn(2.0f, sy, -1.0f);
-        const V3 point = r_madd(vertical, ay, r_madd(horizontal, ax, middle));
-        const V3 on_plane = r_madd(r_sub(point, cam_pos), a.cam.focal, cam_pos);
-        V3 aperture_point = cam_pos;
-        if ((double)a.cam.aperture > 0.00001) {
-            const float rnd1 = curand_uniform(&rs);
-            const float rnd2 = curand_uniform(&rs);
-            const float angle = __fmul_rn(a.meta.two_pi, rnd1);
-            const float dist = __fmul_rn(a.cam.aperture, __fsqrt_rn(rnd2));
-            const float apx = __fmul_rn(cosf(angle), dist);
-            const float apy = __fmul_rn(sinf(angle), dist);
-            aperture_point = r_madd(vaxis, apy, r_madd(haxis, apx, cam_pos));
-        }
-        V3 dir = r_normalize(r_sub(on_plane, aperture_point));
-        dir = r_normalize(dir);
-        RRay ray;
-        ray.o = aperture_point;
-        ray.d = dir;
-        ray.tmin = tmin;
-        ray.tmax = tmax;
+        const RRay ray = camera_ray(a, pixel_x, pixel_y, &rs);
         const V3 L = radiance(a, &rs, ray, err);
         final_color = r_madd(L, __fdiv_rn(1.0f, (float)a.meta.samples), final_color);
     }
@@ -393,6 +427,78 @@ __global__ void __launch_bounds__(256) render_compat_kernel(CompatArgs a) {
     px[1] = __fadd_rn(px[1], final_color.y);
     px[2] = __fadd_rn(px[2], final_color.z);
     if (err) atomicOr(a.err, err);
+}
+
+__device__ __forceinline__ V3 ld3(const float *p) { return V3(p[0], p[1], p[2]); }
+__device__ __forceinline__ void st3(float *p, const V3 &v) {
+    p[0] = v.x;
+    p[1] = v.y;
+    p[2] = v.z;
+}
+
+// tt_compat_replay: one recorded interaction per thread (grid-stride)
+__global__ void compat_replay_kernel(CompatArgs a, const tt_compat_interaction *in, long long n,
+                                     tt_compat_interaction *out) {
+    static_assert(sizeof(curandState) == 48, "curand XORWOW state is 12 words");
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        tt_compat_interaction r = in[i];
+        if (r.kind == 5) {  // environment lookup at a miss
+            st3(r.out_mask, env_lookup(a, ld3(r.d)));
+            out[i] = r;
+            continue;
+        }
+        if (r.kind == 6) {  // a sample's primary ray for the pixel of thread r.thread
+            const int gx = a.cam.width / 16;
+            const int block = r.thread / 256, lane = r.thread % 256;
+            const int x = (block % gx) * 16 + lane % 16, y = (block / gx) * 16 + lane / 16;
+            curandState st;
+            if (r.seq < 0)  // the thread's first sample: the state pathTracingKernel seeds
+                curand_init((unsigned long long)(a.meta.hashed_frame + (unsigned)r.thread), 0, 0, &st);
+            else
+                memcpy(&st, r.rng, sizeof(st));
+            const RRay ray = camera_ray(a, x, a.cam.height - y - 1, &st);
+            st3(r.out_o, ray.o);
+            st3(r.out_d, ray.d);
+            r.tmin = ray.tmin;
+            r.tmax = ray.tmax;
+            memcpy(r.out_rng, &st, sizeof(st));
+            out[i] = r;
+            continue;
+        }
+        RRay ray;
+        ray.o = ld3(r.o);
+        ray.d = ld3(r.d);
+        ray.tmin = r.tmin;
+        ray.tmax = r.tmax;
+        RHit mine;
+        mine.normal = ld3(r.normal);
+        mine.distance = r.distance;
+        hit_frame(mine, ray);
+        RHit h = mine;  // the sampler sees the recorded n / nl / point
+        h.n = ld3(r.n);
+        h.nl = ld3(r.nl);
+        h.point = ld3(r.point);
+        st3(r.n, mine.n);
+        st3(r.nl, mine.nl);
+        st3(r.point, mine.point);
+        curandState st;
+        memcpy(&st, r.rng, sizeof(st));
+        {
+            curandState c = st;
+            r.u0 = curand_uniform(&c);
+        }
+        V3 mask = ld3(r.mask);
+        if (r.material >= 0 && r.material < a.num_materials && r.kind >= MAT_DIFF && r.kind <= MAT_COAT) {
+            sample_material(a.materials[r.material], r.kind, &st, ray, h, mask);
+        } else {
+            r.kind = -1;  // not a record this renderer can replay
+        }
+        st3(r.out_o, ray.o);
+        st3(r.out_d, ray.d);
+        st3(r.out_mask, mask);
+        memcpy(r.out_rng, &st, sizeof(st));
+        out[i] = r;
+    }
 }
 
 }  // namespace tt
@@ -500,6 +606,27 @@ tt_status tt_renderer_check(tt_renderer *r, void *stream) {
         if (w & kErrIter) return fail(TT_ERR_TIMEOUT, "traversal iteration cap reached during rendering");
         return fail(TT_ERR_TIMEOUT, "a radiance-cache tensor-core wait ran out during rendering");
     }
+    return TT_OK;
+}
+
+tt_status tt_compat_replay(const tt_renderer *r, const tt_camera_meta *cam, const tt_render_meta *meta,
+                           const tt_compat_interaction *d_in, int64_t n, tt_compat_interaction *d_out, void *stream) {
+    if (!r || !cam || !meta || (n > 0 && (!d_in || !d_out))) return fail(TT_ERR_INVALID, "null argument");
+    if (cam->width < 16 || cam->height < 16) return fail(TT_ERR_INVALID, "image must be at least 16 x 16");
+    if (n < 0) return fail(TT_ERR_INVALID, "negative record count");
+    if (n == 0) return TT_OK;
+    CompatArgs a{};
+    a.materials = r->materials;
+    a.num_materials = r->num_materials;
+    a.env = r->env_w > 0 ? r->env : nullptr;
+    a.env_w = r->env_w;
+    a.env_h = r->env_h;
+    a.meta = *meta;
+    a.cam = *cam;
+    const int threads = 256;
+    const long long blocks = std::min<long long>((n + threads - 1) / threads, 152ll * 16);
+    compat_replay_kernel<<<(unsigned)blocks, threads, 0, (cudaStream_t)stream>>>(a, d_in, (long long)n, d_out);
+    TT_CUDA_R(cudaGetLastError());
     return TT_OK;
 }
 
