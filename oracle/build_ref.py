@@ -7,6 +7,9 @@ Outputs:
                                  a cudart stub standing in for device memory
   oracle/_ref/ref_intersect.cubin the reference's device intersect() inside a one-ray-per-thread
                                  harness, compiled for sm_103a
+  oracle/_ref/ref_render*.cubin  the reference's pathTracingKernel: as written (ref_render), with its
+                                 material interactions recorded (ref_render_probe), and with
+                                 intersect()'s warp vote taken per lane (ref_render_lane_vote)
 
 The reference sources are compiled where they lie under the reference checkout. Exactly two
 headers are shadowed by patched copies written to a temporary directory (deleted afterwards):
@@ -117,6 +120,14 @@ def _gpu_kernel_header(src: str) -> str:
     return _patch(src, BALLOT_LINE, BALLOT_SHIM)
 
 
+def _gpu_lane_vote_header(src: str) -> str:
+    """The device kernel with its warp vote made per lane: a lane stops looking for leaves when it
+    has found one itself, not when every lane of its warp has (the per-ray algorithm)."""
+    start = src.index('asm("{\\n"')
+    end = src.index(': "r"(leafAddr));', start) + len(': "r"(leafAddr));')
+    return src[:start] + "mask = (leafAddr >= 0) ? 1u : 0u;" + src[end:]
+
+
 def _run(cmd: list[str]) -> None:
     proc = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
     if proc.returncode != 0:
@@ -134,11 +145,14 @@ def build(ref: Path = DEFAULT_REF, quiet: bool = True) -> bool:
         tmp = Path(tmp)
         host_inc = tmp / "host" / "geometry"
         gpu_inc = tmp / "gpu" / "geometry"
+        lane_inc = tmp / "lane" / "geometry"
         host_inc.mkdir(parents=True)
         gpu_inc.mkdir(parents=True)
+        lane_inc.mkdir(parents=True)
         (host_inc / "IntersectKernel.cuh").write_text(_host_kernel_header(kernel))
         (gpu_inc / "IntersectKernel.cuh").write_text(_gpu_kernel_header(kernel))
-        for side in ("host", "gpu"):
+        (lane_inc / "IntersectKernel.cuh").write_text(_gpu_lane_vote_header(kernel))
+        for side in ("host", "gpu", "lane"):
             (tmp / side / "core").mkdir()
             (tmp / side / "core" / "Renderer.h").write_text(RENDERER_STUB)
 
@@ -173,6 +187,11 @@ def build(ref: Path = DEFAULT_REF, quiet: bool = True) -> bool:
         _run([str(cuda / "bin" / "nvcc"), "-cubin", "-gencode=arch=compute_103a,code=sm_103a", "-w",
               "-I" + str(tmp / "gpu"), "-I" + str(ref / "include"), "-I" + str(ref / "lib" / "include"),
               "-I" + str(ref), str(HERE / "ref" / "ref_render_harness.cu"), "-o", str(OUT / "ref_render.cubin")])
+        # the same kernel with intersect()'s warp vote made per lane (nothing else changed)
+        _run([str(cuda / "bin" / "nvcc"), "-cubin", "-gencode=arch=compute_103a,code=sm_103a", "-w",
+              "-I" + str(tmp / "lane"), "-I" + str(ref / "include"), "-I" + str(ref / "lib" / "include"),
+              "-I" + str(ref), str(HERE / "ref" / "ref_render_harness.cu"), "-o",
+              str(OUT / "ref_render_lane_vote.cubin")])
         # the same kernel with every material interaction recorded (ref_render_probe.cu)
         _run([str(cuda / "bin" / "nvcc"), "-cubin", "-gencode=arch=compute_103a,code=sm_103a", "-w",
               "-I" + str(tmp / "gpu"), "-I" + str(ref / "include"), "-I" + str(ref / "lib" / "include"),

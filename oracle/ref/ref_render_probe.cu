@@ -140,10 +140,27 @@ __device__ __inline__ Vec3f probe_hdr(const HDRImage *img, const Ray &ray, Rende
 
 // renderKernel's calls go to the wrappers; the samplers' own headers are already included above,
 // so RenderKernel.cu's includes of them are no-ops and the definitions keep their names.
+// TT_PROBE_KINDS (bit k: MaterialType k, bit 5: hdrSample; default all) picks which calls are
+// recorded, so that a build recording fewer of them can be checked against the plain frame.
+#ifndef TT_PROBE_KINDS
+#define TT_PROBE_KINDS 0x3F
+#endif
+#if TT_PROBE_KINDS & 1
 #define diffSample probe_diff
+#endif
+#if TT_PROBE_KINDS & 2
 #define metalSample probe_metal
+#endif
+#if TT_PROBE_KINDS & 4
 #define specSample probe_spec
+#endif
+#if TT_PROBE_KINDS & 8
 #define refrSample probe_refr
+#endif
+#if TT_PROBE_KINDS & 16
 #define coatSample probe_coat
+#endif
+#if TT_PROBE_KINDS & 32
 #define hdrSample probe_hdr
+#endif
 #include "ref_render_harness.cu"

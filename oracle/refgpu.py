@@ -99,11 +99,16 @@ _SCENE_ARGTYPES = [C.c_char_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C
                    C.c_int, C.c_int, C.c_int, C.c_uint, C.c_int, C.c_float, C.c_float, C.c_void_p]
 
 
+LANE_VOTE_CUBIN = HERE / "_ref" / "ref_render_lane_vote.cubin"
+
+
 def render(bvh_arrays: dict, materials: list, geometries: list, env: np.ndarray | None, cam, meta,
-           accum: np.ndarray) -> tuple[np.ndarray, float]:
+           accum: np.ndarray, lane_vote: bool = False) -> tuple[np.ndarray, float]:
     """One frame of the reference's own pathTracingKernel. materials / geometries: the
     tt_material / tt_geometry records of the scene; cam / meta: CameraMeta / RenderMeta;
-    accum: (W*H*3,) float32 starting contents. Returns (accumulation buffer, kernel ms)."""
+    accum: (W*H*3,) float32 starting contents. lane_vote: the build whose intersect() stops
+    looking for leaves per lane instead of per warp (ref_render_lane_vote.cubin). Returns
+    (accumulation buffer, kernel ms)."""
     h = _load()
     if not hasattr(h, "_render_ready"):
         h.ref_gpu_render.restype = C.c_int
@@ -112,7 +117,7 @@ def render(bvh_arrays: dict, materials: list, geometries: list, env: np.ndarray 
     keep, args = _render_args(bvh_arrays, materials, geometries, env, cam)
     out = np.ascontiguousarray(accum, dtype=np.float32).copy()
     ms = C.c_float(0.0)
-    rc = h.ref_gpu_render(str(RENDER_CUBIN).encode(), *args, meta.frame_number, meta.hashed_frame, meta.samples,
+    rc = h.ref_gpu_render(str(LANE_VOTE_CUBIN if lane_vote else RENDER_CUBIN).encode(), *args, meta.frame_number, meta.hashed_frame, meta.samples,
                           meta.pi, meta.two_pi, out.ctypes.data, C.byref(ms))
     del keep
     if rc != 0:

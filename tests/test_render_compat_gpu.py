@@ -73,10 +73,16 @@ def test_every_reference_material_with_env_dof_and_analytic_objects():
     sc.set_materials(mats)
     sc.set_geometries(geoms)
     sc.set_env(scenes.sky_env(128, 64, sun_radiance=40.0, sun_diameter_deg=6.0))
-    cam = make_camera_meta(128, 64, [0.0, 1.0, 3.2], [0.0, -0.25, -1.0], fov=(55.0, 30.0), aperture=0.03,
+    cam = make_camera_meta(512, 256, [0.0, 1.0, 3.2], [0.0, -0.25, -1.0], fov=(55.0, 30.0), aperture=0.03,
                            focal=3.0)
-    mine, ref = _render_both(sc, cam, samples=4, frame=3)
-    _compare(mine, ref, 128, 64, "materials + env + depth of field")
+    mine, ref = _render_both(sc, cam, samples=8, frame=3)
+    _compare(mine, ref, 512, 256, "materials + env + depth of field", bit_identical=True)
+    # the reference's intersect() stops looking for leaves when its whole warp has found one; the
+    # frame is the same when each lane stops on its own (the per-ray algorithm this project runs)
+    bvh = BVHCompact.build(sc, 1e-5, 1, 8)
+    lane, _ = refgpu.render(bvh.arrays(), sc.materials_raw(), sc.geometries_raw(), sc.env(), cam,
+                            render_meta(3, 8), np.zeros(3 * 512 * 256, np.float32), lane_vote=True)
+    assert np.array_equal(lane.view(np.uint32), ref.view(np.uint32))
 
 
 @needs_ref
@@ -85,7 +91,7 @@ def test_json_scene_camera_matches_reference_kernel(golden_scene_files):
     sc.set_env(scenes.sky_env(64, 32, sun_radiance=20.0, sun_diameter_deg=12.0))  # the scene has no emitter
     cam = camera_meta(sc, 45.0)
     mine, ref = _render_both(sc, cam, samples=2, frame=7)
-    _compare(mine, ref, cam.width, cam.height, "JSON scene (planes, sphere, transforms)")
+    _compare(mine, ref, cam.width, cam.height, "JSON scene (planes, sphere, transforms)", bit_identical=True)
 
 
 def test_compat_render_is_deterministic():

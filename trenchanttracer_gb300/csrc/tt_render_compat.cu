@@ -146,7 +146,7 @@ __device__ __forceinline__ V3 lobe_dir(const V3 &u, const V3 &v, const V3 &w, fl
 }
 
 // `d - n * 2.0f * dot(n, d)` (MetalImpl.cuh:25, CoatImpl.cuh:12-14, RefrImpl.cuh:24,43): inside the
-// reference's kernel dot(n, d) rounds as r_dot_yx in all three samplers; Metal and Refr fuse the
+// reference's kernel dot(n, d) rounds as r_dot_yx in all three samplers (and in Spec's reflection); Metal and Refr fuse the
 // n * 2 * k product into the subtraction, Coat's reflect() keeps it rounded (both measured on
 // interactions recorded in the reference's own kernel, oracle/ref/ref_render_probe.cu).
 __device__ __forceinline__ V3 reflect_ref(const V3 &d, const V3 &n) {
@@ -193,9 +193,12 @@ __device__ __forceinline__ void metal_sample(const MaterialRec &m, curandState *
     mask = r_mul(mask, V3(m.color[0], m.color[1], m.color[2]));
 }
 
-// specSample (include/material/SpecImpl.cuh:12-25): d - n * dot(n, d) * 2.0f
+// specSample (include/material/SpecImpl.cuh:12-25): d - n * dot(n, d) * 2.0f, with dot(n, d) rounded
+// as in the other samplers' reflections (r_dot_yx; found by comparing whole frames of a scene that
+// mixes every material kind, because recording Spec interactions changes how nvcc compiles the
+// reference's kernel)
 __device__ __forceinline__ void spec_sample(const MaterialRec &m, RRay &ray, const RHit &h, V3 &mask) {
-    const float k = r_dot(h.n, ray.d);
+    const float k = r_dot_yx(h.n, ray.d);
     const V3 d(__fmaf_rn(-__fmul_rn(h.n.x, k), 2.0f, ray.d.x), __fmaf_rn(-__fmul_rn(h.n.y, k), 2.0f, ray.d.y),
                __fmaf_rn(-__fmul_rn(h.n.z, k), 2.0f, ray.d.z));
     ray.d = r_normalize(d);
