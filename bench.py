@@ -79,6 +79,38 @@ def load_peaks() -> dict:
     return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
+# the SIMD efficiency and the L2 figures of the trace kernel from the same committed ncu capture
+# (profiles/trace_kernel_terrain_closest.md, incoherent launch): threads per executed instruction
+TRACE_THREADS_PER_INST = 9.74
+
+
+def terrain_config(n_rays: int) -> dict:
+    """The workload description both arms print (the same dict, so the lines compare)."""
+    return {"workload": "terrain ray-cast: 1024x1024-cell fBm heightfield, 2,097,152 tris, world scale 8; "
+                        f"{n_rays // 2:,} coherent primary + {n_rays // 2:,} incoherent rays, closest hit",
+            "bvh": "compact SBVH, split alpha 1e-5, leaf <= 8", "rays_per_step": n_rays,
+            "l2": "inputs larger than L2; L2 also flushed (256 MB write) between GPU steps, untimed"}
+
+
+def reference_workload(width: int = WIDTH) -> dict:
+    """The terrain workload built by the oracle alone (no libtt.so): the mesh from the numpy scene
+    generators, the BVH by the oracle's restatement of the reference's single-threaded SBVH builder
+    (timed), the incoherent rays spawned from the first hits of the oracle's traversal in the
+    reference kernel's arithmetic (so the rays are those of the GPU arm, bit for bit)."""
+    from oracle import oracle
+    from trenchanttracer_gb300 import scenes  # numpy only; loads no library
+    mesh = scenes.terrain(N_CELLS, SCALE)
+    with tempfile.TemporaryDirectory() as d:
+        build_s = oracle.sbvh_build(mesh.vertices, mesh.normals, mesh.vidx, mesh.nidx, mesh.mat,
+                                    Path(d) / "bvh.cache", 1e-5, 1, 8)
+        arr = oracle.read_cache(Path(d) / "bvh.cache")
+    cam = scenes.terrain_camera(SCALE)
+    primary = scenes.pinhole_rays(width, width, cam["eye"], cam["target"], cam["tan_half_fov"])
+    first = oracle.intersect(arr, primary, True, arith=oracle.DEVICE, normals=True)
+    secondary, _ = scenes.secondary_rays(primary, first["t"], first["normal"], primary.shape[0], 11, 1e-4 * SCALE)
+    return {"arrays": arr, "primary": primary, "secondary": secondary, "build_s": build_s, "mesh": mesh}
+
+
 def workload(trace_ext=None, width: int = WIDTH):
     """Scene, BVH and the two ray sets (width^2 rays each). trace_ext(rays) -> (t, normal) gives
     the first hits from which the incoherent rays are spawned (the product's own kernel on the
@@ -222,22 +254,49 @@ def whole_job_rate(units_per_rank: float, ms: float, world: int) -> float:
     return world * units_per_rank / ms / 1e3
 
 
+def host_sbvh_build_seconds(mesh) -> dict:
+    """The terrain's SBVH build on the host: the oracle's single-threaded restatement of the
+    reference's builder, and this project's builder (OpenMP subtrees, same bytes)."""
+    from oracle import oracle
+    from trenchanttracer_gb300 import BVHCompact, Scene
+    with tempfile.TemporaryDirectory() as d:
+        oracle_s = oracle.sbvh_build(mesh.vertices, mesh.normals, mesh.vidx, mesh.nidx, mesh.mat,
+                                     Path(d) / "bvh.cache", 1e-5, 1, 8)
+    sc = Scene.from_mesh(mesh)
+    t0 = time.perf_counter()
+    BVHCompact.build(sc, 1e-5, 1, 8)
+    return {"oracle_s": round(oracle_s, 2), "ours_s": round(time.perf_counter() - t0, 3)}
+
+
+def reference_kernel_rates(bvh_arrays: dict, sets: dict, reps: int = 7) -> dict:
+    """The reference's own CUDA intersect() (oracle/_ref/ref_intersect.cubin: the reference source
+    with its one-line ballot shim, one ray per thread, 256 threads per block) on this GB300, same
+    BVH and rays: Mrays/s per ray set, closest and any hit, from the median of `reps` back-to-back
+    launches (CUDA events)."""
+    from oracle import refgpu
+    if not refgpu.available():
+        return {"unavailable": "oracle/_ref/ref_intersect.cubin was not built (the reference checkout is absent)"}
+    out = {}
+    for name, rays in sets.items():
+        for closest in (True, False):
+            r = refgpu.intersect(bvh_arrays, rays, closest, reps=reps)
+            out[f"{name}_{'closest' if closest else 'any'}_mrays"] = round(rays.shape[0] / r["ms"] / 1e3, 1)
+    out["kernel"] = "the reference's intersect() compiled for sm_103a from its own source, one ray per thread"
+    return out
+
+
 def run_reference(args) -> None:
-    """--impl reference: the reference's traversal on the host cores (the oracle port with the
-    reference's plain float arithmetic, OpenMP), on this arm's workload and metric."""
+    """--impl reference: the reference's host path on the host cores, built only from the oracle
+    (no libtt.so): its SBVH build restated single-threaded as the reference runs it (timed once,
+    reported in cpu_baseline) and its traversal with the reference's plain float arithmetic under
+    OpenMP on all host threads (timed per step), on this arm's workload and metric."""
     _, rank, _ = rank_info()
     if rank != 0:
         return
-    from trenchanttracer_gb300 import scenes
     from oracle import oracle
-
-    def host_ext(bvh, rays):
-        o = oracle.intersect(bvh.arrays(), rays, True, arith=oracle.PLAIN, normals=True)
-        return o["t"], o["normal"]
-
-    _, bvh, primary, secondary, _ = workload(host_ext)
-    arr = bvh.arrays()
-    rays = np.concatenate([primary, secondary])
+    w = reference_workload()
+    arr = w["arrays"]
+    rays = np.concatenate([w["primary"], w["secondary"]])
     vals, secs = [], []
     for i in range(args.warmup + args.steps):
         r = cpu_baseline(arr, rays, 1, False)
@@ -249,12 +308,15 @@ def run_reference(args) -> None:
     line = {"impl": "reference", "metric": METRIC, "value": round(v, 3), "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(float(np.median(secs)) * 1e3, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded fBm terrain, seed 7)",
-            "config": {"workload": "terrain ray-cast: 2,097,152 tris, 4M coherent + 4M incoherent closest-hit rays",
-                       "sample_rays_per_step": r["rays"]},
+            "data": "synthetic (seeded fBm terrain, seed 7; rays seeded)",
+            "config": terrain_config(rays.shape[0]),
             "cpu_baseline": {"value": round(v, 3), "unit": UNIT, "cores": cores, "kind": "port", "cpu": cpu_model(),
                              "sample": f"all {r['rays']:,} rays of both sets per step, "
-                                       f"{float(np.median(secs)):.2f} s per step"},
+                                       f"{float(np.median(secs)):.2f} s per step",
+                             "sbvh_build_s": round(w["build_s"], 2),
+                             "sbvh_build": "the reference's SBVH build + compact emission restated in C "
+                                           "(oracle/tt_oracle_sbvh.c, byte-identical bvh.cache), 1 thread "
+                                           "as the reference builds"},
             "e2e": {"value": round(v, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -375,6 +437,8 @@ def run_ours(args) -> None:
         return
     peaks = load_peaks()
     cpu = cpu_baseline(bvh.arrays(), np.concatenate([primary, secondary]), 1, True, min_seconds=10.0)
+    host_build = host_sbvh_build_seconds(mesh)
+    ref_kernel = reference_kernel_rates(bvh.arrays(), {"primary": primary, "incoherent": secondary, "shadow": shadow})
     bpr = bytes_per_ray(cpu["counters"])
     kernel_ms = (np.mean(launch_ms[0]) + np.mean(launch_ms[1])) / 2.0
     achieved = bpr * (n_rays / 2) / (kernel_ms * 1e-3) / 1e9
@@ -384,12 +448,7 @@ def run_ours(args) -> None:
         "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded fBm terrain, seed 7; rays seeded)",
-        "config": {"workload": "terrain ray-cast: 1024x1024-cell heightfield, 2,097,152 tris, world scale 8; "
-                               f"{primary.shape[0]:,} coherent primary + {secondary.shape[0]:,} incoherent rays, "
-                               "closest hit",
-                   "bvh": "compact SBVH, split alpha 1e-5, leaf <= 8", "rays_per_step": n_rays,
-                   "l2": "inputs larger than L2; L2 also flushed (256 MB write) between steps, untimed",
-                   "parallelism": f"replicas x{world}"},
+        "config": terrain_config(n_rays), "parallelism": f"replicas x{world}",
         "per_set": {"primary_mrays": round(sets[0].shape[0] / np.mean(launch_ms[0]) / 1e3, 1),
                     "incoherent_mrays": round(sets[1].shape[0] / np.mean(launch_ms[1]) / 1e3, 1),
                     "primary_hit_fraction": round(float((ids_p >= 0).mean()), 4),
@@ -397,22 +456,35 @@ def run_ours(args) -> None:
         "any_hit": dict(any_hit, light=SHADOW_LIGHT),
         "e2e": {"value": round(e2e_val, 2), "unit": UNIT, "h2d_bytes_per_step": int(n_rays * 32),
                 "d2h_bytes_per_step": int(n_rays * 8)},
-        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
+        "roofline": {"binding": "issue and latency of divergent traversal: DRAM at 6 % of its peak, real L2 traffic "
+                                f"at {TRACE_L2_TRAFFIC_PCT} % of its peak, {TRACE_THREADS_PER_INST} of 32 lanes per "
+                                "instruction (ncu, incoherent launch)",
+                     "l2": {"frac": round(achieved / TRACE_L2_PEAK_GBS, 4), "achieved": round(achieved, 1),
+                            "peak": TRACE_L2_PEAK_GBS, "unit": "GB/s", "l2_traffic_pct_of_peak": TRACE_L2_TRAFFIC_PCT,
+                            "peak_source": "ncu: lts__t_sectors.sum.per_second / lts__t_sectors.sum.pct_of_peak_"
+                                           "sustained_elapsed x 32 B, incoherent trace launch"},
+                     "simd_efficiency": {"frac": round(TRACE_THREADS_PER_INST / 32.0, 4),
+                                         "threads_per_instruction": TRACE_THREADS_PER_INST,
+                                         "source": "ncu smsp__thread_inst_executed_per_inst_executed, incoherent "
+                                                   "trace launch (profiles/trace_kernel_terrain_closest.md)"},
+                     "bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": TRACE_DRAM_BYTES_PER_LAUNCH,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per trace launch of this "
                                        "workload (mean of the primary and incoherent launches)",
                      "peak_source": f"{peaks['source']} hbm_gbs (MEASURED_PEAKS.json)" if peaks["source"] == "measured"
                      else "fallback 6.8 TB/s", "bytes_per_ray": round(bpr, 1),
-                     "kernel": "tt_trace: ray ordering + trace_warp_kernel<closest> (avg per ray set)", "avg_launch_ms": round(float(kernel_ms), 4),
-                     "l2": {"achieved": round(achieved, 1), "peak": TRACE_L2_PEAK_GBS, "unit": "GB/s",
-                            "frac": round(achieved / TRACE_L2_PEAK_GBS, 4),
-                            "l2_traffic_pct_of_peak": TRACE_L2_TRAFFIC_PCT,
-                            "peak_source": "ncu: lts__t_sectors.sum.per_second / lts__t_sectors.sum.pct_of_peak_"
-                                           "sustained_elapsed x 32 B, incoherent trace launch"}},
+                     "kernel": "tt_trace: ray ordering + trace_warp_kernel<closest> (avg per ray set)",
+                     "avg_launch_ms": round(float(kernel_ms), 4)},
+        "ref_kernel": ref_kernel,
         "cpu_baseline": {"value": round(cpu["mrays"], 3), "unit": UNIT, "cores": cpu["threads"], "kind": "port",
                          "cpu": cpu_model(),
                          "sample": f"all {cpu['rays']:,} rays of both sets, {cpu['passes']} passes, "
-                                   f"{cpu['seconds']:.1f} s"},
+                                   f"{cpu['seconds']:.1f} s",
+                         "sbvh_build_s": host_build["oracle_s"],
+                         "sbvh_build": "the reference's SBVH build + compact emission restated in C "
+                                       "(oracle/tt_oracle_sbvh.c, byte-identical bvh.cache), 1 thread as the "
+                                       "reference builds",
+                         "sbvh_build_s_ours": host_build["ours_s"]},
         "clocks": clocks,
         "gpu_launches": 2 * args.steps * trace_call_launches(dbvh),
     }

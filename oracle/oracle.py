@@ -13,7 +13,8 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 SRC = HERE / "tt_oracle_pt.c"  # includes tt_oracle.c
-SRCS = [HERE / "tt_oracle.c", SRC]
+SBVH_SRC = HERE / "tt_oracle_sbvh.c"
+SRCS = [HERE / "tt_oracle.c", SRC, SBVH_SRC]
 LIB = HERE / "_build" / "liboracle.so"
 
 SLAB_FMA, CROSS_A, CROSS_B, DOT_A, DOT_B, INTERP_A, INTERP_B = 1, 2, 4, 8, 16, 32, 64
@@ -33,8 +34,8 @@ def build(force: bool = False) -> Path:
         return LIB
     LIB.parent.mkdir(exist_ok=True)
     tmp = LIB.with_suffix(".so.tmp")
-    cmd = ["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", str(SRC), "-o", str(tmp),
-           "-lm"]
+    cmd = ["gcc", "-O2", "-std=c11", "-D_POSIX_C_SOURCE=199309L", "-fPIC", "-shared", "-fopenmp",
+           "-ffp-contract=off", str(SRC), str(SBVH_SRC), "-o", str(tmp), "-lm"]
     proc = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
     if proc.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + proc.stdout)
@@ -50,6 +51,10 @@ def _load():
         h.oracle_intersect.restype = C.c_int64
         h.oracle_intersect.argtypes = [C.c_void_p] * 5 + [C.c_void_p, C.c_int64, C.c_int, C.c_int] + \
             [C.c_void_p] * 5 + [C.c_int]
+        h.oracle_sbvh_build.restype = C.c_int
+        h.oracle_sbvh_build.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                        C.c_int, C.c_float, C.c_int, C.c_int, C.c_char_p,
+                                        C.POINTER(C.c_double)]
         h.oracle_max_threads.restype = C.c_int
         h.oracle_wang_hash.restype = C.c_uint32
         h.oracle_wang_hash.argtypes = [C.c_uint32]
@@ -116,6 +121,26 @@ def intersect(bvh_arrays: dict, rays: np.ndarray, closest: bool, arith: int = DE
                                   out["counters"].ctypes.data if counters else None, threads)
     out["overflow"] = int(ov)
     return out
+
+
+def sbvh_build(vertices: np.ndarray, normals: np.ndarray, vidx: np.ndarray, nidx: np.ndarray, mat: np.ndarray | None,
+               cache_path: str | Path, split_alpha: float = 1e-5, leaf_min: int = 1,
+               leaf_max: int = 0x7FFFFFF) -> float:
+    """The reference's SBVH build and compact emission restated in C (tt_oracle_sbvh.c), single
+    threaded as the reference runs it: writes bvh.cache to cache_path (read it with read_cache)
+    and returns the build + emission time in seconds."""
+    v = np.ascontiguousarray(vertices, np.float32)
+    n = np.ascontiguousarray(normals, np.float32)
+    vi = np.ascontiguousarray(vidx, np.int32)
+    ni = np.ascontiguousarray(nidx, np.int32)
+    m = None if mat is None else np.ascontiguousarray(mat, np.uint32)
+    secs = C.c_double(0.0)
+    rc = _load().oracle_sbvh_build(v.ctypes.data, v.size // 3, n.ctypes.data, n.size // 3, vi.ctypes.data,
+                                   ni.ctypes.data, None if m is None else m.ctypes.data, vi.size // 3,
+                                   split_alpha, leaf_min, leaf_max, str(cache_path).encode(), C.byref(secs))
+    if rc != 0:
+        raise RuntimeError(f"oracle SBVH build failed ({rc})")
+    return float(secs.value)
 
 
 def max_threads() -> int:

@@ -37,6 +37,27 @@ def test_bvh_cache_matches_reference_builder(name, leaf_max, golden, golden_scen
 
 
 @pytest.mark.parametrize("name", ["ico3", "terrain64", "cornell4", "mixed"])
+@pytest.mark.parametrize("leaf_max", golden_scenes.LEAF_MAX)
+def test_oracle_sbvh_matches_reference_builder(name, leaf_max, golden, golden_scene_files, tmp_path):
+    """The oracle's own SBVH restatement (oracle/tt_oracle_sbvh.c, the host build bench.py's
+    reference arm times) writes the reference builder's bvh.cache byte for byte."""
+    a = Scene.load_json(golden_scene_files[name]).arrays()
+    out = tmp_path / "oracle.cache"
+    oracle.sbvh_build(a["vertices"], a["normals"], a["vidx"], a["nidx"], a["mat"], out, 1e-5, 1, leaf_max)
+    ref = golden[name][str(leaf_max)]
+    assert list(oracle.read_cache(out)["header"].values()) == ref["header"]
+    assert sha(out) == ref["sha256"]
+
+
+def test_oracle_sbvh_matches_product_builder_on_a_larger_terrain(tmp_path):
+    sc = Scene.from_mesh(scenes.terrain(96, 8.0, seed=11))
+    a = sc.arrays()
+    oracle.sbvh_build(a["vertices"], a["normals"], a["vidx"], a["nidx"], a["mat"], tmp_path / "o.cache", 1e-5, 1, 8)
+    BVHCompact.build(sc, 1e-5, 1, 8).save(tmp_path / "p.cache")
+    assert sha(tmp_path / "o.cache") == sha(tmp_path / "p.cache")
+
+
+@pytest.mark.parametrize("name", ["ico3", "terrain64", "cornell4", "mixed"])
 def test_scene_ingest_matches_reference_loader(name, golden, golden_scene_files):
     a = Scene.load_json(golden_scene_files[name]).arrays()
     digest = hashlib.sha256(b"".join(np.ascontiguousarray(a[k]).tobytes()
