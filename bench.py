@@ -64,11 +64,11 @@ L2_FLUSH_BYTES = 256 << 20
 # ordering kernels around them add 8 MB (primary: the probe only) and 523 MB (incoherent: probe,
 # keys, scan, ordered copy, hit gather). bench.py cannot run ncu itself.
 TRACE_DRAM_BYTES_PER_LAUNCH = 311_000_000
-# L2 of the same GB300 from one ncu capture of the incoherent trace launch: 95.84 sectors/ns were
-# 8.43 % of the sustained peak, i.e. 1,136.5 sectors/ns x 32 B; the launch's own L2 traffic was
-# that 8.4 % of it
+# L2 of the same GB300 from one ncu capture of the incoherent trace launch (1M rays, the current
+# 10-block build): 74.89 sectors/ns were 6.59 % of the sustained peak, i.e. 1,136 sectors/ns x 32 B;
+# the launch's own L2 traffic was that 6.6 % of it
 TRACE_L2_PEAK_GBS = 36_370.0
-TRACE_L2_TRAFFIC_PCT = 8.4
+TRACE_L2_TRAFFIC_PCT = 6.6
 
 
 def load_peaks() -> dict:
@@ -81,7 +81,7 @@ def load_peaks() -> dict:
 
 # the SIMD efficiency and the L2 figures of the trace kernel from the same committed ncu capture
 # (profiles/trace_kernel_terrain_closest.md, incoherent launch): threads per executed instruction
-TRACE_THREADS_PER_INST = 9.74
+TRACE_THREADS_PER_INST = 9.06
 
 
 def terrain_config(n_rays: int) -> dict:
@@ -456,9 +456,9 @@ def run_ours(args) -> None:
         "any_hit": dict(any_hit, light=SHADOW_LIGHT),
         "e2e": {"value": round(e2e_val, 2), "unit": UNIT, "h2d_bytes_per_step": int(n_rays * 32),
                 "d2h_bytes_per_step": int(n_rays * 8)},
-        "roofline": {"binding": "issue and latency of divergent traversal: DRAM at 6 % of its peak, real L2 traffic "
-                                f"at {TRACE_L2_TRAFFIC_PCT} % of its peak, {TRACE_THREADS_PER_INST} of 32 lanes per "
-                                "instruction (ncu, incoherent launch)",
+        "roofline": {"binding": "issue and latency of divergent traversal: DRAM at 4 % of its peak, real L2 traffic "
+                                f"at {TRACE_L2_TRAFFIC_PCT} % of its peak, issue on 59 % of cycles with "
+                                f"{TRACE_THREADS_PER_INST} of 32 lanes per instruction (ncu, incoherent launch)",
                      "l2": {"frac": round(achieved / TRACE_L2_PEAK_GBS, 4), "achieved": round(achieved, 1),
                             "peak": TRACE_L2_PEAK_GBS, "unit": "GB/s", "l2_traffic_pct_of_peak": TRACE_L2_TRAFFIC_PCT,
                             "peak_source": "ncu: lts__t_sectors.sum.per_second / lts__t_sectors.sum.pct_of_peak_"
