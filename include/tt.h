@@ -343,6 +343,35 @@ tt_status tt_render_params_default(tt_render_params *out);
  * shape. Launch only; deterministic for given inputs. */
 tt_status tt_render_native(tt_renderer *renderer, const tt_camera_meta *cam, const tt_render_params *params,
                            void *d_accum, void *stream);
+/* One query of tt_native_sample_probe (160 bytes): the inputs, then what the native renderer's
+ * own device code returned for them. */
+typedef struct tt_sample_probe {
+    /* in */
+    int32_t material;    /* what 0: index into the scene's materials */
+    int32_t entering;    /* what 0: 1 when wo is on the side the normal points to (dielectrics) */
+    float n[3], wo[3];   /* what 0: unit normal facing wo, unit direction towards the viewer */
+    float u[3];          /* uniform numbers in [0, 1) the sampler consumes */
+    int32_t pad0;
+    uint64_t pcg_state, pcg_seq; /* what 2: pcg32_srandom_r(initstate, initseq) */
+    /* out */
+    float wi[3];         /* sampled direction (what 0, 1) */
+    float weight[3];     /* what 0: f |cos| / pdf; what 1: the environment radiance */
+    float pdf;           /* solid-angle pdf of the sample (0: a specular choice or no sample) */
+    float eval_pdf;      /* what 0: the pdf bsdf_eval gives for wi; what 1: env_pdf of wi */
+    float eval[3];       /* what 0: f |cos| that bsdf_eval gives for wi */
+    int32_t specular;
+    uint32_t pcg_out[8]; /* what 2: the stream's first eight outputs */
+    int32_t pad1[4];
+} tt_sample_probe;
+/* Diagnostic (no counterpart in the reference, whose samplers are other ones): runs the native
+ * path tracer's own sampling code on n device queries. what 0: the BSDF sampler of the query's
+ * material (Lambert, GGX conductor, dielectric, Spec, Coat) and bsdf_eval at the sampled
+ * direction; what 1: the environment map's 2D-CDF sampler with u[0], u[1] and env_pdf at the
+ * sampled direction (the scene must have an environment); what 2: the PCG32 generator the
+ * renderer's paths draw from. Lets tests check the samplers' distributions against their stated
+ * densities. Launch only. */
+tt_status tt_native_sample_probe(const tt_renderer *renderer, int32_t what, tt_sample_probe *d_queries, int64_t n,
+                                 void *stream);
 /* The environment's sampling tables built by tt_renderer_create: marginal CDF (env_h + 1 floats)
  * and conditional CDFs (env_h * (env_w + 1) floats), copied to host buffers (either may be
  * NULL). */

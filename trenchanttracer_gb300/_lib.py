@@ -129,6 +129,7 @@ SIGNATURES = {
     "tt_render_compat": (I32, [P, C.POINTER(CameraMeta), C.POINTER(RenderMeta), P, P]),
     "tt_renderer_check": (I32, [P, P]),
     "tt_compat_replay": (I32, [P, C.POINTER(CameraMeta), C.POINTER(RenderMeta), P, I64, P, P]),
+    "tt_native_sample_probe": (I32, [P, I32, P, I64, P]),
     "tt_render_params_default": (I32, [C.POINTER(RenderParams)]),
     "tt_render_native": (I32, [P, C.POINTER(CameraMeta), C.POINTER(RenderParams), P, P]),
     "tt_renderer_env_tables": (I32, [P, P, P]),

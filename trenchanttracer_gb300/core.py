@@ -294,6 +294,25 @@ class Renderer:
                                      int(records_in.shape[0]), C.c_void_p(records_out.data_ptr()),
                                      C.c_void_p(stream)))
 
+    # numpy layout of tt_sample_probe (160 bytes)
+    SAMPLE_PROBE_DTYPE = np.dtype([("material", "<i4"), ("entering", "<i4"), ("n", "<f4", 3), ("wo", "<f4", 3),
+                                   ("u", "<f4", 3), ("pad0", "<i4"), ("pcg_state", "<u8"), ("pcg_seq", "<u8"),
+                                   ("wi", "<f4", 3), ("weight", "<f4", 3), ("pdf", "<f4"), ("eval_pdf", "<f4"),
+                                   ("eval", "<f4", 3), ("specular", "<i4"), ("pcg_out", "<u4", 8),
+                                   ("pad1", "<i4", 4)])
+    PROBE_BSDF, PROBE_ENV, PROBE_PCG32 = 0, 1, 2
+
+    def sample_probe(self, what: int, queries: np.ndarray, stream: int = 0) -> np.ndarray:
+        """Runs the native renderer's sampling code on host queries (SAMPLE_PROBE_DTYPE records)
+        on the GPU and returns the filled records (tt_native_sample_probe)."""
+        import torch
+        q = np.ascontiguousarray(queries, dtype=self.SAMPLE_PROBE_DTYPE)
+        d = torch.from_numpy(q.view(np.uint8).copy()).cuda()
+        check(lib().tt_native_sample_probe(self._h, int(what), C.c_void_p(d.data_ptr()), int(q.shape[0]),
+                                           C.c_void_p(stream)))
+        torch.cuda.synchronize()
+        return d.cpu().numpy().view(self.SAMPLE_PROBE_DTYPE).copy()
+
     def render_native(self, cam: _lib.CameraMeta, params: _lib.RenderParams, accum, stream: int = 0) -> None:
         """Native wavefront path tracer: adds spp samples per pixel to accum (CUDA tensor W*H*3,
         float32, or float64 with the RENDER_ACCUM_F64 flag; row 0 = top)."""

@@ -677,6 +677,41 @@ __global__ void __launch_bounds__(kShadeBlockMax) k_accumulate(NativeArgs a, T *
 
 }  // namespace tt
 
+// ---- sampling probe (tt_native_sample_probe) ------------------------------------------------------
+namespace tt {
+__global__ void k_sample_probe(const MaterialRec *materials, int num_materials, EnvView env, int what,
+                               tt_sample_probe *q, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        tt_sample_probe r = q[i];
+        if (what == 2) {
+            Rng g = pcg32_seed(r.pcg_state, r.pcg_seq);
+            for (int k = 0; k < 8; k++) r.pcg_out[k] = pcg32(g);
+        } else if (what == 1) {
+            V3 dir(0.f, 0.f, 0.f), le(0.f, 0.f, 0.f);
+            r.pdf = env.w > 0 ? env_sample(env, r.u[0], r.u[1], dir, le) : 0.0f;
+            st3(r.wi, dir);
+            st3(r.weight, le);
+            const float st = PT_SQRT(fmaxf(0.0f, PT_FMA(-dir.y, dir.y, 1.0f)));
+            r.eval_pdf = r.pdf > 0.0f ? env_pdf(env, env_texel(env, dir), st) : 0.0f;
+        } else if (r.material >= 0 && r.material < num_materials) {
+            const MaterialRec m = materials[r.material];
+            const V3 nn = ld3(r.n), wo = ld3(r.wo);
+            const BsdfSample s = bsdf_sample(m, nn, wo, r.entering != 0, r.u[0], r.u[1], r.u[2]);
+            st3(r.wi, s.wi);
+            st3(r.weight, s.weight);
+            r.pdf = s.pdf;
+            r.specular = s.specular ? 1 : 0;
+            float ep = 0.0f;
+            V3 ev(0.f, 0.f, 0.f);
+            if (m.kind == MAT_DIFF || m.kind == MAT_GGX) ev = bsdf_eval(m, nn, wo, s.wi, ep);
+            st3(r.eval, ev);
+            r.eval_pdf = ep;
+        }
+        q[i] = r;
+    }
+}
+}  // namespace tt
+
 // ---- environment sampling tables (FP64 prefix sums) ----------------------------------------------
 namespace tt {
 
@@ -1461,6 +1496,27 @@ tt_status tt_batch_free(tt_batch *b) {
     if (b->d_views) cudaFree(b->d_views);
     if (b->cap) cudaStreamDestroy(b->cap);
     delete b;
+    return TT_OK;
+}
+
+tt_status tt_native_sample_probe(const tt_renderer *r, int32_t what, tt_sample_probe *d_q, int64_t n, void *stream) {
+    static_assert(sizeof(tt_sample_probe) == 160, "tt_sample_probe is 160 bytes");
+    if (!r || (n > 0 && !d_q)) return fail(TT_ERR_INVALID, "null argument");
+    if (what < 0 || what > 2) return fail(TT_ERR_INVALID, "what must be 0 (BSDF), 1 (environment) or 2 (PCG32)");
+    if (what == 1 && r->env_w <= 0) return fail(TT_ERR_INVALID, "the scene has no environment map");
+    if (n < 0) return fail(TT_ERR_INVALID, "negative query count");
+    if (n == 0) return TT_OK;
+    EnvView env{};
+    env.tex = r->env;
+    env.marg = r->env_marg;
+    env.cond = r->env_cond;
+    env.w = r->env_w;
+    env.h = r->env_h;
+    env.scale = 1.0f;
+    const long long blocks = std::min<long long>((n + 255) / 256, 152ll * 16);
+    k_sample_probe<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(r->materials, r->num_materials, env, what, d_q,
+                                                                       (long long)n);
+    TT_CUDA_N(cudaGetLastError());
     return TT_OK;
 }
 
