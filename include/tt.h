@@ -235,6 +235,11 @@ tt_status tt_dbvh_check(const tt_dbvh *bvh, void *stream);
  * A caller may sort its rays by these keys on the host to trace them coherently. */
 tt_status tt_ray_order_keys(const tt_ray *rays, int64_t n, const float lo[3], const float hi[3], uint32_t *keys,
                             int32_t *key_bits);
+/* The same keys computed on the device by the ordering kernels' own key function, for n device
+ * rays (16-byte aligned) into d_keys; no counterpart in the reference. Launch only. A check that
+ * the host keys above are the device's, bit for bit. */
+tt_status tt_ray_order_keys_device(const tt_ray *d_rays, int64_t n, const float lo[3], const float hi[3],
+                                   uint32_t *d_keys, int32_t *key_bits, void *stream);
 
 /* Allocation-free tracing with HOST ray and hit buffers. No counterpart in the reference: it is
  * an addition for callers that cannot allocate device memory, such as a host application whose
@@ -243,8 +248,12 @@ tt_status tt_ray_order_keys(const tt_ray *rays, int64_t n, const float lo[3], co
  * cudaMalloc can cause. tt_trace_host allocates its device staging on first use and whenever a
  * call needs more; this entry point never allocates (no cudaMalloc, cudaFree or allocating
  * library call). Ray and hit staging, the work counter and the error word live in one fixed
- * ~10 MiB array inside libtt.so that every GPU loading the library holds until the process
- * exits.
+ * ~10 MiB array inside libtt.so. The array is reserved on a device when the library's device
+ * code is first loaded there (CUDA loads modules lazily by default: at the first libtt call that
+ * uses the device) and is held until the process exits, so a caller whose arena will take all
+ * device memory makes a warm-up call on each device before its arena grows: with n = 0 this
+ * entry point only loads the library's device code on the current device (reserving the array)
+ * and looks up the array's address, and returns TT_OK, or the CUDA error if that fails.
  *   d_nodes, d_vertices, d_tri_indices  the caller's device copies of the compact BVH arrays
  *                                       (the layout of tt_bvh_arrays / bvh.cache); 16-, 16- and
  *                                       4-byte aligned
@@ -252,8 +261,8 @@ tt_status tt_ray_order_keys(const tt_ray *rays, int64_t n, const float lo[3], co
  *                                       rejected with TT_ERR_INVALID and a message
  * Results are those of tt_trace_host with the default kernel variant. The stream is
  * synchronised before returning. The first call on each device also looks up the device address
- * of the staging array; make that first call before any stream capture. All calls share the one
- * array: calls that overlap on the GPU (other host threads, other streams) race. */
+ * of the staging array; make that first call (the warm-up) before any stream capture. All calls
+ * share the one array: calls that overlap on the GPU (other host threads, other streams) race. */
 /* ---- camera and frame metadata (host) ---------------------------------------------------- */
 /* Camera(config) + Camera::setFovx(fovx) + Camera::getCameraMeta() for the scene's camera block
  * (src/core/Camera.cpp:12-44, :115-140; the reference's main uses fovx = 45). */

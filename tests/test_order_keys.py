@@ -153,3 +153,31 @@ def test_terrain_box_gives_the_longest_sides_most_origin_bits():
     got, _ = ray_order_keys(rays, lo, hi)
     ref, _ = keys_np(rays, lo, hi)
     assert np.array_equal(got, ref)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n", [3000, 1 << 16, 1 << 22])
+def test_device_keys_equal_host_keys(n):
+    """The ordering kernels' key function on the GPU (tt_ray_order_keys_device) gives the host
+    keys bit for bit, edge directions and origins included, for key widths 6 + 8 to 13 + 8."""
+    import ctypes as C
+    torch = pytest.importorskip("torch")
+    from trenchanttracer_gb300 import _lib
+    lo, hi = [-2.0, -1.0, -2.5], [2.0, 1.5, 2.0]
+    d = [(0, 0, 0), (1, 0, 0), (-1, 0, 0), (0, -1, 0), (0, 0, -1), (-1, -1, -1), (np.nan, 1, 0), (np.inf, 0, 0),
+         (1e-30, -1e-30, 1e-30), (3e38, 3e38, 0), (-0.0, -0.0, 1), (0.125, 0.75, -0.125)]
+    o = [(0, 0, 0), (-2, -1, -2.5), (2, 1.5, 2), (np.nan, 0, 0), (1e30, -1e30, 0), (1.999999, 1.4999, 1.999)]
+    edge = np.array([[*oo, *dd, 0.0, 1e30] for oo in o for dd in d], F)
+    rays = random_rays(n, 11)
+    rays[:edge.shape[0]] = edge
+    host, bits = ray_order_keys(rays, lo, hi)
+    dr = torch.from_numpy(rays).cuda()
+    dk = torch.empty(n, dtype=torch.int32, device="cuda")
+    lo_a, hi_a = np.array(lo, F), np.array(hi, F)
+    dbits = C.c_int32()
+    _lib.check(_lib.lib().tt_ray_order_keys_device(C.c_void_p(dr.data_ptr()), n, C.c_void_p(lo_a.ctypes.data),
+                                                    C.c_void_p(hi_a.ctypes.data), C.c_void_p(dk.data_ptr()),
+                                                    C.byref(dbits), None))
+    torch.cuda.synchronize()
+    assert dbits.value == bits
+    assert np.array_equal(dk.cpu().numpy().view(np.uint32), host)

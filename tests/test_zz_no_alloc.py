@@ -6,6 +6,7 @@ their own memory and trace through this entry point, which stages rays and hits 
 inside libtt.so. This file is collected last so that a failure here does not hide any other test.
 """
 import ctypes as C
+import struct
 
 import numpy as np
 import pytest
@@ -56,3 +57,49 @@ def test_noalloc_rejects_oversized_batches():
                                           1, None)
     assert st == 1  # TT_ERR_INVALID
     assert b"staging capacity" in _lib.lib().tt_last_error_string()
+
+
+def _self_loop_arrays(child1_box_empty: bool):
+    """A corrupt BVH whose root lists itself as both children (the one the trace tests use):
+    child 1 far from every ray makes a ray loop without pushing (the iteration cap), child 1 over
+    the rays makes it push until the stack bound."""
+    big = 1e3
+    c1lo, c1hi = (1e6, 1e6 + 1.0) if child1_box_empty else (-big, big)
+    nodes = np.zeros((4, 4), np.float32)
+    nodes[0] = [-big, big, -big, big]
+    nodes[1] = [c1lo, c1hi, c1lo, c1hi]
+    nodes[2] = [-big, big, c1lo, c1hi]
+    nodes.view(np.int32)[3] = [0, 0, 0, 0]
+    verts = np.array([[0x80000000, 0, 0, 0]], np.uint32).view(np.int32)
+    return (torch.from_numpy(nodes.view(np.int32).copy()).cuda(), torch.from_numpy(verts.copy()).cuda(),
+            torch.zeros(1, dtype=torch.int32, device="cuda"))
+
+
+@pytest.mark.parametrize("child1_empty,status,word", [(True, 4, b"iteration cap"), (False, 5, b"stack")])
+def test_noalloc_reports_traversal_errors_then_starts_clean(child1_empty, status, word):
+    """The error word lives in the shared array's header: a corrupt BVH's error reaches the
+    caller as a status and message, and the next call on a valid BVH starts from a clean word."""
+    rays = scenes.random_rays(64, 3, [-1] * 3, [1] * 3)
+    hits = np.zeros((64, 2), np.int32)
+    bad = _self_loop_arrays(child1_empty)
+    st = _lib.lib().tt_trace_host_noalloc(C.c_void_p(bad[0].data_ptr()), C.c_void_p(bad[1].data_ptr()),
+                                          C.c_void_p(bad[2].data_ptr()), C.c_void_p(rays.ctypes.data), 64,
+                                          C.c_void_p(hits.ctypes.data), 1, None)
+    assert st == status  # 4 = TT_ERR_TIMEOUT (iteration cap), 5 = TT_ERR_BOUNDS (stack)
+    assert word in _lib.lib().tt_last_error_string()
+    mesh = scenes.terrain(32, 8.0, seed=2)
+    bvh = BVHCompact.build(Scene.from_mesh(mesh), 1e-5, 1, 8)
+    a = bvh.arrays()
+    dev = (torch.from_numpy(a["nodes"]).cuda(), torch.from_numpy(a["vertices"]).cuda(),
+           torch.from_numpy(a["tri_indices"]).cuda())
+    good = scenes.random_rays(4096, 9, [-9.0, -2.0, -9.0], [9.0, 4.0, 9.0])
+    want = np.empty((good.shape[0], 2), np.int32)
+    DeviceBVH(bvh).intersect_host(good, want, closest=True)
+    assert np.array_equal(_noalloc(dev, good, True), want)
+
+
+def test_noalloc_warm_up_call():
+    """n = 0 loads the library's device code on the current device (reserving the staging array)
+    and returns TT_OK: what a caller does before its own arena takes the device's memory."""
+    torch.cuda.init()
+    assert _lib.lib().tt_trace_host_noalloc(None, None, None, None, 0, None, 1, None) == 0

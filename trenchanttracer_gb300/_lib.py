@@ -119,6 +119,7 @@ SIGNATURES = {
     "tt_trace_ext": (I32, [P, P, I64, P, I32, P]),
     "tt_trace_host": (I32, [P, P, I64, P, I32, P]),
     "tt_ray_order_keys": (I32, [P, I64, P, P, P, P]),
+    "tt_ray_order_keys_device": (I32, [P, I64, P, P, P, P, P]),
     "tt_dbvh_check": (I32, [P, P]),
     "tt_trace_host_noalloc": (I32, [P, P, P, P, I64, P, I32, P]),
     "tt_camera_meta_from_scene": (I32, [P, F32, C.POINTER(CameraMeta)]),

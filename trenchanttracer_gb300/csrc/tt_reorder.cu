@@ -24,6 +24,7 @@
 // overlapping them.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <string>
@@ -390,7 +391,33 @@ tt_status reorder_unpermute(const OrderOut &out, int64_t n, void *hits, size_t h
     return TT_OK;
 }
 
+// tt_ray_order_keys_device: the key of every ray, as the ordering kernels compute it
+__global__ void __launch_bounds__(kOrderBlock) k_order_keys_only(const float4 *rays, int64_t n, OrderGrid g,
+                                                                unsigned *keys) {
+    for (int64_t i = (int64_t)blockIdx.x * kOrderBlock + threadIdx.x; i < n; i += (int64_t)gridDim.x * kOrderBlock)
+        keys[i] = order_key(__ldg(rays + 2 * i), __ldg(rays + 2 * i + 1), g);
+}
+
 }  // namespace tt
+
+extern "C" tt_status tt_ray_order_keys_device(const tt_ray *d_rays, int64_t n, const float lo[3], const float hi[3],
+                                              uint32_t *d_keys, int32_t *key_bits, void *stream) {
+    if (n < 0 || n >= ((int64_t)1 << 31)) return tt::fail(TT_ERR_INVALID, "tt_ray_order_keys_device: n out of range");
+    if (!lo || !hi || !key_bits || (n > 0 && (!d_rays || !d_keys)))
+        return tt::fail(TT_ERR_INVALID, "tt_ray_order_keys_device: null argument");
+    if (reinterpret_cast<uintptr_t>(d_rays) & 15)
+        return tt::fail(TT_ERR_INVALID, "tt_ray_order_keys_device: rays must be 16-byte aligned");
+    const int ob = tt::order_origin_bits(n);
+    *key_bits = tt::kOrderDirBits + ob;
+    if (n == 0) return TT_OK;
+    const tt::OrderGrid g = tt::order_grid(lo, hi, ob);
+    const int64_t blocks = std::min<int64_t>((n + tt::kOrderBlock - 1) / tt::kOrderBlock, 152 * 8);
+    tt::k_order_keys_only<<<(unsigned)blocks, tt::kOrderBlock, 0, (cudaStream_t)stream>>>(
+        reinterpret_cast<const float4 *>(d_rays), n, g, d_keys);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return tt::fail(TT_ERR_CUDA, std::string("tt_ray_order_keys_device: ") + cudaGetErrorString(e));
+    return TT_OK;
+}
 
 extern "C" tt_status tt_ray_order_keys(const tt_ray *rays, int64_t n, const float lo[3], const float hi[3],
                                        uint32_t *keys, int32_t *key_bits) {

@@ -424,7 +424,9 @@ static tt_status read_error_word(const DeviceBVH &d, cudaStream_t stream) {
 // ---- allocation-free host-buffer tracing ----------------------------------------------------------
 // A fixed staging area for tt_trace_host_noalloc: a 256-byte header (64-bit work counter, 32-bit
 // error word) followed by room for kNoAllocMaxRays rays (32 B each) and their hits (8 B each),
-// about 10 MiB in all. Every GPU that loads this library holds it until the process exits.
+// about 10 MiB in all. It is reserved on a GPU when this library's module is loaded there (with
+// CUDA's lazy loading, at the first call that runs libtt code on that GPU) and held until the
+// process exits.
 constexpr int64_t kNoAllocMaxRays = 1 << 18;
 constexpr size_t kNoAllocHeader = 256;
 constexpr size_t kNoAllocBytes = kNoAllocHeader + (size_t)kNoAllocMaxRays * (32 + 8);
@@ -453,6 +455,8 @@ static tt_status noalloc_setup(NoAllocDevice &out) {
         if (e != cudaSuccess || !p) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
         int sms = 0, bps = 0;
         TT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        // one launch size for closest and any hit: the kernels claim rays from a counter, so the
+        // grid only needs to fill the SMs, and the closest-hit build has the larger register count
         TT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kernel_for<true, false>(VARIANT_WARP_SH16),
                                                               kTraceBlock, 0));
         d.num_sms = sms;
@@ -680,14 +684,14 @@ tt_status tt_trace_host_noalloc(const void *d_nodes, const void *d_vertices, con
                                         " rays exceed the allocation-free staging capacity of " +
                                         std::to_string(kNoAllocMaxRays) +
                                         " rays per call; split the batch (or use tt_trace_host)");
-    if (n == 0) return TT_OK;
+    NoAllocDevice nd;
+    if (n == 0) return noalloc_setup(nd);  // a warm-up: loads this library's device code here
     if (!d_nodes || !d_vertices || !d_tri_indices || !h_rays || !h_hits)
         return fail(TT_ERR_INVALID, "tt_trace_host_noalloc: null argument");
     if ((reinterpret_cast<uintptr_t>(d_nodes) & 15) || (reinterpret_cast<uintptr_t>(d_vertices) & 15) ||
         (reinterpret_cast<uintptr_t>(d_tri_indices) & 3))
         return fail(TT_ERR_INVALID, "tt_trace_host_noalloc: BVH arrays must be 16-byte (nodes, vertices) and "
                                     "4-byte (triangle indices) aligned");
-    NoAllocDevice nd;
     tt_status st = noalloc_setup(nd);
     if (st != TT_OK) return st;
     DeviceBVH d;  // a view only: nothing here is owned or freed
