@@ -199,6 +199,11 @@ void tt_dbvh_free(tt_dbvh *dbvh);
 #define TT_VARIANT_SORTED_OCC 7
 #define TT_NUM_VARIANTS 8
 tt_status tt_dbvh_set_variant(tt_dbvh *bvh, int32_t variant);
+/* How many bytes of the node array's top levels the trace launches keep persisting in L2 (an
+ * access-policy window over the start of the array, where tt_bvh_upload lays the tree's top
+ * levels out breadth first; the persisting set-aside is a limit of the calling process's
+ * context). 0 = no window. No counterpart in the reference. */
+tt_status tt_dbvh_set_l2_window(tt_dbvh *bvh, int64_t bytes);
 tt_status tt_dbvh_get_variant(const tt_dbvh *bvh, int32_t *variant);
 /* Autotuner: traces the n device rays with every variant (the warp-vote one only when
  * include_vote != 0), three launches each, keeps the fastest for `bvh` and writes each

@@ -286,7 +286,8 @@ def test_environment_sampling_follows_luminance_times_sin_theta(renderer):
     assert p > 1e-4
     # the stated solid-angle pdf: p(texel) w h / (2 pi^2 sin(theta)) at the sample's own theta
     sin_theta = np.sqrt(np.maximum(0.0, 1.0 - d[:, 1] ** 2))
-    ref = p_texel[y, x] * w * h / (2 * math.pi ** 2 * sin_theta)
+    with np.errstate(divide="ignore"):
+        ref = p_texel[y, x] * w * h / (2 * math.pi ** 2 * sin_theta)
     big = p_texel[y, x] > 1e-7
     assert np.median(np.abs(out["pdf"][big] / ref[big] - 1.0)) < 3e-4  # float CDF entries: ~1e-4
     assert np.quantile(np.abs(out["pdf"][big] / ref[big] - 1.0), 0.999) < 1e-2

@@ -113,6 +113,7 @@ SIGNATURES = {
     "tt_bvh_upload": (I32, [P, C.POINTER(P)]),
     "tt_dbvh_free": (None, [P]),
     "tt_dbvh_set_variant": (I32, [P, I32]),
+    "tt_dbvh_set_l2_window": (I32, [P, I64]),
     "tt_dbvh_get_variant": (I32, [P, C.POINTER(I32)]),
     "tt_dbvh_autotune": (I32, [P, P, I64, P, I32, I32, P, P]),
     "tt_trace": (I32, [P, P, I64, P, I32, P]),

@@ -217,6 +217,10 @@ class DeviceBVH:
     NUM_VARIANTS = 8
     DETERMINISTIC_VARIANTS = (0, 1, 2, 3, 5, 6, 7)
 
+    def set_l2_window(self, nbytes: int) -> None:
+        """Bytes of the node array's top levels kept persisting in L2 (tt_dbvh_set_l2_window)."""
+        check(lib().tt_dbvh_set_l2_window(self._h, int(nbytes)))
+
     def set_variant(self, variant: int) -> None:
         """Kernel shape of the traversal calls (include/tt.h, tt_dbvh_set_variant)."""
         check(lib().tt_dbvh_set_variant(self._h, int(variant)))

@@ -56,6 +56,10 @@ constexpr int kOccBlocks = 12;  // resident blocks per SM the *_OCC variants are
 // resident blocks per SM the default (ordered) variant is compiled for: 48 registers, 8 bytes
 // spilled; against 8 blocks at 61 registers it traces the terrain sets 4 % faster (9: 2 %)
 constexpr int kSortedBlocks = 10;
+// the node array's top levels laid out first at upload (bytes), and the default L2 persisting
+// window of the trace launches over them
+constexpr size_t kL2TopRegion = 16ull << 20;
+constexpr size_t kL2WindowDefault = 8ull << 20;
 
 struct DeviceBVH {
     BvhView view;
@@ -73,6 +77,8 @@ struct DeviceBVH {
     size_t l2_window_bytes = 0;
     float l2_hit_ratio = 0.0f;
     bool l2_setup = false;
+    size_t l2_top_bytes = 0;                   // the breadth-first top of the node array (upload)
+    size_t l2_window_want = kL2WindowDefault;  // tt_dbvh_set_l2_window
     float lo[3] = {-1.f, -1.f, -1.f}, hi[3] = {1.f, 1.f, 1.f};  // scene bounds (root boxes)
     // ray-ordering scratch per work-counter slot (caller stream, three pipeline streams)
     void *order[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -228,6 +234,60 @@ static tt_status cuda_fail(cudaError_t e, const char *what) {
         if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
     } while (0)
 
+// The device's node order: the top levels of the tree first (breadth first from the root, until
+// they fill top_bytes), then every other inner node in the file's depth-first order. Child order,
+// node contents and leaf addresses are unchanged, only inner-child addresses are renumbered, so a
+// traversal visits the same nodes and leaves in the same order and returns the same hits. The
+// L2 persisting window of the trace launches then covers a prefix of the array that is exactly
+// the tree's top levels (the file's depth-first order scatters them over the whole array).
+// Returns false, leaving `out` empty, for an array whose child addresses do not form a tree.
+static bool top_first_nodes(const std::vector<I4> &nodes, size_t top_bytes, std::vector<I4> &out, size_t &top_out) {
+    const size_t count = nodes.size() / 4;
+    out.clear();
+    top_out = 0;
+    if (count == 0 || nodes.size() % 4) return false;
+    std::vector<int64_t> new_index(count, -1), order;
+    order.reserve(count);
+    const size_t top_nodes = std::max<size_t>(1, top_bytes / 64);
+    // breadth first, level by level, while the placed nodes fit in top_bytes
+    new_index[0] = 0;
+    order.push_back(0);
+    for (size_t head = 0; head < order.size() && order.size() < top_nodes; head++) {
+        const I4 &c = nodes[4 * (size_t)order[head] + 3];
+        for (int32_t addr : {c.x, c.y}) {
+            if (addr < 0) continue;  // a leaf
+            if (addr % 4 || (size_t)addr / 4 >= count) return false;
+            const size_t k = (size_t)addr / 4;
+            if (new_index[k] >= 0) return false;  // not a tree
+            if (order.size() >= top_nodes) break;
+            new_index[k] = (int64_t)order.size();
+            order.push_back((int64_t)k);
+        }
+    }
+    top_out = 64 * order.size();
+    for (size_t k = 0; k < count; k++)
+        if (new_index[k] < 0) {
+            new_index[k] = (int64_t)order.size();
+            order.push_back((int64_t)k);
+        }
+    out.resize(nodes.size());
+    for (size_t j = 0; j < count; j++) {
+        const size_t k = (size_t)order[j];
+        for (int q = 0; q < 4; q++) out[4 * j + q] = nodes[4 * k + q];
+        I4 &c = out[4 * j + 3];
+        for (int32_t *addr : {&c.x, &c.y}) {
+            if (*addr < 0) continue;
+            if (*addr % 4 || (size_t)*addr / 4 >= count) {
+                out.clear();
+                top_out = 0;
+                return false;
+            }
+            *addr = (int32_t)(4 * new_index[(size_t)*addr / 4]);
+        }
+    }
+    return true;
+}
+
 static tt_status upload(const CompactBVH &b, DeviceBVH &d) {
     int dev = 0;
     TT_CUDA(cudaGetDevice(&dev));
@@ -246,7 +306,17 @@ static tt_status upload(const CompactBVH &b, DeviceBVH &d) {
     if (e != cudaSuccess) return fail(TT_ERR_OOM, std::string("cudaMalloc BVH: ") + cudaGetErrorString(e));
     char *p = static_cast<char *>(d.base);
     d.view.nodes = reinterpret_cast<const float4 *>(p);
-    TT_CUDA(cudaMemcpy(p, b.nodes.data(), nb, cudaMemcpyHostToDevice));
+    {
+        std::vector<I4> reordered;
+        size_t top = 0;
+        if (top_first_nodes(b.nodes, kL2TopRegion, reordered, top)) {
+            TT_CUDA(cudaMemcpy(p, reordered.data(), nb, cudaMemcpyHostToDevice));
+            d.l2_top_bytes = top;
+        } else {
+            TT_CUDA(cudaMemcpy(p, b.nodes.data(), nb, cudaMemcpyHostToDevice));
+            d.l2_top_bytes = nb;  // file order: only the whole array is a window over the top levels
+        }
+    }
     p += align(nb);
     d.view.verts = reinterpret_cast<const float4 *>(p);
     TT_CUDA(cudaMemcpy(p, b.vertices.data(), vb, cudaMemcpyHostToDevice));
@@ -330,13 +400,13 @@ static void setup_l2_window(DeviceBVH &d) {
     if (cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, d.device) == cudaSuccess &&
         cudaDeviceGetAttribute(&max_window, cudaDevAttrMaxAccessPolicyWindowSize, d.device) == cudaSuccess &&
         max_persist > 0 && max_window > 0) {
-        const size_t nb = 16ull * d.num_nodes;
+        const size_t nb = std::min(std::min((size_t)16 * (size_t)d.num_nodes, d.l2_top_bytes), d.l2_window_want);
         size_t cur = 0;
         cudaDeviceGetLimit(&cur, cudaLimitPersistingL2CacheSize);
         const size_t want = std::min(nb, (size_t)max_persist);
         if (want > cur && cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, want) == cudaSuccess)
             cudaDeviceGetLimit(&cur, cudaLimitPersistingL2CacheSize);
-        d.l2_window_bytes = cur ? std::min(nb, (size_t)max_window) : 0;
+        d.l2_window_bytes = (cur && nb) ? std::min(nb, (size_t)max_window) : 0;
         d.l2_hit_ratio = cur >= d.l2_window_bytes ? 1.0f : (float)cur / (float)d.l2_window_bytes;
     }
     cudaGetLastError();
@@ -506,6 +576,14 @@ void tt_dbvh_free(tt_dbvh *dbvh) {
     if (!dbvh) return;
     release(dbvh->d);
     delete dbvh;
+}
+
+tt_status tt_dbvh_set_l2_window(tt_dbvh *bvh, int64_t bytes) {
+    if (!bvh || bytes < 0) return fail(TT_ERR_INVALID, "null BVH or negative window");
+    bvh->d.l2_window_want = (size_t)bytes;
+    bvh->d.l2_setup = false;  // the next trace launch sets the window (and the set-aside) up again
+    bvh->d.l2_window_bytes = 0;
+    return TT_OK;
 }
 
 tt_status tt_dbvh_set_variant(tt_dbvh *bvh, int32_t variant) {
