@@ -606,6 +606,7 @@ def run_render(args) -> None:
     torch.cuda.synchronize(dev)
     r.check()
     r.stats(reset=True)
+    r.launches(reset=True)
     ms = []
     with Clocks(0) as clk:
         for k in range(args.steps):
@@ -618,6 +619,7 @@ def run_render(args) -> None:
             ms.append(e0.elapsed_time(e1))
     r.check()
     st = r.stats(reset=True)
+    launches = r.launches(reset=True)
     mean_ms = float(np.mean(ms))
     paths = cfg["width"] * cfg["height"] * cfg["spp"]
     rays = (st["extension_rays"] + st["shadow_rays"]) / args.steps
@@ -635,9 +637,6 @@ def run_render(args) -> None:
     img = host.numpy()
     assert np.isfinite(img).all()
     cpu = render_cpu_baseline(bvh, sc, cam, cfg["spp"], cfg["depth"])
-    # per wave: raygen, per bounce extend / shade / shadow (+ 4 ordering kernels and the hit gather
-    # when ordered), accumulate
-    launches = args.steps * (1 + (3 + 5 * r.launch[3]) * cfg["depth"] + 1) * -(-paths // r.launch[2])
     line = {
         "metric": f"Msamples/s native path tracer ({args.workload})", "value": round(paths / mean_ms / 1e3, 2),
         "unit": "Msamples/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,

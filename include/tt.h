@@ -395,18 +395,27 @@ tt_status tt_renderer_env_tables(const tt_renderer *renderer, float *marginal, f
 typedef struct tt_launch_shape {
     int32_t block;        /* threads per block: 64, 128 or 256 */
     int32_t stack_shared; /* traversal stack entries per thread kept in shared memory: 0, 8 or 16 */
-    int32_t wave_paths;   /* paths in flight per wave (queue capacity): 1 .. 2^24 */
+    int32_t wave_paths;   /* paths in flight per wave (queue capacity): 1 .. 2^26 */
     int32_t ordered;      /* 1: order each extension queue by origin and direction cell before
                              tracing it (coherent queues, e.g. camera rays, are left alone) */
+    int32_t streamed;     /* 1: a render of more paths than one wave streams them through a pool
+                             of wave_paths slots that is refilled with new camera paths as paths
+                             end (no refill for cached renders, or when max_depth * wave_paths
+                             exceeds 2^29), so every bounce launch traces a full queue; 0: waves
+                             of wave_paths paths, each traced bounce by bounce to its end */
     float ms;             /* tt_batch_autotune: the trial's time; otherwise 0 */
 } tt_launch_shape;
-/* Default: 128 threads, 16 shared entries, 2^22 paths, unordered. Results do not depend on the
- * shape. */
+/* Default: 128 threads, 16 shared entries, 2^22 paths, unordered, streamed. Results do not depend
+ * on the shape: every pixel adds its samples in sample order whatever the shape. */
 tt_status tt_renderer_set_launch(tt_renderer *renderer, const tt_launch_shape *shape);
 tt_status tt_renderer_get_launch(const tt_renderer *renderer, tt_launch_shape *shape);
 /* Counters of the native path tracer since the last reset: out[0] extension rays (closest hit),
  * out[1] shadow rays (any hit), out[2] paths. Synchronous. */
 tt_status tt_renderer_stats(tt_renderer *renderer, uint64_t *out, int32_t reset);
+/* Kernels the native path tracer issued since the last reset (launched, or captured into a batch's
+ * graph), counted on the host: its own kernels and the ordering kernels, not a cached render's
+ * network kernels. */
+tt_status tt_renderer_launches(tt_renderer *renderer, uint64_t *out, int32_t reset);
 
 /* Batched rendering (no counterpart in the reference): many views of any size and sample count
  * rendered by one sequence of persistent wavefront kernels over a shared path index space, which
@@ -435,9 +444,12 @@ tt_status tt_batch_info(const tt_batch *batch, int64_t *total_paths, int64_t *ac
 tt_status tt_batch_render(tt_batch *batch, void *d_accum, int32_t use_graph, void *stream);
 /* Nodes of the captured graph (0 before the first graph render). */
 tt_status tt_batch_graph_kernels(const tt_batch *batch, int32_t *kernels);
-/* Times the first sample_paths paths of the batch (0: 2^23) under every launch shape (block x
- * stack_shared x wave_paths in {2^20, 2^21, 2^22}), keeps the fastest as the renderer's shape and
- * writes up to max_results trials to results. Synchronous; touches no accumulation buffer. */
+/* Times the first sample_paths paths of the batch (0: 2^27) under launch shapes in two stages:
+ * block x stack_shared at 2^22-path waves, ordered and streamed; then the fastest of those at
+ * wave_paths in {2^20, 2^22, 2^24, 2^26}, ordered or not, streamed or not (waves that would hold
+ * the whole sample twice over are skipped). Keeps the fastest trial as the renderer's shape and
+ * writes up to max_results trials to results (at most 9 + 16). Synchronous; touches no
+ * accumulation buffer. */
 tt_status tt_batch_autotune(tt_batch *batch, int64_t sample_paths, void *stream, tt_launch_shape *results,
                             int32_t max_results, int32_t *n_results);
 tt_status tt_batch_free(tt_batch *batch);

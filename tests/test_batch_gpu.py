@@ -3,7 +3,8 @@ graph-captured wavefront render.
 
 Every view of a batch must be bit-identical to a plain tt_render_native of that view, whatever
 the launch shape (block size, shared stack depth, paths per wave — including waves that split
-pixels and views), with or without the CUDA graph; the ray counters must agree too.
+pixels and views — ordered queues, waves or a streamed pool), with or without the CUDA graph;
+the ray counters must agree too.
 """
 import numpy as np
 import pytest
@@ -72,9 +73,10 @@ def test_batch_equals_sequential_renders(showcase):
     assert np.array_equal(plain.view(np.uint32), seq.view(np.uint32))
 
 
-@pytest.mark.parametrize("shape", [(64, 0, 777, 0), (256, 8, 4096, 0), (128, 16, 1 << 20, 0), (64, 16, 31, 0),
-                                   (64, 0, 777, 1), (256, 8, 4096, 1), (128, 16, 1 << 20, 1), (64, 16, 31, 1),
-                                   (128, 16, 65536, 1)])
+@pytest.mark.parametrize("shape", [(64, 0, 777, 0, 0), (256, 8, 4096, 0, 1), (128, 16, 1 << 20, 0, 1),
+                                   (64, 16, 31, 0, 0), (64, 16, 31, 0, 1), (64, 0, 777, 1, 1), (256, 8, 4096, 1, 0),
+                                   (128, 16, 1 << 20, 1, 0), (64, 16, 31, 1, 1), (128, 16, 65536, 1, 1),
+                                   (128, 16, 1000, 1, 1)])
 def test_result_does_not_depend_on_launch_shape(showcase, shape):
     views = _views(seed=1, count=5)
     base = _sequential(showcase, views)
@@ -88,6 +90,35 @@ def test_result_does_not_depend_on_launch_shape(showcase, shape):
         showcase.set_launch(*old)
     assert np.array_equal(got.view(np.uint32), base.view(np.uint32))
     assert np.array_equal(seq.view(np.uint32), base.view(np.uint32))
+
+
+@pytest.mark.parametrize("wave,depth,ordered,f64", [(97, 5, 0, 0), (1000, 1, 0, 0), (4096, 12, 1, 0),
+                                                    (50000, 5, 1, 0), (3001, 5, 0, 1), (65536, 9, 1, 1)])
+def test_streamed_render_matches_waves(showcase, wave, depth, ordered, f64):
+    """A render of more paths than one wave streams them through a pool of `wave` slots that is
+    refilled as paths end (the queues mix paths of every age, and each path's radiance waits in
+    a ring until all earlier paths have ended); the image must be bit-identical to the render in
+    one wave, and the ray and path counters equal."""
+    cam = make_camera_meta(64, 48, [2.0, 1.2, 2.5], [-2.0, -0.8, -2.5], fov=(50.0, 37.5))
+    params = render_params(spp=7, sample_offset=3, seed=11, max_depth=depth, rr_depth=2, env_scale=1.5, flags=f64)
+    dt = torch.float64 if f64 else torch.float32
+    old = showcase.launch
+    try:
+        out = []
+        for shape in [(128, 16, 1 << 22, 0), (64, 8, wave, ordered)]:
+            showcase.set_launch(*shape)
+            acc = torch.zeros(64 * 48 * 3, dtype=dt, device="cuda")
+            showcase.stats(reset=True)
+            showcase.render_native(cam, params, acc)
+            torch.cuda.synchronize()
+            showcase.check()
+            out.append((acc.cpu().numpy(), showcase.stats(reset=True)))
+    finally:
+        showcase.set_launch(*old)
+    (waves, s_waves), (streamed, s_streamed) = out
+    assert waves.max() > 0
+    assert np.array_equal(streamed.view(np.uint64 if f64 else np.uint32), waves.view(np.uint64 if f64 else np.uint32))
+    assert s_streamed == s_waves and s_waves["paths"] == 64 * 48 * 7
 
 
 def test_graph_replays_and_recaptures(showcase):
@@ -128,8 +159,8 @@ def test_ray_counters_and_autotune(showcase):
     assert s_seq == s_batch
     assert s_seq["paths"] == sum(c.width * c.height * s for c, s, _, _ in views)
     assert s_seq["extension_rays"] >= s_seq["paths"] and s_seq["shadow_rays"] > 0
-    assert len(trials) >= 18 and all(t[4] > 0 for t in trials)
+    assert len(trials) >= 11 and all(t[5] > 0 for t in trials)
     assert {t[3] for t in trials} == {0, 1}
-    best = min(trials, key=lambda t: t[4])
-    assert showcase.launch == best[:4]
+    best = min(trials, key=lambda t: t[5])
+    assert showcase.launch == best[:5]
     assert np.array_equal(got.view(np.uint32), seq.view(np.uint32))

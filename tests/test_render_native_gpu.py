@@ -220,13 +220,16 @@ def test_ordered_queues_give_the_same_image():
         r.set_launch(128, 16, 1 << 22, 1)
         assert r.launch[3] == 1
         ordered = _render(r, cam, params)
-        r.set_launch(64, 0, 100000, 1)  # waves that split the image, still above the ordering threshold
+        r.set_launch(64, 0, 100000, 1, 0)  # waves that split the image, still above the ordering threshold
         ordered_waves = _render(r, cam, params)
+        r.set_launch(64, 0, 100000, 1, 1)  # a streamed pool: the survivors ordered, new camera rays not
+        ordered_streamed = _render(r, cam, params)
     finally:
         r.set_launch(*old)
     assert plain.max() > 0
     assert np.array_equal(ordered.view(np.uint32), plain.view(np.uint32))
     assert np.array_equal(ordered_waves.view(np.uint32), plain.view(np.uint32))
+    assert np.array_equal(ordered_streamed.view(np.uint32), plain.view(np.uint32))
     small = make_camera_meta(24, 20, [0.0, 0.0, 1.55], [0.0, 0.0, -1.0], fov=(45.0, 38.0))
     r.set_launch(128, 16, 1 << 22, 1)
     try:

@@ -66,10 +66,10 @@ RENDER_NO_ENV_SAMPLING = 2
 class LaunchShape(C.Structure):
     """tt_launch_shape (include/tt.h)."""
     _fields_ = [("block", C.c_int32), ("stack_shared", C.c_int32), ("wave_paths", C.c_int32), ("ordered", C.c_int32),
-                ("ms", C.c_float)]
+                ("streamed", C.c_int32), ("ms", C.c_float)]
 
     def as_tuple(self) -> tuple:
-        return (self.block, self.stack_shared, self.wave_paths, self.ordered)
+        return (self.block, self.stack_shared, self.wave_paths, self.ordered, self.streamed)
 
 
 class CacheParams(C.Structure):
@@ -138,6 +138,7 @@ SIGNATURES = {
     "tt_renderer_set_launch": (I32, [P, C.POINTER(LaunchShape)]),
     "tt_renderer_get_launch": (I32, [P, C.POINTER(LaunchShape)]),
     "tt_renderer_stats": (I32, [P, P, I32]),
+    "tt_renderer_launches": (I32, [P, P, I32]),
     "tt_batch_create": (I32, [P, P, I32, C.POINTER(RenderParams), C.POINTER(P)]),
     "tt_batch_info": (I32, [P, C.POINTER(I64), C.POINTER(I64)]),
     "tt_batch_render": (I32, [P, P, I32, P]),

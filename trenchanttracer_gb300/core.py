@@ -329,10 +329,11 @@ class Renderer:
         check(lib().tt_render_cached(self._h, cache._h, C.byref(cam), C.byref(params), C.c_void_p(accum.data_ptr()),
                                      int(bool(train)), C.c_void_p(stream)))
 
-    def set_launch(self, block: int, stack_shared: int, wave_paths: int, ordered: int = 0) -> None:
+    def set_launch(self, block: int, stack_shared: int, wave_paths: int, ordered: int = 0, streamed: int = 1) -> None:
         """Launch shape of the native kernels (include/tt.h, tt_launch_shape); ordered = 1 orders
-        each extension queue by origin and direction cell before tracing it."""
-        shape = _lib.LaunchShape(int(block), int(stack_shared), int(wave_paths), int(ordered), 0.0)
+        each extension queue by origin and direction cell before tracing it; streamed = 1 streams
+        a render of more paths than one wave through a refilled pool of wave_paths slots."""
+        shape = _lib.LaunchShape(int(block), int(stack_shared), int(wave_paths), int(ordered), int(streamed), 0.0)
         check(lib().tt_renderer_set_launch(self._h, C.byref(shape)))
 
     @property
@@ -346,6 +347,12 @@ class Renderer:
         out = np.zeros(3, np.uint64)
         check(lib().tt_renderer_stats(self._h, _ptr(out), int(bool(reset))))
         return {"extension_rays": int(out[0]), "shadow_rays": int(out[1]), "paths": int(out[2])}
+
+    def launches(self, reset: bool = False) -> int:
+        """Path-tracer kernels issued since the last reset (include/tt.h, tt_renderer_launches)."""
+        out = np.zeros(1, np.uint64)
+        check(lib().tt_renderer_launches(self._h, _ptr(out), int(bool(reset))))
+        return int(out[0])
 
     def env_tables(self, env_w: int, env_h: int) -> tuple[np.ndarray, np.ndarray]:
         marg = np.empty(env_h + 1, np.float32)
@@ -392,12 +399,12 @@ class Batch:
         return n.value
 
     def autotune(self, sample_paths: int = 0, stream: int = 0) -> list:
-        """Times every launch shape on the batch's first paths, keeps the fastest; returns
-        [(block, stack_shared, wave_paths, ordered, ms)]."""
+        """Times launch shapes on the batch's first paths (include/tt.h, tt_batch_autotune), keeps
+        the fastest; returns [(block, stack_shared, wave_paths, ordered, streamed, ms)]."""
         res = (_lib.LaunchShape * 64)()
         n = C.c_int32()
         check(lib().tt_batch_autotune(self._h, int(sample_paths), C.c_void_p(stream), res, 64, C.byref(n)))
-        return [(r.block, r.stack_shared, r.wave_paths, r.ordered, r.ms) for r in res[:min(n.value, 64)]]
+        return [r.as_tuple() + (r.ms,) for r in res[:min(n.value, 64)]]
 
     def split(self, accum) -> list:
         """The per-view (H, W, 3) images of an accumulation buffer (torch tensor or numpy array)."""

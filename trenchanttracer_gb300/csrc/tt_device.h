@@ -41,6 +41,8 @@ struct tt_renderer {
     // launch shape of the native kernels (tt_renderer_set_launch, tt_batch_autotune)
     int launch_block = 128, launch_stack = 16, launch_wave = 1 << 22;
     int launch_order = 0;  // order each extension queue by origin and direction cell before tracing
+    int launch_stream = 1; // stream renders of more paths than one wave through a refilled pool
+    unsigned long long launches = 0;  // path-tracer kernels issued (launched or captured)
     float order_lo[3] = {-1.f, -1.f, -1.f}, order_hi[3] = {1.f, 1.f, 1.f};  // scene bounds
     size_t order_off = 0;       // byte offset of the ordering scratch inside `paths` (0: none)
     size_t order_state_at = 0;  // its state block, relative to the scratch
@@ -50,9 +52,15 @@ struct tt_renderer {
     void *cache_mem = nullptr;
     size_t cache_bytes = 0;
     long long cache_queries = 0, cache_records = 0;
+    // streamed renders (more paths than one wave, refilled as paths end): the radiance ring, the
+    // pool's path indices, its free-slot stack and the plan record, one allocation
+    void *stream_mem = nullptr;
+    size_t stream_bytes = 0;
 };
 
 namespace tt {
+// Error-word bit of the renderer: a streamed render ended with paths unfinished.
+constexpr uint32_t kErrStream = 16u;
 // [0] extension rays, [1] shadow rays, [2] paths traced by the native path tracer
 inline unsigned long long *renderer_stats(tt_renderer *r) {
     return reinterpret_cast<unsigned long long *>(reinterpret_cast<char *>(r->err) + 64);

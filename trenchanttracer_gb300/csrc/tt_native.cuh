@@ -93,14 +93,52 @@ struct CacheView {
 };
 
 // Ordering of an extension queue (tt_reorder.cu): when order_built(state), k_extend reads the
-// ordered copy of the queue's rays and writes hits by ordered slot, and k_order_gather_hits moves
-// each hit back to its queue slot (pos: the ordered slot of each queue slot).
+// ordered copy of the queue's first *n_sorted rays and writes their hits by ordered slot, and
+// k_order_gather_hits moves each of those hits back to its queue slot (pos: the ordered slot of
+// each queue slot). The rest of the queue (a streamed render's new camera rays, coherent as they
+// are) is traced in place.
 struct OrderView {
     const float4 *sorted;  // nullptr: ordering off
     float *hit_t, *hit_u, *hit_v;
     int *hit_prim;
     const int *pos;
     const unsigned long long *state;
+    const int *n_sorted;
+};
+
+// Path state by index: the state slot of a path in waves, the queue slot in a streamed render.
+struct PathState {
+    float *beta, *L;  // 3 per path
+    float *last_pdf;
+    uint64_t *rng, *rng_inc;
+    int *depth, *flags;
+    long long *g;     // streamed renders: the path's index
+};
+
+// Streamed render: a pool of wave_paths queue slots that is refilled with the next paths of the
+// index space as paths end, so every bounce launch works on a full pool and the few long paths
+// at the end of a wave no longer hold the GPU half idle. The path state lives in queue order, one
+// copy per queue parity: shade writes each survivor's state next to its ray in the next queue,
+// and the refill writes new paths' state behind the survivors, so every state access is
+// coalesced. An ended path's radiance goes to a ring of ring_n entries at (path index mod
+// ring_n), where it waits until every path below it has ended; an accumulate pass then adds that
+// range in sample order, exactly as the wave scheme does, so the image bits do not change.
+// ring_n = max_depth * pool holds every path still in flight plus one refill.
+struct StreamPlan {
+    long long next;                 // the next path of the index space to start
+    long long frontier;             // every path below it has been accumulated
+    unsigned long long min_alive;   // smallest path index among the last shade's survivors
+    long long acc_lo, acc_hi;       // the range the next accumulate pass adds
+    long long new_first;            // the paths the next refill starts: [new_first, + new_n)
+    int new_n, new_at;              // how many, and their first slot in the extension queue
+};
+
+struct StreamView {
+    long long total;    // paths of the render
+    long long ring_n;   // entries of the radiance ring
+    float *ring;        // 3 floats per entry
+    PathState st[2];    // path state by queue slot, by queue parity
+    StreamPlan *plan;
 };
 
 struct NativeArgs {
@@ -120,6 +158,7 @@ struct NativeArgs {
     unsigned int *err;
     unsigned long long *stats;  // [0] extension rays, [1] shadow rays, [2] paths
     CacheView cache;
+    StreamView stream;  // a streamed render's state (ring == nullptr: waves)
     const struct GeomNode *gnodes;  // box hierarchy over the analytic objects, or nullptr
     const int *gidx;
     OrderView order;

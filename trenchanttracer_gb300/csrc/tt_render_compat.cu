@@ -20,6 +20,7 @@
 
 #include "tt_device.h"
 #include "tt_refmath.cuh"
+#include "tt_reorder.h"
 
 namespace tt {
 
@@ -607,6 +608,8 @@ tt_status tt_renderer_check(tt_renderer *r, void *stream) {
         TT_CUDA_R(cudaMemset(r->err, 0, 4));
         if (w & kErrStack) return fail(TT_ERR_BOUNDS, "traversal stack overflow during rendering");
         if (w & kErrIter) return fail(TT_ERR_TIMEOUT, "traversal iteration cap reached during rendering");
+        if (w & kErrOrder) return fail(TT_ERR_BOUNDS, "ray ordering: a slot index out of range during rendering");
+        if (w & kErrStream) return fail(TT_ERR_TIMEOUT, "a streamed render ended with paths unfinished");
         return fail(TT_ERR_TIMEOUT, "a radiance-cache tensor-core wait ran out during rendering");
     }
     return TT_OK;

@@ -26,13 +26,9 @@ __global__ void __launch_bounds__(kBlock) k_extend(NativeArgs a, int cur) {
     TravStack<kSh, kBlock> stack;
     stack.sh = sh_stack + threadIdx.x;
     uint32_t err = 0;
-    // an ordered queue: rays and hits by ordered slot, moved back by k_order_gather_hits
+    // an ordered queue prefix: rays and hits by ordered slot, moved back by k_order_gather_hits
     const bool ordered = a.order.sorted && order_built(a.order.state);
-    const float4 *rays = ordered ? a.order.sorted : a.ps.ray[cur];
-    float *hit_t = ordered ? a.order.hit_t : a.ps.hit_t;
-    float *hit_u = ordered ? a.order.hit_u : a.ps.hit_u;
-    float *hit_v = ordered ? a.order.hit_v : a.ps.hit_v;
-    int *hit_prim = ordered ? a.order.hit_prim : a.ps.hit_prim;
+    const int n_sorted = ordered ? *a.order.n_sorted : 0;
     for (;;) {
         int base = 0;
         if (lane == 0) base = atomicAdd(a.ps.counts + 3, 32);
@@ -41,16 +37,18 @@ __global__ void __launch_bounds__(kBlock) k_extend(NativeArgs a, int cur) {
         const int q = base + lane;
         const unsigned mask = __ballot_sync(0xffffffffu, q < n);
         if (q < n) {
+            const bool srt = q < n_sorted;
+            const float4 *rays = srt ? a.order.sorted : a.ps.ray[cur];
             const float4 r0 = rays[2 * q], r1 = rays[2 * q + 1];
             const TraceResult tr = traverse_on<true>(stack, a.bvh, r0, r1, err);
             float t = tr.t, hu = tr.u, hv = tr.v;
             int prim = tr.addr;
             if (a.num_geoms)
                 analytic_hit(a, mask, true, V3(r0.x, r0.y, r0.z), V3(r0.w, r1.x, r1.y), r1.z, t, prim, hu, hv, false);
-            hit_t[q] = t;
-            hit_prim[q] = prim;
-            hit_u[q] = hu;
-            hit_v[q] = hv;
+            (srt ? a.order.hit_t : a.ps.hit_t)[q] = t;
+            (srt ? a.order.hit_prim : a.ps.hit_prim)[q] = prim;
+            (srt ? a.order.hit_u : a.ps.hit_u)[q] = hu;
+            (srt ? a.order.hit_v : a.ps.hit_v)[q] = hv;
         }
         __syncwarp();
     }
@@ -86,8 +84,10 @@ __global__ void __launch_bounds__(kBlock) k_shadow(NativeArgs a) {
                 blocked = blocked || prim != -1;
             }
             if (!blocked) {
-                const int i = a.ps.shadow_path[j];
-                float *L = a.ps.L + 3ll * i;
+                // a path's radiance: L[3 * t] for t >= 0, else (an ended path of a streamed
+                // render) ring entry -1 - t
+                const int t = a.ps.shadow_path[j];
+                float *L = t >= 0 ? a.ps.L + 3ll * t : a.stream.ring + 3ll * (-1ll - t);
                 const float *c = a.ps.shadow_val + 3ll * j;
                 L[0] = PT_ADD(L[0], c[0]);
                 L[1] = PT_ADD(L[1], c[1]);
@@ -102,7 +102,7 @@ __global__ void __launch_bounds__(kBlock) k_shadow(NativeArgs a) {
 
 __global__ void __launch_bounds__(256) k_order_gather_hits(NativeArgs a, int cur) {
     if (!a.order.sorted || !order_built(a.order.state)) return;
-    const int n = a.ps.counts[cur];
+    const int n = *a.order.n_sorted;
     unsigned bad = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const int p = __ldcs(a.order.pos + i);

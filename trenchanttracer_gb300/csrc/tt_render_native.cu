@@ -452,6 +452,66 @@ __device__ __forceinline__ void put_ray(float4 *rays, int slot, const V3 &o, con
     rays[2 * slot + 1] = make_float4(d.y, d.z, 0.0f, 1e20f);
 }
 
+// The camera ray of path g (batch-global index), its PCG32 state after the jitter (and lens)
+// draws and its stream index. cc caches the last view's frame across a thread's paths.
+struct CamFrame {
+    int v = -1;
+    ViewRec vw;
+    V3 pos, view, right, up;
+};
+
+__device__ __forceinline__ void camera_path(const NativeArgs &a, long long g, CamFrame &cc, V3 &org, V3 &dir,
+                                            Rng &rg, long long &gid) {
+    const int v = find_view(a, g);
+    if (v != cc.v) {
+        cc.vw = view_of(a, v);
+        cc.pos = V3(cc.vw.pos[0], cc.vw.pos[1], cc.vw.pos[2]);
+        cc.view = normalize(V3(cc.vw.view[0], cc.vw.view[1], cc.vw.view[2]));
+        cc.right = normalize(cross(cc.view, V3(cc.vw.up[0], cc.vw.up[1], cc.vw.up[2])));
+        cc.up = cross(cc.right, cc.view);
+        cc.v = v;
+    }
+    const ViewRec &vw = cc.vw;
+    gid = vw.stream0 + (g - vw.first);
+    const int pixel = (int)(gid % vw.npix);
+    const int px = pixel % vw.width, py = pixel / vw.width;
+    rg = pcg32_seed(vw.seed_state, (uint64_t)gid);
+    const float jx = uniform(rg), jy = uniform(rg);
+    const float sx = PT_SUB(PT_MUL(2.0f, PT_DIV(PT_ADD((float)px, jx), (float)vw.width)), 1.0f);
+    const float sy = PT_SUB(1.0f, PT_MUL(2.0f, PT_DIV(PT_ADD((float)py, jy), (float)vw.height)));
+    const V3 dp = madd(cc.up, PT_MUL(sy, vw.tany), madd(cc.right, PT_MUL(sx, vw.tanx), cc.view));
+    org = cc.pos;
+    if (vw.aperture > 1e-5f) {
+        // thin lens: aim at the pinhole ray's point on the focal plane from a point of the lens disc
+        const V3 focus = madd(dp, vw.focal, cc.pos);
+        const float u1 = uniform(rg), u2 = uniform(rg);
+        const float r = PT_MUL(vw.aperture, PT_SQRT(u1));
+        float sp, cp;
+        sincos(PT_MUL(kTwoPi, u2), sp, cp);
+        org = madd(cc.up, PT_MUL(r, sp), madd(cc.right, PT_MUL(r, cp), cc.pos));
+        dir = normalize(sub(focus, org));
+    } else {
+        dir = normalize(dp);
+    }
+}
+
+__device__ __forceinline__ PathState wave_state(const PathSoA &ps) {
+    return PathState{ps.beta, ps.L, ps.last_pdf, ps.rng, ps.rng_inc, ps.depth, ps.flags, nullptr};
+}
+
+// A new path in state slot i, its camera ray in slot q of `rays`.
+__device__ __forceinline__ void start_path(const PathState &S, int i, float4 *rays, int q, const V3 &org,
+                                           const V3 &dir, const Rng &rg, int flags) {
+    put_ray(rays, q, org, dir);
+    st3(S.beta + 3ll * i, V3(1.f, 1.f, 1.f));
+    st3(S.L + 3ll * i, V3(0.f, 0.f, 0.f));
+    S.rng[i] = rg.state;
+    S.rng_inc[i] = rg.inc;
+    S.last_pdf[i] = 0.0f;
+    S.depth[i] = 0;
+    S.flags[i] = flags;
+}
+
 // Camera rays of the wave's paths into queue 0.
 __global__ void __launch_bounds__(kShadeBlockMax) k_raygen(NativeArgs a) {
     const int stride = gridDim.x * blockDim.x;
@@ -469,51 +529,77 @@ __global__ void __launch_bounds__(kShadeBlockMax) k_raygen(NativeArgs a) {
     }
     if (a.cache.enabled)  // this wave's training slots start empty
         for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < a.cache.train_slots; s += stride) a.cache.s_path[s] = -1;
-    int cached = -1;
-    ViewRec vw;
-    V3 cam_pos, view, right, up;
+    CamFrame cc;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.wave_paths; i += stride) {
-        const long long g = a.wave_first + i;
-        const int v = find_view(a, g);
-        if (v != cached) {
-            vw = view_of(a, v);
-            cam_pos = V3(vw.pos[0], vw.pos[1], vw.pos[2]);
-            view = normalize(V3(vw.view[0], vw.view[1], vw.view[2]));
-            right = normalize(cross(view, V3(vw.up[0], vw.up[1], vw.up[2])));
-            up = cross(right, view);
-            cached = v;
-        }
-        const long long gid = vw.stream0 + (g - vw.first);
-        const int pixel = (int)(gid % vw.npix);
-        const int px = pixel % vw.width, py = pixel / vw.width;
-        Rng rg = pcg32_seed(vw.seed_state, (uint64_t)gid);
-        const float jx = uniform(rg), jy = uniform(rg);
-        const float sx = PT_SUB(PT_MUL(2.0f, PT_DIV(PT_ADD((float)px, jx), (float)vw.width)), 1.0f);
-        const float sy = PT_SUB(1.0f, PT_MUL(2.0f, PT_DIV(PT_ADD((float)py, jy), (float)vw.height)));
-        const V3 dp = madd(up, PT_MUL(sy, vw.tany), madd(right, PT_MUL(sx, vw.tanx), view));
-        V3 org = cam_pos, dir;
-        if (vw.aperture > 1e-5f) {
-            // thin lens: aim at the pinhole ray's point on the focal plane from a point of the lens disc
-            const V3 focus = madd(dp, vw.focal, cam_pos);
-            const float u1 = uniform(rg), u2 = uniform(rg);
-            const float r = PT_MUL(vw.aperture, PT_SQRT(u1));
-            float sp, cp;
-            sincos(PT_MUL(kTwoPi, u2), sp, cp);
-            org = madd(up, PT_MUL(r, sp), madd(right, PT_MUL(r, cp), cam_pos));
-            dir = normalize(sub(focus, org));
-        } else {
-            dir = normalize(dp);
-        }
-        put_ray(a.ps.ray[0], i, org, dir);
-        st3(a.ps.beta + 3ll * i, V3(1.f, 1.f, 1.f));
-        st3(a.ps.L + 3ll * i, V3(0.f, 0.f, 0.f));
-        a.ps.rng[i] = rg.state;
-        a.ps.rng_inc[i] = rg.inc;
-        a.ps.last_pdf[i] = 0.0f;
-        a.ps.depth[i] = 0;
+        V3 org, dir;
+        Rng rg;
+        long long gid;
+        camera_path(a, a.wave_first + i, cc, org, dir, rg, gid);
         const bool train = a.cache.train && ((unsigned long long)gid + a.cache.train_phase) % a.cache.train_stride == 0;
-        a.ps.flags[i] = kFlagSpecular | (train ? kFlagTrain : 0);
+        start_path(wave_state(a.ps), i, a.ps.ray[0], i, org, dir, rg, kFlagSpecular | (train ? kFlagTrain : 0));
         a.ps.queue[0][i] = i;
+    }
+}
+
+// ---- streamed renders -------------------------------------------------------------------------
+// Per iteration (queue parity c): k_stream_plan (one thread) -> k_accumulate_stream -> k_regen ->
+// extend -> k_shade_stream -> shadow. The plan turns the last shade's survivors and ended paths
+// into the frontier (all paths below it have ended), the range to accumulate and the refill.
+
+__global__ void k_stream_init(NativeArgs a) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    StreamPlan *pl = a.stream.plan;
+    pl->next = 0;
+    pl->frontier = 0;
+    pl->min_alive = ~0ull;
+    pl->acc_lo = pl->acc_hi = 0;
+    pl->new_first = 0;
+    pl->new_n = pl->new_at = 0;
+    for (int k = 0; k < 5; k++) a.ps.counts[k] = 0;
+}
+
+// final = 1: no refill, and the frontier must have reached the end of the index space.
+__global__ void k_stream_plan(NativeArgs a, int c, int pool, int final) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    StreamPlan *pl = a.stream.plan;
+    const int alive = a.ps.counts[c];
+    const long long next = pl->next;
+    const long long front = pl->min_alive < (unsigned long long)next ? (long long)pl->min_alive : next;
+    pl->acc_lo = pl->frontier;
+    pl->acc_hi = front;
+    pl->frontier = front;
+    long long n_new = 0;
+    if (!final) {
+        n_new = min((long long)(pool - alive), a.stream.total - next);
+        n_new = min(n_new, front + a.stream.ring_n - next);  // ring entries not yet accumulated
+        n_new = max(n_new, 0ll);
+    } else if (front != a.stream.total) {
+        atomicOr(a.err, kErrStream);
+    }
+    pl->new_first = next;
+    pl->new_n = (int)n_new;
+    pl->new_at = alive;
+    pl->next = next + n_new;
+    pl->min_alive = ~0ull;
+    a.ps.counts[c] = alive + (int)n_new;
+}
+
+// The refill: new paths behind the survivors in queue c.
+__global__ void __launch_bounds__(kShadeBlockMax) k_regen(NativeArgs a, int c) {
+    const StreamPlan *pl = a.stream.plan;
+    const int n = pl->new_n, at = pl->new_at;
+    const long long first = pl->new_first;
+    if (blockIdx.x == 0 && threadIdx.x == 0 && n > 0) atomicAdd(a.stats + 2, (unsigned long long)n);
+    const PathState &S = a.stream.st[c];
+    CamFrame cc;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const long long g = first + t;
+        V3 org, dir;
+        Rng rg;
+        long long gid;
+        camera_path(a, g, cc, org, dir, rg, gid);
+        start_path(S, at + t, a.ps.ray[c], at + t, org, dir, rg, kFlagSpecular);
+        S.g[at + t] = g;
     }
 }
 
@@ -522,29 +608,41 @@ __device__ __forceinline__ float ray_eps(const NativeArgs &a, const V3 &p) {
     return PT_MUL(a.p.ray_eps, fmaxf(1.0f, m));
 }
 
-__global__ void __launch_bounds__(kShadeBlockMax) k_shade(NativeArgs a, int cur) {
+// kStream: a streamed render. The state is read by queue slot from copy `cur` and written for
+// each survivor at its slot of the next queue in copy cur ^ 1; an ended path leaves its radiance
+// in the ring, and the survivors report the smallest path index among them. In waves the state
+// stays in the path's own slot.
+template <bool kStream>
+__device__ __forceinline__ void shade_queue(const NativeArgs &a, int cur) {
     const int n = a.ps.counts[cur];
     const int stride = gridDim.x * blockDim.x;
     const int rounds = (n + stride - 1) / stride;
     const bool use_env = a.env.w > 0;
+    const PathState S = kStream ? a.stream.st[cur] : wave_state(a.ps);
     for (int round = 0, q = blockIdx.x * blockDim.x + threadIdx.x; round < rounds; round++, q += stride) {
         const bool live = q < n;
         bool alive = false;
         bool shadow = false;
-        int i = 0;
+        int i = 0;         // state slot
+        long long pg = 0;  // kStream: the path's index
         V3 sh_o, sh_d, sh_val, next_o, next_d;
+        V3 beta, L;
+        Rng g;
+        int depth = 0, flags_next = 0;
+        float pdf_next = 0.0f;
         if (live) {
-            i = a.ps.queue[cur][q];
-            Rng g;
-            g.state = a.ps.rng[i];
-            g.inc = a.ps.rng_inc[i];
+            i = kStream ? q : a.ps.queue[cur][q];
+            if (kStream) pg = S.g[i];
+            g.state = S.rng[i];
+            g.inc = S.rng_inc[i];
             const float4 r0 = a.ps.ray[cur][2 * q], r1 = a.ps.ray[cur][2 * q + 1];
             const V3 o(r0.x, r0.y, r0.z), d(r0.w, r1.x, r1.y);
-            V3 beta = ld3(a.ps.beta + 3ll * i), L = ld3(a.ps.L + 3ll * i);
+            beta = ld3(S.beta + 3ll * i);
+            L = ld3(S.L + 3ll * i);
             const int prim = a.ps.hit_prim[q];
-            int flags = a.ps.flags[i];
-            const float last_pdf = a.ps.last_pdf[i];
-            int depth = a.ps.depth[i];
+            int flags = S.flags[i];
+            const float last_pdf = S.last_pdf[i];
+            depth = S.depth[i];
             if (prim == -1) {
                 if (use_env) {
                     const int texel = env_texel(a.env, d);
@@ -627,52 +725,103 @@ __global__ void __launch_bounds__(kShadeBlockMax) k_shade(NativeArgs a, int cur)
                         const V3 off = dot(bs.wi, nl) >= 0.0f ? nl : V3(-nl.x, -nl.y, -nl.z);
                         next_o = madd(off, eps, p);
                         next_d = bs.wi;
-                        st3(a.ps.beta + 3ll * i, beta);
-                        a.ps.last_pdf[i] = bs.pdf;
-                        a.ps.flags[i] = (flags & kFlagsKept) | ((bs.specular || !nee) ? kFlagSpecular : 0);
-                        a.ps.depth[i] = depth;
+                        pdf_next = bs.pdf;
+                        flags_next = (flags & kFlagsKept) | ((bs.specular || !nee) ? kFlagSpecular : 0);
+                        if (!kStream) {
+                            st3(S.beta + 3ll * i, beta);
+                            S.last_pdf[i] = pdf_next;
+                            S.flags[i] = flags_next;
+                            S.depth[i] = depth;
+                        }
                     }
                 }
             }
-            st3(a.ps.L + 3ll * i, L);
-            a.ps.rng[i] = g.state;
+            if (!kStream) {
+                st3(S.L + 3ll * i, L);
+                S.rng[i] = g.state;
+            }
         }
         const int slot = warp_append(a.ps.counts + (cur ^ 1), alive);
         if (alive) {
-            a.ps.queue[cur ^ 1][slot] = i;
+            if (!kStream) a.ps.queue[cur ^ 1][slot] = i;
             put_ray(a.ps.ray[cur ^ 1], slot, next_o, next_d);
+            if (kStream) {
+                const PathState &N = a.stream.st[cur ^ 1];
+                st3(N.beta + 3ll * slot, beta);
+                st3(N.L + 3ll * slot, L);
+                N.rng[slot] = g.state;
+                N.rng_inc[slot] = g.inc;
+                N.last_pdf[slot] = pdf_next;
+                N.flags[slot] = flags_next;
+                N.depth[slot] = depth;
+                N.g[slot] = pg;
+            }
+        }
+        long long ring_e = 0;
+        if (kStream && live && !alive) {
+            ring_e = pg % a.stream.ring_n;
+            st3(a.stream.ring + 3 * ring_e, L);
         }
         const int sslot = warp_append(a.ps.counts + 2, shadow);
         if (shadow) {
-            a.ps.shadow_path[sslot] = i;
+            // the shadow stage adds to L[3 * t] of the state it is given for t >= 0, else to ring
+            // entry -1 - t
+            a.ps.shadow_path[sslot] = !kStream ? i : (alive ? slot : (int)(-1 - ring_e));
             put_ray(a.ps.shadow_ray, sslot, sh_o, sh_d);
             st3(a.ps.shadow_val + 3ll * sslot, sh_val);
+        }
+        if (kStream) {
+            unsigned long long m = alive ? (unsigned long long)pg : ~0ull;
+            for (int o = 16; o > 0; o >>= 1) {
+                const unsigned long long other = __shfl_xor_sync(0xffffffffu, m, o);
+                m = other < m ? other : m;
+            }
+            if ((threadIdx.x & 31) == 0 && m != ~0ull) atomicMin(&a.stream.plan->min_alive, m);
         }
     }
 }
 
-// Adds the wave's path radiance to the views' accumulation blocks. The thread of a pixel's first
-// path in the wave adds all of that pixel's paths in the wave, in sample order.
-template <typename T>
-__global__ void __launch_bounds__(kShadeBlockMax) k_accumulate(NativeArgs a, T *accum) {
-    const int stride = gridDim.x * blockDim.x;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.wave_paths; i += stride) {
-        const long long g = a.wave_first + i;
+__global__ void __launch_bounds__(kShadeBlockMax) k_shade(NativeArgs a, int cur) { shade_queue<false>(a, cur); }
+
+__global__ void __launch_bounds__(kShadeBlockMax) k_shade_stream(NativeArgs a, int cur) { shade_queue<true>(a, cur); }
+
+// Adds the radiance of paths [first, first + n) to the views' accumulation blocks. The thread of
+// a pixel's first path in the range adds all of that pixel's paths in the range, in sample order,
+// so the sums do not depend on how a render is cut into ranges. kRing: path g's radiance is at
+// ring entry g mod ring_n, else at L[g - first].
+template <typename T, bool kRing>
+__device__ __forceinline__ void accumulate_range(const NativeArgs &a, T *accum, long long first, long long n,
+                                                 const float *L) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const long long g = first + i;
         const ViewRec vw = view_of(a, find_view(a, g));
         const long long l = g - vw.first;
-        if (l >= vw.npix && g - vw.npix >= a.wave_first) continue;  // not the pixel's first path here
+        if (l >= vw.npix && g - vw.npix >= first) continue;  // not the pixel's first path here
         const long long pixel = l % vw.npix;
         T *px = accum + vw.accum + 3 * pixel;
         T acc[3] = {px[0], px[1], px[2]};
-        for (long long k = i, lk = l; k < a.wave_paths && lk < vw.paths; k += vw.npix, lk += vw.npix) {
-            acc[0] += (T)a.ps.L[3 * k];
-            acc[1] += (T)a.ps.L[3 * k + 1];
-            acc[2] += (T)a.ps.L[3 * k + 2];
+        for (long long k = i, lk = l; k < n && lk < vw.paths; k += vw.npix, lk += vw.npix) {
+            const long long e = kRing ? (first + k) % a.stream.ring_n : k;
+            acc[0] += (T)L[3 * e];
+            acc[1] += (T)L[3 * e + 1];
+            acc[2] += (T)L[3 * e + 2];
         }
         px[0] = acc[0];
         px[1] = acc[1];
         px[2] = acc[2];
     }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kShadeBlockMax) k_accumulate(NativeArgs a, T *accum) {
+    accumulate_range<T, false>(a, accum, a.wave_first, a.wave_paths, a.ps.L);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kShadeBlockMax) k_accumulate_stream(NativeArgs a, T *accum) {
+    const long long lo = a.stream.plan->acc_lo, hi = a.stream.plan->acc_hi;
+    accumulate_range<T, true>(a, accum, lo, hi - lo, a.stream.ring);
 }
 
 }  // namespace tt
@@ -878,6 +1027,7 @@ void native_release(tt_renderer *r) {
     if (r->env_cond) cudaFree(r->env_cond);
     if (r->paths) cudaFree(r->paths);
     if (r->cache_mem) cudaFree(r->cache_mem);
+    if (r->stream_mem) cudaFree(r->stream_mem);
     if (r->geom_tree) cudaFree(r->geom_tree);
     r->geom_tree = nullptr;
     r->num_geom_nodes = 0;
@@ -887,6 +1037,8 @@ void native_release(tt_renderer *r) {
     r->path_capacity = 0;
     r->cache_mem = nullptr;
     r->cache_bytes = 0;
+    r->stream_mem = nullptr;
+    r->stream_bytes = 0;
 }
 
 // Path state for `cap` paths, carved out of one allocation sized for the renderer's capacity (so
@@ -959,7 +1111,7 @@ static tt_status ensure_paths(tt_renderer *r, int cap, PathSoA &ps) {
     return TT_OK;
 }
 
-constexpr int kMaxWavePaths = 1 << 24;
+constexpr int kMaxWavePaths = 1 << 26;
 
 static int block_index(int block) {
     for (int i = 0; i < kNumBlockShapes; i++)
@@ -978,6 +1130,7 @@ struct Launch {
     int block = 0, wave = 0;
     int grid_trace = 0, grid_shade = 0, grid_gather = 0;
     bool order = false;  // order the extension queues (scratch in the path allocation)
+    bool stream = true;  // stream a render of more paths than one wave (StreamPlan)
 };
 
 // Where a render's queue ordering works: the scratch inside the path allocation and the scene
@@ -999,11 +1152,13 @@ static OrderPlan order_plan(const tt_renderer *r) {
     return o;
 }
 
-static tt_status resolve_launch(tt_renderer *r, int block, int sh, int wave, int order, Launch &L) {
+static tt_status resolve_launch(tt_renderer *r, int block, int sh, int wave, int order, int stream, Launch &L) {
     const int bi = block_index(block), si = stack_index(sh);
-    if (bi < 0 || si < 0 || wave < 1 || wave > kMaxWavePaths || (order != 0 && order != 1))
+    if (bi < 0 || si < 0 || wave < 1 || wave > kMaxWavePaths || (order != 0 && order != 1) ||
+        (stream != 0 && stream != 1))
         return fail(TT_ERR_INVALID, "launch shape: block must be 64/128/256, stack_shared 0/8/16, "
-                                    "wave_paths 1..16777216, ordered 0 or 1");
+                                    "wave_paths 1..67108864, ordered and streamed 0 or 1");
+    L.stream = stream != 0;
     L.tk = trace_kernels(block, sh);
     L.block = block;
     L.wave = wave;
@@ -1016,9 +1171,10 @@ static tt_status resolve_launch(tt_renderer *r, int block, int sh, int wave, int
         r->occ_trace[bi][si] = std::max(1, std::min(b, b2));
     }
     if (!r->occ_shade[bi]) {
-        int b = 0;
+        int b = 0, b2 = 0;
         TT_CUDA_N(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, (const void *)k_shade, block, 0));
-        r->occ_shade[bi] = std::max(1, b);
+        TT_CUDA_N(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, (const void *)k_shade_stream, block, 0));
+        r->occ_shade[bi] = std::max(1, std::min(b, b2));
     }
     L.grid_trace = r->num_sms * r->occ_trace[bi][si];
     L.grid_shade = r->num_sms * r->occ_shade[bi];
@@ -1093,8 +1249,8 @@ static NativeArgs base_args(tt_renderer *r, const tt_render_params &p, const Pat
 // Issues the kernels of `total` paths (waves of L.wave) on stream s. accum = nullptr: no
 // accumulation (autotuning trials). cache: the radiance cache of a cached render (a.cache set up),
 // queried after the second bounce and trained after every wave when `train`.
-static tt_status issue(NativeArgs a, long long total, const Launch &L, const OrderPlan &plan, void *accum,
-                       cudaStream_t s, tt_cache *cache = nullptr, bool train = false) {
+static tt_status issue_waves(NativeArgs a, long long total, const Launch &L, const OrderPlan &plan, void *accum,
+                             cudaStream_t s, tt_renderer *r, tt_cache *cache, bool train) {
     const bool f64 = (a.p.flags & TT_RENDER_ACCUM_F64) != 0;
     if (L.order && !plan.scratch) return fail(TT_ERR_INVALID, "queue ordering: no scratch for it");
     const long long qcap = std::min<long long>(L.wave, total);  // queue capacity: the path arrays' size
@@ -1115,6 +1271,7 @@ static tt_status issue(NativeArgs a, long long total, const Launch &L, const Ord
                 return fail(TT_ERR_INVALID, "cache: more training paths in a wave than training slots");
         }
         k_raygen<<<L.grid_shade, L.block, 0, s>>>(a);
+        r->launches += 1 + (accum ? 1 : 0) + (unsigned long long)a.p.max_depth * (L.order ? 8 : 3);
         for (int b = 0; b < a.p.max_depth; b++) {
             if (L.order) {  // order the queue; the probe leaves coherent queues (camera rays) alone
                 OrderOut oo;
@@ -1122,6 +1279,7 @@ static tt_status issue(NativeArgs a, long long total, const Launch &L, const Ord
                                                   plan.scratch, plan.state_at, a.err, s, &oo);
                 if (st != TT_OK) return st;
                 float *h = static_cast<float *>(oo.sorted_hits);
+                a.order.n_sorted = a.ps.counts + (b & 1);
                 a.order.sorted = oo.sorted;
                 a.order.pos = oo.pos;
                 a.order.state = oo.state;
@@ -1140,14 +1298,17 @@ static tt_status issue(NativeArgs a, long long total, const Launch &L, const Ord
                                                          a.cache.q_rgb, nrc::cache_params(cache).use_ema, a.err, s);
             if (st != TT_OK) return st;
             k_cache_resolve<<<L.grid_shade, L.block, 0, s>>>(a);
+            r->launches += 1;
         }
         if (cache && train) {
             if (a.cache.train_slots > 0) {  // the records in slot order
                 const unsigned nb = (unsigned)((a.cache.train_slots + 1023) / 1024);
                 k_cache_count<<<nb, 1024, 0, s>>>(a);
                 k_cache_compact<<<nb, 1024, 0, s>>>(a);
+                r->launches += 2;
             }
             k_cache_targets<<<L.grid_shade, L.block, 0, s>>>(a);
+            r->launches += 1;
         }
         if (accum) {
             if (f64) k_accumulate<double><<<L.grid_shade, L.block, 0, s>>>(a, (double *)accum);
@@ -1160,6 +1321,121 @@ static tt_status issue(NativeArgs a, long long total, const Launch &L, const Ord
     }
     TT_CUDA_N(cudaGetLastError());
     return TT_OK;
+}
+
+// Radiance ring entries of a streamed render of pool slots and max_depth bounces (0: too many to
+// stream; such renders run in waves).
+constexpr long long kMaxRingEntries = 1ll << 29;
+static long long stream_ring_entries(long long pool, int max_depth) {
+    const long long n = pool * (long long)max_depth;
+    return n <= kMaxRingEntries ? n : 0;
+}
+
+// The streamed render's buffers for `pool` slots and `ring` entries, carved out of one allocation
+// that only grows (a reallocation bumps paths_gen, so captured graphs are rebuilt): the ring, the
+// second copy of the path state (the first is the wave arrays of `ps`) and both copies' path
+// indices.
+static tt_status ensure_stream(tt_renderer *r, const PathSoA &ps, long long pool, long long ring, StreamView &sv) {
+    auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+    constexpr int kArrays = 11;
+    const size_t P = (size_t)pool;
+    const size_t sizes[kArrays] = {12ull * (size_t)ring, 12 * P, 12 * P, 4 * P, 8 * P, 8 * P, 4 * P, 4 * P,
+                                   8 * P, 8 * P, sizeof(StreamPlan)};
+    size_t need = 0;
+    for (size_t x : sizes) need += al(x);
+    if (r->stream_bytes < need) {
+        if (r->stream_mem) cudaFree(r->stream_mem);
+        r->stream_mem = nullptr;
+        r->stream_bytes = 0;
+        const cudaError_t e = cudaMalloc(&r->stream_mem, need);
+        if (e != cudaSuccess) return fail(TT_ERR_OOM, std::string("streamed render: ") + cudaGetErrorString(e));
+        r->stream_bytes = need;
+        r->paths_gen++;
+    }
+    char *p = static_cast<char *>(r->stream_mem);
+    void *v[kArrays];
+    for (int k = 0; k < kArrays; k++) {
+        v[k] = p;
+        p += al(sizes[k]);
+    }
+    sv.ring = (float *)v[0];
+    sv.ring_n = ring;
+    sv.st[0] = PathState{ps.beta, ps.L, ps.last_pdf, ps.rng, ps.rng_inc, ps.depth, ps.flags, (long long *)v[8]};
+    sv.st[1] = PathState{(float *)v[1], (float *)v[2], (float *)v[3], (uint64_t *)v[4], (uint64_t *)v[5],
+                         (int *)v[6], (int *)v[7], (long long *)v[9]};
+    sv.plan = (StreamPlan *)v[10];
+    return TT_OK;
+}
+
+// A streamed render of `total` paths through a pool of L.wave slots (see StreamPlan). The
+// iteration count is an upper bound fixed on the host, so the sequence can be captured: while
+// paths remain, every iteration extends a full pool, so ceil(total / pool) * max_depth
+// iterations extend every path of up to max_depth bounces, and max_depth more drain the pool;
+// iterations after the last path ends find empty queues and return at once. The final plan
+// flags the error word if any path had not ended.
+static tt_status issue_stream(NativeArgs a, long long total, const Launch &L, const OrderPlan &plan, void *accum,
+                              cudaStream_t s, tt_renderer *r) {
+    const bool f64 = (a.p.flags & TT_RENDER_ACCUM_F64) != 0;
+    if (L.order && !plan.scratch) return fail(TT_ERR_INVALID, "queue ordering: no scratch for it");
+    const long long pool = L.wave;
+    StreamView sv{};
+    tt_status st = ensure_stream(r, a.ps, pool, stream_ring_entries(pool, a.p.max_depth), sv);
+    if (st != TT_OK) return st;
+    sv.total = total;
+    a.stream = sv;
+    const long long iters = (total + pool - 1) / pool * a.p.max_depth + a.p.max_depth;
+    // init; per iteration plan, accumulate, refill, extend, shade, shadow (+ 4 ordering kernels
+    // and the hit gather); the final plan and accumulate
+    r->launches += 1 + (unsigned long long)iters * ((accum ? 6 : 5) + (L.order ? 5 : 0)) + (accum ? 2 : 1);
+    k_stream_init<<<1, 32, 0, s>>>(a);
+    for (long long it = 0; it <= iters; it++) {
+        const int c = (int)(it & 1);
+        const bool last = it == iters;
+        k_stream_plan<<<1, 32, 0, s>>>(a, c, (int)pool, last ? 1 : 0);
+        if (accum) {
+            if (f64) k_accumulate_stream<double><<<L.grid_shade, L.block, 0, s>>>(a, (double *)accum);
+            else k_accumulate_stream<float><<<L.grid_shade, L.block, 0, s>>>(a, (float *)accum);
+        }
+        if (last) break;
+        k_regen<<<L.grid_shade, L.block, 0, s>>>(a, c);
+        if (L.order) {
+            // the survivors (queue slots below new_at) are ordered; the new camera rays behind
+            // them are coherent already
+            OrderOut oo;
+            const int *n_sorted = &sv.plan->new_at;
+            st = reorder_rays(a.ps.ray[c], pool, n_sorted, plan.lo, plan.hi, plan.scratch, plan.state_at, a.err, s, &oo);
+            if (st != TT_OK) return st;
+            float *h = static_cast<float *>(oo.sorted_hits);
+            a.order.n_sorted = n_sorted;
+            a.order.sorted = oo.sorted;
+            a.order.pos = oo.pos;
+            a.order.state = oo.state;
+            a.order.hit_t = h;
+            a.order.hit_u = h + pool;
+            a.order.hit_v = h + 2 * pool;
+            a.order.hit_prim = reinterpret_cast<int *>(h + 3 * pool);
+        }
+        L.tk.extend<<<L.grid_trace, L.block, 0, s>>>(a, c);
+        if (L.order) k_order_gather_hits<<<L.grid_gather, 256, 0, s>>>(a, c);
+        k_shade_stream<<<L.grid_shade, L.block, 0, s>>>(a, c);
+        NativeArgs as = a;  // shadow rays of survivors add to their state in the next queue
+        as.ps.L = sv.st[c ^ 1].L;
+        L.tk.shadow<<<L.grid_trace, L.block, 0, s>>>(as);
+    }
+    TT_CUDA_N(cudaGetLastError());
+    return TT_OK;
+}
+
+// Issues the kernels of `total` paths on stream s: streamed through a pool of L.wave slots when
+// they are more than one wave (plain renders), else in waves.
+static bool streamed(long long total, const Launch &L, int max_depth, const tt_cache *cache) {
+    return L.stream && !cache && total > L.wave && stream_ring_entries(L.wave, max_depth) > 0;
+}
+
+static tt_status issue(NativeArgs a, long long total, const Launch &L, const OrderPlan &plan, void *accum,
+                       cudaStream_t s, tt_renderer *r, tt_cache *cache = nullptr, bool train = false) {
+    if (streamed(total, L, a.p.max_depth, cache)) return issue_stream(a, total, L, plan, accum, s, r);
+    return issue_waves(a, total, L, plan, accum, s, r, cache, train);
 }
 
 // Query and training buffers of a cached render: `queries` query slots, `records` training slots.
@@ -1220,7 +1496,7 @@ struct tt_batch {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     void *graph_accum = nullptr;
-    int graph_block = 0, graph_stack = -1, graph_wave = 0, graph_order = -1;
+    int graph_block = 0, graph_stack = -1, graph_wave = 0, graph_order = -1, graph_stream = -1;
     unsigned long long graph_paths_gen = 0;
     int graph_kernels = 0;
 };
@@ -1270,7 +1546,7 @@ tt_status tt_render_native(tt_renderer *r, const tt_camera_meta *cam, const tt_r
     if (st != TT_OK) return st;
     const ViewRec v = make_view(*cam, p->spp, p->sample_offset, p->seed, 0, 0);
     Launch L;
-    st = resolve_launch(r, r->launch_block, r->launch_stack, r->launch_wave, r->launch_order, L);
+    st = resolve_launch(r, r->launch_block, r->launch_stack, r->launch_wave, r->launch_order, r->launch_stream, L);
     if (st != TT_OK) return st;
     PathSoA ps;
     st = ensure_paths(r, (int)std::min<long long>(v.paths, L.wave), ps);
@@ -1279,7 +1555,7 @@ tt_status tt_render_native(tt_renderer *r, const tt_camera_meta *cam, const tt_r
     a.views = nullptr;
     a.n_views = 1;
     a.view0 = v;
-    return issue(a, v.paths, L, order_plan(r), d_accum, (cudaStream_t)stream);
+    return issue(a, v.paths, L, order_plan(r), d_accum, (cudaStream_t)stream, r);
 }
 
 tt_status tt_render_cached(tt_renderer *r, tt_cache *c, const tt_camera_meta *cam, const tt_render_params *p,
@@ -1291,7 +1567,7 @@ tt_status tt_render_cached(tt_renderer *r, tt_cache *c, const tt_camera_meta *ca
     const tt_cache_params &cp = nrc::cache_params(c);
     const ViewRec v = make_view(*cam, p->spp, p->sample_offset, p->seed, 0, 0);
     Launch L;
-    st = resolve_launch(r, r->launch_block, r->launch_stack, r->launch_wave, r->launch_order, L);
+    st = resolve_launch(r, r->launch_block, r->launch_stack, r->launch_wave, r->launch_order, r->launch_stream, L);
     if (st != TT_OK) return st;
     const int wave = (int)std::min<long long>(v.paths, L.wave);
     PathSoA ps;
@@ -1308,18 +1584,20 @@ tt_status tt_render_cached(tt_renderer *r, tt_cache *c, const tt_camera_meta *ca
     a.cache.train = train ? 1 : 0;
     a.cache.spread_c = cp.spread_c;
     a.cache.train_stride = 1;
-    return issue(a, v.paths, L, order_plan(r), d_accum, (cudaStream_t)stream, c, train != 0);
+    return issue(a, v.paths, L, order_plan(r), d_accum, (cudaStream_t)stream, r, c, train != 0);
 }
 
 tt_status tt_renderer_set_launch(tt_renderer *r, const tt_launch_shape *shape) {
     if (!r || !shape) return fail(TT_ERR_INVALID, "null argument");
     Launch L;
-    tt_status st = resolve_launch(r, shape->block, shape->stack_shared, shape->wave_paths, shape->ordered, L);
+    tt_status st = resolve_launch(r, shape->block, shape->stack_shared, shape->wave_paths, shape->ordered,
+                                  shape->streamed, L);
     if (st != TT_OK) return st;
     r->launch_block = shape->block;
     r->launch_stack = shape->stack_shared;
     r->launch_wave = shape->wave_paths;
     r->launch_order = shape->ordered;
+    r->launch_stream = shape->streamed;
     return TT_OK;
 }
 
@@ -1329,7 +1607,15 @@ tt_status tt_renderer_get_launch(const tt_renderer *r, tt_launch_shape *shape) {
     shape->stack_shared = r->launch_stack;
     shape->wave_paths = r->launch_wave;
     shape->ordered = r->launch_order;
+    shape->streamed = r->launch_stream;
     shape->ms = 0.0f;
+    return TT_OK;
+}
+
+tt_status tt_renderer_launches(tt_renderer *r, uint64_t *out, int32_t reset) {
+    if (!r || !out) return fail(TT_ERR_INVALID, "null argument");
+    *out = r->launches;
+    if (reset) r->launches = 0;
     return TT_OK;
 }
 
@@ -1385,20 +1671,26 @@ tt_status tt_batch_render(tt_batch *b, void *d_accum, int use_graph, void *strea
     if (!b || !d_accum) return fail(TT_ERR_INVALID, "null argument");
     tt_renderer *r = b->r;
     Launch L;
-    tt_status st = resolve_launch(r, r->launch_block, r->launch_stack, r->launch_wave, r->launch_order, L);
+    tt_status st = resolve_launch(r, r->launch_block, r->launch_stack, r->launch_wave, r->launch_order, r->launch_stream, L);
     if (st != TT_OK) return st;
     PathSoA ps;
     st = ensure_paths(r, (int)std::min<long long>(b->total_paths, L.wave), ps);
     if (st != TT_OK) return st;
+    if (streamed(b->total_paths, L, b->p.max_depth, nullptr)) {  // allocate before any capture
+        StreamView sv;
+        st = ensure_stream(r, ps, L.wave, stream_ring_entries(L.wave, b->p.max_depth), sv);
+        if (st != TT_OK) return st;
+    }
     const NativeArgs a = batch_args(b, ps);
-    if (!use_graph) return issue(a, b->total_paths, L, order_plan(r), d_accum, (cudaStream_t)stream);
+    if (!use_graph) return issue(a, b->total_paths, L, order_plan(r), d_accum, (cudaStream_t)stream, r);
     const bool stale = !b->exec || b->graph_accum != d_accum || b->graph_block != L.block ||
                        b->graph_stack != r->launch_stack || b->graph_wave != L.wave || b->graph_order != r->launch_order ||
+                       b->graph_stream != r->launch_stream ||
                        b->graph_paths_gen != r->paths_gen;
     if (stale) {
         drop_graph(b);
         TT_CUDA_N(cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal));
-        st = issue(a, b->total_paths, L, order_plan(r), d_accum, b->cap);
+        st = issue(a, b->total_paths, L, order_plan(r), d_accum, b->cap, r);
         cudaGraph_t g = nullptr;
         const cudaError_t e = cudaStreamEndCapture(b->cap, &g);
         if (st != TT_OK) {
@@ -1420,6 +1712,7 @@ tt_status tt_batch_render(tt_batch *b, void *d_accum, int use_graph, void *strea
         b->graph_stack = r->launch_stack;
         b->graph_wave = L.wave;
         b->graph_order = r->launch_order;
+        b->graph_stream = r->launch_stream;
         b->graph_paths_gen = r->paths_gen;
     }
     TT_CUDA_N(cudaGraphLaunch(b->exec, (cudaStream_t)stream));
@@ -1437,12 +1730,15 @@ tt_status tt_batch_autotune(tt_batch *b, int64_t sample_paths, void *stream, tt_
     if (!b) return fail(TT_ERR_INVALID, "null batch");
     tt_renderer *r = b->r;
     cudaStream_t s = (cudaStream_t)stream;
-    const long long sample = std::min<long long>(b->total_paths, sample_paths > 0 ? sample_paths : (8ll << 20));
-    static const int kWaves[] = {1 << 20, 1 << 21, 1 << 22};
+    const long long sample = std::min<long long>(b->total_paths, sample_paths > 0 ? sample_paths : (1ll << 27));
+    // a wave's last bounces trace few rays at the latency of the longest ones, so larger waves
+    // (or a streamed pool) pay that tail less often; the sample has to span more than one of the
+    // largest waves to show it
+    static const int kWaves[] = {1 << 20, 1 << 22, 1 << 24, 1 << 26};
     PathSoA ps;
     const int order_was = r->launch_order;
     r->launch_order = 1;  // the trials with ordered queues need its scratch
-    tt_status st = ensure_paths(r, (int)std::min<long long>(sample, kWaves[2]), ps);
+    tt_status st = ensure_paths(r, (int)std::min<long long>(sample, kWaves[3]), ps);
     r->launch_order = order_was;
     if (st != TT_OK) return st;
     NativeArgs a = batch_args(b, ps);
@@ -1451,41 +1747,58 @@ tt_status tt_batch_autotune(tt_batch *b, int64_t sample_paths, void *stream, tt_
     TT_CUDA_N(cudaEventCreate(&e0));
     TT_CUDA_N(cudaEventCreate(&e1));
     float best = 3.4e38f;
-    tt_launch_shape best_shape{r->launch_block, r->launch_stack, r->launch_wave, r->launch_order, 0.0f};
+    tt_launch_shape best_shape{r->launch_block, r->launch_stack, r->launch_wave, r->launch_order, r->launch_stream, 0.0f};
     int count = 0;
-    for (int bi = 0; bi < kNumBlockShapes; bi++)
-        for (int si = 0; si < kNumStackShapes; si++)
-            for (int wave : kWaves)
-                for (int order = 0; order < 2; order++) {
+    // times the sample under one shape (buffers allocated before the timed region)
+    auto trial = [&](int block, int sh, int wave, int order, int strm) -> tt_status {
+        Launch L;
+        tt_status t = resolve_launch(r, block, sh, wave, order, strm, L);
+        if (t == TT_OK && streamed(sample, L, b->p.max_depth, nullptr)) {
+            StreamView sv;
+            t = ensure_stream(r, ps, wave, stream_ring_entries(wave, b->p.max_depth), sv);
+        }
+        if (t == TT_OK) t = issue(a, std::min<long long>(sample, 1 << 16), L, plan, nullptr, s, r);  // warm-up
+        cudaError_t e = cudaEventRecord(e0, s);
+        if (t == TT_OK && e == cudaSuccess) t = issue(a, sample, L, plan, nullptr, s, r);
+        if (e == cudaSuccess) e = cudaEventRecord(e1, s);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        float ms = 0.0f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        if (t != TT_OK) return t;
+        if (e != cudaSuccess) return cuda_fail_n(e, "autotune timing");
+        const tt_launch_shape shape{block, sh, wave, order, strm, ms};
+        if (results && count < max_results) results[count] = shape;
+        count++;
+        if (ms < best) {
+            best = ms;
+            best_shape = shape;
+        }
+        return TT_OK;
+    };
+    // stage 1: threads per block x shared stack entries, at 2^22-path waves, ordered and streamed
+    for (int bi = 0; bi < kNumBlockShapes && st == TT_OK; bi++)
+        for (int si = 0; si < kNumStackShapes && st == TT_OK; si++)
+            st = trial(kBlockShapes[bi], kStackShapes[si], kWaves[1], 1, 1);
+    // stage 2: the fastest of those at every wave size, ordered or not, streamed or in waves (a
+    // sample that fits one wave is the same either way)
+    const int bb = best_shape.block, bs = best_shape.stack_shared;
+    for (int wave : kWaves)
+        for (int order = 0; order < 2; order++)
+            for (int strm = 0; strm < 2; strm++) {
+                if (st != TT_OK) break;
                 if (wave > kWaves[0] && wave / 2 >= sample) continue;  // the same as a smaller wave
-                Launch L;
-                st = resolve_launch(r, kBlockShapes[bi], kStackShapes[si], wave, order, L);
-                if (st == TT_OK) st = issue(a, std::min<long long>(sample, 1 << 16), L, plan, nullptr, s);  // warm-up
-                cudaError_t e = cudaEventRecord(e0, s);
-                if (st == TT_OK && e == cudaSuccess) st = issue(a, sample, L, plan, nullptr, s);
-                if (e == cudaSuccess) e = cudaEventRecord(e1, s);
-                if (e == cudaSuccess) e = cudaEventSynchronize(e1);
-                float ms = 0.0f;
-                if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
-                if (st != TT_OK || e != cudaSuccess) {
-                    cudaEventDestroy(e0);
-                    cudaEventDestroy(e1);
-                    return st != TT_OK ? st : cuda_fail_n(e, "autotune timing");
-                }
-                const tt_launch_shape shape{kBlockShapes[bi], kStackShapes[si], wave, order, ms};
-                if (results && count < max_results) results[count] = shape;
-                count++;
-                if (ms < best) {
-                    best = ms;
-                    best_shape = shape;
-                }
+                if (strm && sample <= wave) continue;
+                if (wave == kWaves[1] && order == 1 && strm == 1) continue;  // timed in stage 1
+                st = trial(bb, bs, wave, order, strm);
             }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    if (st != TT_OK) return st;
     r->launch_block = best_shape.block;
     r->launch_stack = best_shape.stack_shared;
     r->launch_wave = best_shape.wave_paths;
     r->launch_order = best_shape.ordered;
+    r->launch_stream = best_shape.streamed;
     if (n_results) *n_results = count;
     return TT_OK;
 }
