@@ -375,7 +375,8 @@ typedef struct tt_sample_probe {
     float eval[3];       /* what 0: f |cos| that bsdf_eval gives for wi */
     int32_t specular;
     uint32_t pcg_out[8]; /* what 2: the stream's first eight outputs */
-    int32_t pad1[4];
+    int32_t texel;       /* what 1: the texel (row * env_w + column) the CDF searches chose */
+    int32_t pad1[3];
 } tt_sample_probe;
 /* Diagnostic (no counterpart in the reference, whose samplers are other ones): runs the native
  * path tracer's own sampling code on n device queries. what 0: the BSDF sampler of the query's

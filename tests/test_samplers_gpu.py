@@ -293,3 +293,52 @@ def test_environment_sampling_follows_luminance_times_sin_theta(renderer):
     assert np.quantile(np.abs(out["pdf"][big] / ref[big] - 1.0), 0.999) < 1e-2
     # env_pdf (what light sampling's MIS weight uses for a BSDF-sampled direction) agrees
     assert np.quantile(np.abs(out["eval_pdf"] / out["pdf"] - 1.0), 0.999) < 1e-3
+
+
+def test_environment_guide_tables_give_the_full_inverse_cdf(renderer):
+    """The environment sampler searches each CDF only between the entries of a guide table (the
+    answers at u = k / g); the texel it picks must be the full inverse-CDF search's answer (the
+    smallest i with cdf[i + 1] > u) for uniform draws and for draws placed exactly on CDF entries,
+    on guide grid points and one ulp either side of them."""
+    r, sc = renderer
+    h, w = sc.env().shape[:2]
+    marg, cond = r.env_tables(w, h)
+    rng = np.random.default_rng(7)
+    u1 = [rng.random(1 << 20, dtype=np.float32)]
+    u2 = [rng.random(1 << 20, dtype=np.float32)]
+    edges = np.concatenate([marg[1:-1], np.arange(1, 1024, dtype=np.float32) / np.float32(1024)])
+    for e in (edges, np.nextafter(edges, np.float32(0)), np.nextafter(edges, np.float32(1))):
+        u1.append(e.astype(np.float32))
+        u2.append(rng.random(e.size, dtype=np.float32))
+    rows = rng.integers(0, h, 4096)  # draws on the conditional CDFs' own entries
+    for k in range(4):
+        cols = rng.integers(1, w, rows.size)
+        v = cond[rows, cols]
+        if k == 1:
+            v = np.nextafter(v, np.float32(0))
+        elif k == 2:
+            v = np.nextafter(v, np.float32(1))
+        elif k == 3:
+            v = (cols // 4).astype(np.float32) / np.float32(512)
+        mid = ((marg[rows] + marg[rows + 1]) * np.float32(0.5)).astype(np.float32)
+        u1.append(mid)
+        u2.append(v.astype(np.float32))
+    u1 = np.concatenate(u1)
+    u2 = np.concatenate(u2)
+    keep = (u1 < 1) & (u2 < 1) & (u1 >= 0) & (u2 >= 0)
+    u1, u2 = u1[keep], u2[keep]
+    q = np.zeros(u1.size, Renderer.SAMPLE_PROBE_DTYPE)
+    q["u"][:, 0] = u1
+    q["u"][:, 1] = u2
+    out = r.sample_probe(Renderer.PROBE_ENV, q)
+    y = np.minimum(np.searchsorted(marg[1:], u1, side="right"), h - 1)
+    x = np.empty_like(y)
+    for yy in np.unique(y):
+        sel = y == yy
+        x[sel] = np.minimum(np.searchsorted(cond[yy, 1:], u2[sel], side="right"), w - 1)
+    has_row = marg[y + 1] > marg[y]
+    assert (out["texel"][~has_row] == -1).all()
+    got = out["texel"][has_row]
+    want = (y * w + x)[has_row]
+    assert has_row.mean() > 0.99
+    assert np.array_equal(got, want), f"{(got != want).sum()} of {got.size} texels differ from the full search"

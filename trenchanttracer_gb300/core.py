@@ -303,7 +303,7 @@ class Renderer:
                                    ("u", "<f4", 3), ("pad0", "<i4"), ("pcg_state", "<u8"), ("pcg_seq", "<u8"),
                                    ("wi", "<f4", 3), ("weight", "<f4", 3), ("pdf", "<f4"), ("eval_pdf", "<f4"),
                                    ("eval", "<f4", 3), ("specular", "<i4"), ("pcg_out", "<u4", 8),
-                                   ("pad1", "<i4", 4)])
+                                   ("texel", "<i4"), ("pad1", "<i4", 3)])
     PROBE_BSDF, PROBE_ENV, PROBE_PCG32 = 0, 1, 2
 
     def sample_probe(self, what: int, queries: np.ndarray, stream: int = 0) -> np.ndarray:

@@ -33,6 +33,9 @@ struct tt_renderer {
     // native path tracer
     float *env_marg = nullptr;  // env_h + 1
     float *env_cond = nullptr;  // env_h * (env_w + 1)
+    // guide tables of the CDFs: env_gm + 1 entries for the marginal, then env_gc + 1 per row
+    int *env_guide = nullptr;
+    int env_gm = 0, env_gc = 0;
     void *paths = nullptr;      // path state, queues and shadow rays for path_capacity paths
     size_t paths_bytes = 0;
     int path_capacity = 0;

@@ -28,6 +28,12 @@ struct EnvView {
     const float4 *tex;  // w*h radiance
     const float *marg;  // h+1 marginal CDF over rows
     const float *cond;  // h*(w+1) conditional CDFs per row
+    // Guide tables (gm, gc powers of two): guide_m[k] is the marginal search's answer for
+    // u = k / gm, and guide_c[y * (gc + 1) + k] row y's for u = k / gc. The answer for any u lies
+    // between the entries of the two grid points around it, so the search runs on that range
+    // only and returns the index the full search would.
+    const int *guide_m, *guide_c;
+    int gm, gc;
     int w, h;
     float scale;
 };

@@ -97,8 +97,8 @@ __device__ __forceinline__ float env_pdf(const EnvView &e, int texel, float sin_
     return PT_MUL(PT_MUL(pr, pc), jac);
 }
 
-__device__ __forceinline__ int cdf_search(const float *cdf, int n, float u) {
-    int lo = 0, hi = n - 1;
+// The smallest i in [lo, hi] with cdf[i + 1] > u, else hi: over [0, n - 1] the inverse CDF.
+__device__ __forceinline__ int cdf_search_in(const float *cdf, int lo, int hi, float u) {
     while (lo < hi) {
         const int mid = (lo + hi) >> 1;
         if (__ldg(cdf + mid + 1) <= u) lo = mid + 1;
@@ -107,13 +107,26 @@ __device__ __forceinline__ int cdf_search(const float *cdf, int n, float u) {
     return lo;
 }
 
-// Samples a direction by the 2D CDF. Returns pdf (0 = no sample), radiance and direction.
-__device__ __forceinline__ float env_sample(const EnvView &e, float u1, float u2, V3 &dir, V3 &le) {
-    const int y = cdf_search(e.marg, e.h, u1);
+__device__ __forceinline__ int cdf_search(const float *cdf, int n, float u) { return cdf_search_in(cdf, 0, n - 1, u); }
+
+// The same answer, searched between the guide entries of the grid points k / g <= u < (k + 1) / g
+// (g a power of two, so u * g and k / g are exact); the answer is monotone in u.
+__device__ __forceinline__ int cdf_search_guided(const float *cdf, const int *guide, int g, float u) {
+    int k = (int)(u * (float)g);
+    k = k < 0 ? 0 : (k >= g ? g - 1 : k);
+    return cdf_search_in(cdf, __ldg(guide + k), __ldg(guide + k + 1), u);
+}
+
+// Samples a direction by the 2D CDF. Returns pdf (0 = no sample), radiance, direction and the
+// chosen texel (-1: a row without power).
+__device__ __forceinline__ float env_sample(const EnvView &e, float u1, float u2, V3 &dir, V3 &le, int &texel) {
+    const int y = cdf_search_guided(e.marg, e.guide_m, e.gm, u1);
     const float m0 = __ldg(e.marg + y), m1 = __ldg(e.marg + y + 1);
+    texel = -1;
     if (!(m1 > m0)) return 0.0f;
     const float *row = e.cond + (size_t)y * (e.w + 1);
-    const int x = cdf_search(row, e.w, u2);
+    const int x = cdf_search_guided(row, e.guide_c + (size_t)y * (e.gc + 1), e.gc, u2);
+    texel = y * e.w + x;
     const float c0 = __ldg(row + x), c1 = __ldg(row + x + 1);
     if (!(c1 > c0)) return 0.0f;
     float dv = PT_DIV(PT_SUB(u1, m0), PT_SUB(m1, m0));
@@ -125,7 +138,6 @@ __device__ __forceinline__ float env_sample(const EnvView &e, float u1, float u2
     float st;
     dir = uv_to_dir(u, v, st);
     if (st <= 0.0f) return 0.0f;
-    const int texel = y * e.w + x;
     le = env_radiance(e, texel);
     const float jac = PT_DIV((float)e.w * (float)e.h, PT_MUL(PT_MUL(2.0f * kPi, kPi), st));
     return PT_MUL(PT_MUL(PT_SUB(m1, m0), PT_SUB(c1, c0)), jac);
@@ -695,7 +707,8 @@ __device__ __forceinline__ void shade_queue(const NativeArgs &a, int cur) {
                 if (nee) {
                     const float u1 = uniform(g), u2 = uniform(g);
                     V3 wi, le;
-                    const float pl = env_sample(a.env, u1, u2, wi, le);
+                    int texel;
+                    const float pl = env_sample(a.env, u1, u2, wi, le, texel);
                     if (pl > 0.0f) {
                         float pb;
                         const V3 fc = bsdf_eval(m, nl, wo, wi, pb);
@@ -837,7 +850,8 @@ __global__ void k_sample_probe(const MaterialRec *materials, int num_materials, 
             for (int k = 0; k < 8; k++) r.pcg_out[k] = pcg32(g);
         } else if (what == 1) {
             V3 dir(0.f, 0.f, 0.f), le(0.f, 0.f, 0.f);
-            r.pdf = env.w > 0 ? env_sample(env, r.u[0], r.u[1], dir, le) : 0.0f;
+            r.texel = -1;
+            r.pdf = env.w > 0 ? env_sample(env, r.u[0], r.u[1], dir, le, r.texel) : 0.0f;
             st3(r.wi, dir);
             st3(r.weight, le);
             const float st = PT_SQRT(fmaxf(0.0f, PT_FMA(-dir.y, dir.y, 1.0f)));
@@ -886,6 +900,20 @@ __global__ void k_env_rows(const float4 *tex, int w, int h, float *cond, double 
         const float wt = PT_MUL(luminance(c.x, c.y, c.z), st);
         acc2 += (double)(wt > 0.0f ? wt : 0.0f);
         row[x + 1] = acc > 0.0 ? __double2float_rn(acc2 / acc) : PT_DIV((float)(x + 1), (float)w);
+    }
+}
+
+// Guide entries: the full search's answer at u = k / gm (marginal) and k / gc (each row).
+__global__ void k_env_guides(const float *marg, const float *cond, int w, int h, int gm, int gc, int *guide) {
+    const long long n = (long long)(gm + 1) + (long long)h * (gc + 1);
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        if (i <= gm) {
+            guide[i] = cdf_search(marg, h, (float)i * (1.0f / (float)gm));
+        } else {
+            const long long j = i - (gm + 1);
+            const int y = (int)(j / (gc + 1)), k = (int)(j % (gc + 1));
+            guide[i] = cdf_search(cond + (size_t)y * (w + 1), w, (float)k * (1.0f / (float)gc));
+        }
     }
 }
 
@@ -1016,6 +1044,17 @@ tt_status native_setup(tt_renderer *r, const std::vector<GeomRec> &geoms) {
     TT_CUDA_N(cudaMalloc(&rowsum, sizeof(double) * h));
     k_env_rows<<<(h + 127) / 128, 128>>>(r->env, w, h, r->env_cond, rowsum);
     k_env_marginal<<<1, 1>>>(rowsum, h, r->env_marg);
+    auto pow2_at_least = [](int x) {
+        int p = 1;
+        while (p < x) p <<= 1;
+        return p;
+    };
+    r->env_gm = pow2_at_least(h);
+    r->env_gc = pow2_at_least(std::max(1, w / 4));
+    const long long guides = (long long)(r->env_gm + 1) + (long long)h * (r->env_gc + 1);
+    TT_CUDA_N(cudaMalloc(&r->env_guide, sizeof(int) * guides));
+    k_env_guides<<<(unsigned)std::min<long long>((guides + 255) / 256, 4096), 256>>>(
+        r->env_marg, r->env_cond, w, h, r->env_gm, r->env_gc, r->env_guide);
     cudaError_t e = cudaDeviceSynchronize();
     cudaFree(rowsum);
     if (e != cudaSuccess) return cuda_fail_n(e, "environment tables");
@@ -1025,6 +1064,8 @@ tt_status native_setup(tt_renderer *r, const std::vector<GeomRec> &geoms) {
 void native_release(tt_renderer *r) {
     if (r->env_marg) cudaFree(r->env_marg);
     if (r->env_cond) cudaFree(r->env_cond);
+    if (r->env_guide) cudaFree(r->env_guide);
+    r->env_guide = nullptr;
     if (r->paths) cudaFree(r->paths);
     if (r->cache_mem) cudaFree(r->cache_mem);
     if (r->stream_mem) cudaFree(r->stream_mem);
@@ -1236,6 +1277,10 @@ static NativeArgs base_args(tt_renderer *r, const tt_render_params &p, const Pat
     a.env.tex = r->env;
     a.env.marg = r->env_marg;
     a.env.cond = r->env_cond;
+    a.env.guide_m = r->env_guide;
+    a.env.guide_c = r->env_guide ? r->env_guide + r->env_gm + 1 : nullptr;
+    a.env.gm = r->env_gm;
+    a.env.gc = r->env_gc;
     a.env.w = r->env_w;
     a.env.h = r->env_h;
     a.env.scale = p.env_scale;
@@ -1823,6 +1868,10 @@ tt_status tt_native_sample_probe(const tt_renderer *r, int32_t what, tt_sample_p
     env.tex = r->env;
     env.marg = r->env_marg;
     env.cond = r->env_cond;
+    env.guide_m = r->env_guide;
+    env.guide_c = r->env_guide ? r->env_guide + r->env_gm + 1 : nullptr;
+    env.gm = r->env_gm;
+    env.gc = r->env_gc;
     env.w = r->env_w;
     env.h = r->env_h;
     env.scale = 1.0f;
