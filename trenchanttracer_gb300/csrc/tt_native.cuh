@@ -112,6 +112,14 @@ struct OrderView {
     const int *n_sorted;
 };
 
+// Ordering of the shadow queue: when order_built(state), k_shadow traces the queue in the order of
+// `sorted` and takes each ray's path and value from its original slot src[p].
+struct ShadowOrderView {
+    const float4 *sorted;  // nullptr: ordering off
+    const int *src;
+    const unsigned long long *state;
+};
+
 // Path state by index: the state slot of a path in waves, the queue slot in a streamed render.
 struct PathState {
     float *beta, *L;  // 3 per path
@@ -168,6 +176,7 @@ struct NativeArgs {
     const struct GeomNode *gnodes;  // box hierarchy over the analytic objects, or nullptr
     const int *gidx;
     OrderView order;
+    ShadowOrderView shadow_order;
 };
 
 __device__ __forceinline__ int find_view(const NativeArgs &a, long long g) {

@@ -65,6 +65,9 @@ __global__ void __launch_bounds__(kBlock) k_shadow(NativeArgs a) {
     TravStack<kSh, kBlock> stack;
     stack.sh = sh_stack + threadIdx.x;
     uint32_t err = 0;
+    // an ordered queue: rays in sorted order, each ray's path and value at its original slot
+    const bool ordered = a.shadow_order.sorted && order_built(a.shadow_order.state);
+    const float4 *rays = ordered ? a.shadow_order.sorted : a.ps.shadow_ray;
     for (;;) {
         int base = 0;
         if (lane == 0) base = atomicAdd(a.ps.counts + 4, 32);
@@ -73,7 +76,7 @@ __global__ void __launch_bounds__(kBlock) k_shadow(NativeArgs a) {
         const int j = base + lane;
         const unsigned mask = __ballot_sync(0xffffffffu, j < n);
         if (j < n) {
-            const float4 r0 = a.ps.shadow_ray[2 * j], r1 = a.ps.shadow_ray[2 * j + 1];
+            const float4 r0 = rays[2 * j], r1 = rays[2 * j + 1];
             const TraceResult tr = traverse_on<false>(stack, a.bvh, r0, r1, err);
             bool blocked = tr.addr >= 0;
             if (a.num_geoms) {
@@ -83,12 +86,15 @@ __global__ void __launch_bounds__(kBlock) k_shadow(NativeArgs a) {
                              true);
                 blocked = blocked || prim != -1;
             }
-            if (!blocked) {
+            const int src = ordered ? a.shadow_order.src[j] : j;
+            if ((unsigned)src >= (unsigned)n) {  // not reachable with a consistent ordering
+                err |= kErrOrder;
+            } else if (!blocked) {
                 // a path's radiance: L[3 * t] for t >= 0, else (an ended path of a streamed
                 // render) ring entry -1 - t
-                const int t = a.ps.shadow_path[j];
+                const int t = a.ps.shadow_path[src];
                 float *L = t >= 0 ? a.ps.L + 3ll * t : a.stream.ring + 3ll * (-1ll - t);
-                const float *c = a.ps.shadow_val + 3ll * j;
+                const float *c = a.ps.shadow_val + 3ll * src;
                 L[0] = PT_ADD(L[0], c[0]);
                 L[1] = PT_ADD(L[1], c[1]);
                 L[2] = PT_ADD(L[2], c[2]);

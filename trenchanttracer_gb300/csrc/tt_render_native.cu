@@ -1294,6 +1294,21 @@ static NativeArgs base_args(tt_renderer *r, const tt_render_params &p, const Pat
 // Issues the kernels of `total` paths (waves of L.wave) on stream s. accum = nullptr: no
 // accumulation (autotuning trials). cache: the radiance cache of a cached render (a.cache set up),
 // queried after the second bounce and trained after every wave when `train`.
+// Whether shade can queue shadow rays: they sample the environment light.
+static bool has_shadows(const NativeArgs &a) { return a.env.w > 0 && !(a.p.flags & TT_RENDER_NO_ENV_SAMPLING); }
+
+// Orders the shadow queue (a.ps.counts[2] rays of at most cap) for the shadow stage.
+static tt_status order_shadows(NativeArgs &a, long long cap, const OrderPlan &plan, cudaStream_t s) {
+    OrderOut so;
+    const tt_status st = reorder_rays(a.ps.shadow_ray, cap, a.ps.counts + 2, plan.lo, plan.hi, plan.scratch,
+                                      plan.state_at, a.err, s, &so, true);
+    if (st != TT_OK) return st;
+    a.shadow_order.sorted = so.sorted;
+    a.shadow_order.src = so.src;
+    a.shadow_order.state = so.state;
+    return TT_OK;
+}
+
 static tt_status issue_waves(NativeArgs a, long long total, const Launch &L, const OrderPlan &plan, void *accum,
                              cudaStream_t s, tt_renderer *r, tt_cache *cache, bool train) {
     const bool f64 = (a.p.flags & TT_RENDER_ACCUM_F64) != 0;
@@ -1316,7 +1331,7 @@ static tt_status issue_waves(NativeArgs a, long long total, const Launch &L, con
                 return fail(TT_ERR_INVALID, "cache: more training paths in a wave than training slots");
         }
         k_raygen<<<L.grid_shade, L.block, 0, s>>>(a);
-        r->launches += 1 + (accum ? 1 : 0) + (unsigned long long)a.p.max_depth * (L.order ? 8 : 3);
+        r->launches += 1 + (accum ? 1 : 0) + (unsigned long long)a.p.max_depth * (L.order ? (has_shadows(a) ? 12 : 8) : 3);
         for (int b = 0; b < a.p.max_depth; b++) {
             if (L.order) {  // order the queue; the probe leaves coherent queues (camera rays) alone
                 OrderOut oo;
@@ -1336,6 +1351,10 @@ static tt_status issue_waves(NativeArgs a, long long total, const Launch &L, con
             L.tk.extend<<<L.grid_trace, L.block, 0, s>>>(a, b & 1);
             if (L.order) k_order_gather_hits<<<L.grid_gather, 256, 0, s>>>(a, b & 1);
             k_shade<<<L.grid_shade, L.block, 0, s>>>(a, b & 1);
+            if (L.order && has_shadows(a)) {  // the shadow queue too (scratch shared with the extension queue's)
+                const tt_status st = order_shadows(a, qcap, plan, s);
+                if (st != TT_OK) return st;
+            }
             L.tk.shadow<<<L.grid_trace, L.block, 0, s>>>(a);
         }
         if (cache) {  // every path queries at most once, so all queries of the wave fit
@@ -1430,8 +1449,10 @@ static tt_status issue_stream(NativeArgs a, long long total, const Launch &L, co
     a.stream = sv;
     const long long iters = (total + pool - 1) / pool * a.p.max_depth + a.p.max_depth;
     // init; per iteration plan, accumulate, refill, extend, shade, shadow (+ 4 ordering kernels
-    // and the hit gather); the final plan and accumulate
-    r->launches += 1 + (unsigned long long)iters * ((accum ? 6 : 5) + (L.order ? 5 : 0)) + (accum ? 2 : 1);
+    // and the hit gather for the extension queue, 4 for the shadow queue); the final plan and
+    // accumulate
+    r->launches += 1 + (unsigned long long)iters * ((accum ? 6 : 5) + (L.order ? (has_shadows(a) ? 9 : 5) : 0)) +
+                   (accum ? 2 : 1);
     k_stream_init<<<1, 32, 0, s>>>(a);
     for (long long it = 0; it <= iters; it++) {
         const int c = (int)(it & 1);
@@ -1463,6 +1484,10 @@ static tt_status issue_stream(NativeArgs a, long long total, const Launch &L, co
         L.tk.extend<<<L.grid_trace, L.block, 0, s>>>(a, c);
         if (L.order) k_order_gather_hits<<<L.grid_gather, 256, 0, s>>>(a, c);
         k_shade_stream<<<L.grid_shade, L.block, 0, s>>>(a, c);
+        if (L.order && has_shadows(a)) {
+            st = order_shadows(a, pool, plan, s);
+            if (st != TT_OK) return st;
+        }
         NativeArgs as = a;  // shadow rays of survivors add to their state in the next queue
         as.ps.L = sv.st[c ^ 1].L;
         L.tk.shadow<<<L.grid_trace, L.block, 0, s>>>(as);

@@ -51,6 +51,7 @@ struct OrderArgs {
     OrderGrid g;
     uint2 *kr;         // per ray: key, rank within the key
     int *pos;          // per ray: its sorted slot
+    int *src;          // per sorted slot: its ray (nullptr: not wanted)
     float4 *sorted;    // per sorted slot: the ray
     unsigned *counts;  // 2^key_bits
     unsigned *sums;    // chunk totals
@@ -215,6 +216,7 @@ __global__ void __launch_bounds__(kOrderBlock) k_order_scatter(OrderArgs a) {
             a.sorted[2 * pos] = __ldg(a.rays + 2 * i);
             a.sorted[2 * pos + 1] = __ldg(a.rays + 2 * i + 1);
             a.pos[i] = (int)pos;
+            if (a.src) a.src[pos] = (int)i;
         } else {
             a.pos[i] = -1;
             bad = 1;
@@ -299,7 +301,7 @@ size_t reorder_scratch_bytes(int64_t n) { return reorder_state_offset(n) + 256; 
 static std::atomic<int> g_order_sms[64];  // SMs per device (0 = not yet known)
 
 tt_status reorder_rays(const float4 *rays, int64_t n, const int *n_dev, const float lo[3], const float hi[3],
-                       void *scratch, size_t state_at, unsigned *err, cudaStream_t s, OrderOut *out) {
+                       void *scratch, size_t state_at, unsigned *err, cudaStream_t s, OrderOut *out, bool with_src) {
     if (n <= 0 || n >= ((int64_t)1 << 31)) return fail(TT_ERR_INVALID, "ray ordering: n must be in 1..2^31-1");
     if (state_at < reorder_state_offset(n) || (state_at & 255))
         return fail(TT_ERR_INVALID, "ray ordering: scratch too small for this many rays");
@@ -328,6 +330,7 @@ tt_status reorder_rays(const float4 *rays, int64_t n, const int *n_dev, const fl
     a.sorted = reinterpret_cast<float4 *>(p);
     p += al256(32ull * n);
     void *sorted_hits = p;
+    a.src = with_src ? static_cast<int *>(sorted_hits) : nullptr;
     p += al256(24ull * n);
     a.counts = reinterpret_cast<unsigned *>(p);
     p += al256(4ull << kOrderBits);
@@ -346,6 +349,7 @@ tt_status reorder_rays(const float4 *rays, int64_t n, const int *n_dev, const fl
     out->sorted = a.sorted;
     out->sorted_hits = sorted_hits;
     out->state = a.state;
+    out->src = a.src;
     return TT_OK;
 }
 

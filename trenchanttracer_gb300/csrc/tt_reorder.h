@@ -90,6 +90,7 @@ struct OrderOut {
     const float4 *sorted;             // 2 float4 per sorted slot
     void *sorted_hits;                // hit record per sorted slot, written by the trace kernel
     const unsigned long long *state;  // order_built(state): whether pos / sorted were built
+    const int *src;                   // with_src: the ray slot of each sorted slot (in sorted_hits)
 };
 
 // Launches (on stream s) the ordering of n rays (or of min(*n_dev, n) when n_dev is set: a count
@@ -97,9 +98,11 @@ struct OrderOut {
 // reorder_scratch_bytes(n); its 256-byte state block sits at byte state_at, zeroed when the
 // scratch was made and fixed for its life (reorder_state_offset of the size it was made for).
 // Calls on one scratch must be ordered (one stream). Launches only, no allocation, so a call can
-// be captured in a CUDA graph. Device-side errors go to *err as kErrOrder.
+// be captured in a CUDA graph. Device-side errors go to *err as kErrOrder. with_src: the scatter
+// also writes the inverse permutation (out->src, over the sorted_hits region), for a pass that
+// reads the rays in sorted order and their other records by original slot.
 tt_status reorder_rays(const float4 *rays, int64_t n, const int *n_dev, const float lo[3], const float hi[3],
-                       void *scratch, size_t state_at, unsigned *err, cudaStream_t s, OrderOut *out);
+                       void *scratch, size_t state_at, unsigned *err, cudaStream_t s, OrderOut *out, bool with_src = false);
 
 // After the trace kernel wrote hits of hit_bytes (8 or 24) per sorted slot into out.sorted_hits:
 // moves each ray's hit to hits[ray] (launch only; nothing to do when the order was not built).
