@@ -445,12 +445,14 @@ tt_status tt_batch_info(const tt_batch *batch, int64_t *total_paths, int64_t *ac
 tt_status tt_batch_render(tt_batch *batch, void *d_accum, int32_t use_graph, void *stream);
 /* Nodes of the captured graph (0 before the first graph render). */
 tt_status tt_batch_graph_kernels(const tt_batch *batch, int32_t *kernels);
-/* Times the first sample_paths paths of the batch (0: 2^27) under launch shapes in two stages:
- * block x stack_shared at 2^22-path waves, ordered and streamed; then the fastest of those at
- * wave_paths in {2^20, 2^22, 2^24, 2^26}, ordered or not, streamed or not (waves that would hold
- * the whole sample twice over are skipped). Keeps the fastest trial as the renderer's shape and
- * writes up to max_results trials to results (at most 9 + 16). Synchronous; touches no
- * accumulation buffer. */
+/* Times the batch's first paths under launch shapes in two stages: block x stack_shared (9
+ * trials, written first to results) at 2^22-path waves, ordered and streamed, on a quarter of
+ * the sample (at least 2^22 paths); then the fastest block and stack_shared at wave_paths in
+ * {2^20, 2^22, 2^24, 2^26}, ordered or not, streamed or not (waves that would hold the whole
+ * sample twice over are skipped, and a sample that fits one wave is timed in waves only), on
+ * sample_paths paths (0: 2^28; at most the batch). Keeps the fastest stage-2 trial as the
+ * renderer's shape and writes up to max_results trials to results (at most 9 + 16).
+ * Synchronous; touches no accumulation buffer. */
 tt_status tt_batch_autotune(tt_batch *batch, int64_t sample_paths, void *stream, tt_launch_shape *results,
                             int32_t max_results, int32_t *n_results);
 tt_status tt_batch_free(tt_batch *batch);

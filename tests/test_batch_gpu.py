@@ -161,6 +161,9 @@ def test_ray_counters_and_autotune(showcase):
     assert s_seq["extension_rays"] >= s_seq["paths"] and s_seq["shadow_rays"] > 0
     assert len(trials) >= 11 and all(t[5] > 0 for t in trials)
     assert {t[3] for t in trials} == {0, 1}
-    best = min(trials, key=lambda t: t[5])
+    stage1, stage2 = trials[:9], trials[9:]  # block x stack first, then waves / ordering / streaming
+    assert {(t[0], t[1]) for t in stage1} == {(b, s) for b in (64, 128, 256) for s in (0, 8, 16)}
+    assert {(t[0], t[1]) for t in stage2} == {min(stage1, key=lambda t: t[5])[:2]}
+    best = min(stage2, key=lambda t: t[5])
     assert showcase.launch == best[:5]
     assert np.array_equal(got.view(np.uint32), seq.view(np.uint32))

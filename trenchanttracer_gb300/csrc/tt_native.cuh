@@ -317,6 +317,7 @@ __device__ __forceinline__ void analytic_hit(const NativeArgs &a, unsigned mask,
 // Kernels of one traversal launch shape (threads per block, shared-memory stack entries).
 struct TraceKernels {
     void (*extend)(NativeArgs, int);
+    void (*extend_prefix)(NativeArgs, int);  // for queues ordered only up to *order.n_sorted
     void (*shadow)(NativeArgs);
 };
 // Moves the hits of an ordered extension queue back to their queue slots (nothing when the

@@ -13,7 +13,9 @@ namespace tt {
 
 using namespace pt;
 
-template <int kBlock, int kSh>
+// kPrefix: the ordering covers only the queue's first *n_sorted slots (a streamed render's
+// survivors); the rest is traced in place. Without it an ordered queue is ordered whole.
+template <int kBlock, int kSh, bool kPrefix>
 __global__ void __launch_bounds__(kBlock) k_extend(NativeArgs a, int cur) {
     __shared__ int sh_stack[(kSh > 0 ? kSh : 1) * kBlock];
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -28,7 +30,7 @@ __global__ void __launch_bounds__(kBlock) k_extend(NativeArgs a, int cur) {
     uint32_t err = 0;
     // an ordered queue prefix: rays and hits by ordered slot, moved back by k_order_gather_hits
     const bool ordered = a.order.sorted && order_built(a.order.state);
-    const int n_sorted = ordered ? *a.order.n_sorted : 0;
+    const int n_sorted = ordered ? (kPrefix ? *a.order.n_sorted : n) : 0;
     for (;;) {
         int base = 0;
         if (lane == 0) base = atomicAdd(a.ps.counts + 3, 32);
@@ -37,7 +39,7 @@ __global__ void __launch_bounds__(kBlock) k_extend(NativeArgs a, int cur) {
         const int q = base + lane;
         const unsigned mask = __ballot_sync(0xffffffffu, q < n);
         if (q < n) {
-            const bool srt = q < n_sorted;
+            const bool srt = kPrefix ? q < n_sorted : ordered;
             const float4 *rays = srt ? a.order.sorted : a.ps.ray[cur];
             const float4 r0 = rays[2 * q], r1 = rays[2 * q + 1];
             const TraceResult tr = traverse_on<true>(stack, a.bvh, r0, r1, err);
@@ -128,7 +130,8 @@ __global__ void __launch_bounds__(256) k_order_gather_hits(NativeArgs a, int cur
 template <int kBlock, int kSh>
 static TraceKernels kernels_of() {
     TraceKernels k;
-    k.extend = k_extend<kBlock, kSh>;
+    k.extend = k_extend<kBlock, kSh, false>;
+    k.extend_prefix = k_extend<kBlock, kSh, true>;
     k.shadow = k_shadow<kBlock, kSh>;
     return k;
 }
@@ -139,7 +142,7 @@ static TraceKernels kernels_of_block(int sh) {
         case 0: return kernels_of<kBlock, 0>();
         case 8: return kernels_of<kBlock, 8>();
         case 16: return kernels_of<kBlock, 16>();
-        default: return TraceKernels{nullptr, nullptr};
+        default: return TraceKernels{nullptr, nullptr, nullptr};
     }
 }
 
@@ -148,7 +151,7 @@ TraceKernels trace_kernels(int block, int stack_shared) {
         case 64: return kernels_of_block<64>(stack_shared);
         case 128: return kernels_of_block<128>(stack_shared);
         case 256: return kernels_of_block<256>(stack_shared);
-        default: return TraceKernels{nullptr, nullptr};
+        default: return TraceKernels{nullptr, nullptr, nullptr};
     }
 }
 

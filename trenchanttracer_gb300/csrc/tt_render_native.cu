@@ -630,7 +630,8 @@ __device__ __forceinline__ void shade_queue(const NativeArgs &a, int cur) {
     const int stride = gridDim.x * blockDim.x;
     const int rounds = (n + stride - 1) / stride;
     const bool use_env = a.env.w > 0;
-    const PathState S = kStream ? a.stream.st[cur] : wave_state(a.ps);
+// the state field f this queue reads (kept as kernel-parameter reads, not copied to registers)
+#define TT_ST(f) (kStream ? (cur ? a.stream.st[1].f : a.stream.st[0].f) : a.ps.f)
     for (int round = 0, q = blockIdx.x * blockDim.x + threadIdx.x; round < rounds; round++, q += stride) {
         const bool live = q < n;
         bool alive = false;
@@ -638,23 +639,24 @@ __device__ __forceinline__ void shade_queue(const NativeArgs &a, int cur) {
         int i = 0;         // state slot
         long long pg = 0;  // kStream: the path's index
         V3 sh_o, sh_d, sh_val, next_o, next_d;
-        V3 beta, L;
-        Rng g;
-        int depth = 0, flags_next = 0;
+        // kStream: what a survivor carries to its slot of the next queue
+        V3 out_beta, out_L;
+        uint64_t out_rng = 0, out_inc = 0;
+        int out_depth = 0, flags_next = 0;
         float pdf_next = 0.0f;
         if (live) {
             i = kStream ? q : a.ps.queue[cur][q];
-            if (kStream) pg = S.g[i];
-            g.state = S.rng[i];
-            g.inc = S.rng_inc[i];
+            if (kStream) pg = (cur ? a.stream.st[1].g : a.stream.st[0].g)[i];
+            Rng g;
+            g.state = TT_ST(rng)[i];
+            g.inc = TT_ST(rng_inc)[i];
             const float4 r0 = a.ps.ray[cur][2 * q], r1 = a.ps.ray[cur][2 * q + 1];
             const V3 o(r0.x, r0.y, r0.z), d(r0.w, r1.x, r1.y);
-            beta = ld3(S.beta + 3ll * i);
-            L = ld3(S.L + 3ll * i);
+            V3 beta = ld3(TT_ST(beta) + 3ll * i), L = ld3(TT_ST(L) + 3ll * i);
             const int prim = a.ps.hit_prim[q];
-            int flags = S.flags[i];
-            const float last_pdf = S.last_pdf[i];
-            depth = S.depth[i];
+            int flags = TT_ST(flags)[i];
+            const float last_pdf = TT_ST(last_pdf)[i];
+            int depth = TT_ST(depth)[i];
             if (prim == -1) {
                 if (use_env) {
                     const int texel = env_texel(a.env, d);
@@ -738,20 +740,27 @@ __device__ __forceinline__ void shade_queue(const NativeArgs &a, int cur) {
                         const V3 off = dot(bs.wi, nl) >= 0.0f ? nl : V3(-nl.x, -nl.y, -nl.z);
                         next_o = madd(off, eps, p);
                         next_d = bs.wi;
-                        pdf_next = bs.pdf;
-                        flags_next = (flags & kFlagsKept) | ((bs.specular || !nee) ? kFlagSpecular : 0);
-                        if (!kStream) {
-                            st3(S.beta + 3ll * i, beta);
-                            S.last_pdf[i] = pdf_next;
-                            S.flags[i] = flags_next;
-                            S.depth[i] = depth;
+                        if (kStream) {
+                            pdf_next = bs.pdf;
+                            flags_next = (flags & kFlagsKept) | ((bs.specular || !nee) ? kFlagSpecular : 0);
+                        } else {
+                            st3(TT_ST(beta) + 3ll * i, beta);
+                            TT_ST(last_pdf)[i] = bs.pdf;
+                            TT_ST(flags)[i] = (flags & kFlagsKept) | ((bs.specular || !nee) ? kFlagSpecular : 0);
+                            TT_ST(depth)[i] = depth;
                         }
                     }
                 }
             }
-            if (!kStream) {
-                st3(S.L + 3ll * i, L);
-                S.rng[i] = g.state;
+            if (kStream) {
+                out_beta = beta;
+                out_L = L;
+                out_rng = g.state;
+                out_inc = g.inc;
+                out_depth = depth;
+            } else {
+                st3(TT_ST(L) + 3ll * i, L);
+                TT_ST(rng)[i] = g.state;
             }
         }
         const int slot = warp_append(a.ps.counts + (cur ^ 1), alive);
@@ -759,21 +768,21 @@ __device__ __forceinline__ void shade_queue(const NativeArgs &a, int cur) {
             if (!kStream) a.ps.queue[cur ^ 1][slot] = i;
             put_ray(a.ps.ray[cur ^ 1], slot, next_o, next_d);
             if (kStream) {
-                const PathState &N = a.stream.st[cur ^ 1];
-                st3(N.beta + 3ll * slot, beta);
-                st3(N.L + 3ll * slot, L);
-                N.rng[slot] = g.state;
-                N.rng_inc[slot] = g.inc;
+                const PathState &N = cur ? a.stream.st[0] : a.stream.st[1];
+                st3(N.beta + 3ll * slot, out_beta);
+                st3(N.L + 3ll * slot, out_L);
+                N.rng[slot] = out_rng;
+                N.rng_inc[slot] = out_inc;
                 N.last_pdf[slot] = pdf_next;
                 N.flags[slot] = flags_next;
-                N.depth[slot] = depth;
+                N.depth[slot] = out_depth;
                 N.g[slot] = pg;
             }
         }
         long long ring_e = 0;
         if (kStream && live && !alive) {
             ring_e = pg % a.stream.ring_n;
-            st3(a.stream.ring + 3 * ring_e, L);
+            st3(a.stream.ring + 3 * ring_e, out_L);
         }
         const int sslot = warp_append(a.ps.counts + 2, shadow);
         if (shadow) {
@@ -792,6 +801,7 @@ __device__ __forceinline__ void shade_queue(const NativeArgs &a, int cur) {
             if ((threadIdx.x & 31) == 0 && m != ~0ull) atomicMin(&a.stream.plan->min_alive, m);
         }
     }
+#undef TT_ST
 }
 
 __global__ void __launch_bounds__(kShadeBlockMax) k_shade(NativeArgs a, int cur) { shade_queue<false>(a, cur); }
@@ -1481,7 +1491,7 @@ static tt_status issue_stream(NativeArgs a, long long total, const Launch &L, co
             a.order.hit_v = h + 2 * pool;
             a.order.hit_prim = reinterpret_cast<int *>(h + 3 * pool);
         }
-        L.tk.extend<<<L.grid_trace, L.block, 0, s>>>(a, c);
+        (L.order ? L.tk.extend_prefix : L.tk.extend)<<<L.grid_trace, L.block, 0, s>>>(a, c);
         if (L.order) k_order_gather_hits<<<L.grid_gather, 256, 0, s>>>(a, c);
         k_shade_stream<<<L.grid_shade, L.block, 0, s>>>(a, c);
         if (L.order && has_shadows(a)) {
@@ -1800,10 +1810,11 @@ tt_status tt_batch_autotune(tt_batch *b, int64_t sample_paths, void *stream, tt_
     if (!b) return fail(TT_ERR_INVALID, "null batch");
     tt_renderer *r = b->r;
     cudaStream_t s = (cudaStream_t)stream;
-    const long long sample = std::min<long long>(b->total_paths, sample_paths > 0 ? sample_paths : (1ll << 27));
-    // a wave's last bounces trace few rays at the latency of the longest ones, so larger waves
-    // (or a streamed pool) pay that tail less often; the sample has to span more than one of the
-    // largest waves to show it
+    // stage 2 times `sample` paths, stage 1 a quarter of them (at least 2^22): a wave's last bounces
+    // trace few rays at the latency of the longest ones, so larger waves (or a streamed pool) pay
+    // that tail less often, and the sample has to span several of the largest waves to show it
+    const long long sample = std::min<long long>(b->total_paths, sample_paths > 0 ? sample_paths : (1ll << 28));
+    const long long sample1 = std::min<long long>(sample, std::max<long long>(sample / 4, 1ll << 22));
     static const int kWaves[] = {1 << 20, 1 << 22, 1 << 24, 1 << 26};
     PathSoA ps;
     const int order_was = r->launch_order;
@@ -1819,17 +1830,17 @@ tt_status tt_batch_autotune(tt_batch *b, int64_t sample_paths, void *stream, tt_
     float best = 3.4e38f;
     tt_launch_shape best_shape{r->launch_block, r->launch_stack, r->launch_wave, r->launch_order, r->launch_stream, 0.0f};
     int count = 0;
-    // times the sample under one shape (buffers allocated before the timed region)
-    auto trial = [&](int block, int sh, int wave, int order, int strm) -> tt_status {
+    // times n paths under one shape (buffers allocated before the timed region)
+    auto trial = [&](long long n, int block, int sh, int wave, int order, int strm) -> tt_status {
         Launch L;
         tt_status t = resolve_launch(r, block, sh, wave, order, strm, L);
-        if (t == TT_OK && streamed(sample, L, b->p.max_depth, nullptr)) {
+        if (t == TT_OK && streamed(n, L, b->p.max_depth, nullptr)) {
             StreamView sv;
             t = ensure_stream(r, ps, wave, stream_ring_entries(wave, b->p.max_depth), sv);
         }
-        if (t == TT_OK) t = issue(a, std::min<long long>(sample, 1 << 16), L, plan, nullptr, s, r);  // warm-up
+        if (t == TT_OK) t = issue(a, std::min<long long>(n, 1 << 16), L, plan, nullptr, s, r);  // warm-up
         cudaError_t e = cudaEventRecord(e0, s);
-        if (t == TT_OK && e == cudaSuccess) t = issue(a, sample, L, plan, nullptr, s, r);
+        if (t == TT_OK && e == cudaSuccess) t = issue(a, n, L, plan, nullptr, s, r);
         if (e == cudaSuccess) e = cudaEventRecord(e1, s);
         if (e == cudaSuccess) e = cudaEventSynchronize(e1);
         float ms = 0.0f;
@@ -1848,18 +1859,18 @@ tt_status tt_batch_autotune(tt_batch *b, int64_t sample_paths, void *stream, tt_
     // stage 1: threads per block x shared stack entries, at 2^22-path waves, ordered and streamed
     for (int bi = 0; bi < kNumBlockShapes && st == TT_OK; bi++)
         for (int si = 0; si < kNumStackShapes && st == TT_OK; si++)
-            st = trial(kBlockShapes[bi], kStackShapes[si], kWaves[1], 1, 1);
+            st = trial(sample1, kBlockShapes[bi], kStackShapes[si], kWaves[1], 1, 1);
     // stage 2: the fastest of those at every wave size, ordered or not, streamed or in waves (a
-    // sample that fits one wave is the same either way)
+    // sample that fits one wave is the same either way); the renderer keeps the fastest of these
     const int bb = best_shape.block, bs = best_shape.stack_shared;
+    best = 3.4e38f;
     for (int wave : kWaves)
         for (int order = 0; order < 2; order++)
             for (int strm = 0; strm < 2; strm++) {
                 if (st != TT_OK) break;
                 if (wave > kWaves[0] && wave / 2 >= sample) continue;  // the same as a smaller wave
                 if (strm && sample <= wave) continue;
-                if (wave == kWaves[1] && order == 1 && strm == 1) continue;  // timed in stage 1
-                st = trial(bb, bs, wave, order, strm);
+                st = trial(sample, bb, bs, wave, order, strm);
             }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
