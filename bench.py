@@ -664,11 +664,15 @@ def run_batch(args) -> None:
     dev = torch.device("cuda", 0)
     sc, mesh, _ = render_scene("terrain", 64, 64)
     r = Renderer(DeviceBVH(BVHCompact.build(sc, 1e-5, 1, 8)), sc)
-    views = scenes.orbit_views(64)
+    views = scenes.orbit_views(64)[:args.views]
     P = dict(max_depth=8, rr_depth=4)
     b = Batch(r, views, render_params(**P))
     t0 = time.perf_counter()
-    trials = b.autotune()
+    if args.launch:
+        r.set_launch(*[int(x) for x in args.launch.split(",")])
+        trials = []
+    else:
+        trials = b.autotune()
     tune_s = time.perf_counter() - t0
     acc = torch.zeros(b.accum_elems, dtype=torch.float32, device=dev)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=dev)
@@ -714,17 +718,17 @@ def run_batch(args) -> None:
     mean_ms = float(np.mean(ms))
     rays = (st["extension_rays"] + st["shadow_rays"]) / args.steps
     line = {
-        "metric": "Msamples/s batched uneven renders (64 views, one graph launch)",
+        "metric": f"Msamples/s batched uneven renders ({len(views)} views, one graph launch)",
         "value": round(b.total_paths / mean_ms / 1e3, 2), "unit": "Msamples/s", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(mean_ms, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded terrain and orbit poses)",
-        "config": {"workload": "64 orbit views of the terrain (2,097,152 tris, sky + sun), sizes from "
+        "config": {"workload": f"{len(views)} orbit views of the terrain (2,097,152 tris, sky + sun), sizes from "
                                "{256,512,768,1024}^2, spp from {4,16,64}, depth 8, RR from 4",
                    "paths_per_step": b.total_paths, "graph_kernels": b.graph_kernels,
                    "launch_shape": list(r.launch), "autotune_s": round(tune_s, 2), "autotune_trials": len(trials),
                    "l2": "L2 flushed (256 MB write) between steps, untimed"},
         "sequential": {"value": round(b.total_paths / float(np.mean(seq)) / 1e3, 2), "unit": "Msamples/s",
-                       "ms_per_step": round(float(np.mean(seq)), 3), "how": "64 tt_render_native calls"},
+                       "ms_per_step": round(float(np.mean(seq)), 3), "how": f"{len(views)} tt_render_native calls"},
         "mrays_per_s": round(rays / mean_ms / 1e3, 1),
         "e2e": {"value": round(b.total_paths / float(np.mean(e2e)) / 1e3, 2), "unit": "Msamples/s",
                 "h2d_bytes_per_step": 0, "d2h_bytes_per_step": int(b.accum_elems * 4)},
@@ -991,6 +995,9 @@ def main() -> None:
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=["terrain", "cornell", "multimaterial", "batch", "cache", "mlp"], default="terrain")
     ap.add_argument("--cache-scene", choices=["multimaterial", "terrain"], default="multimaterial")
+    ap.add_argument("--views", type=int, default=64, help="batch: the first N of the 64 orbit views (profiling)")
+    ap.add_argument("--launch", default="",
+                    help="batch: block,stack_shared,wave_paths,ordered,streamed instead of autotuning (profiling)")
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--ordered", type=int, choices=[-1, 0, 1], default=-1,
                     help="cornell / multimaterial: order each extension queue before tracing it "
