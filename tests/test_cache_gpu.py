@@ -130,6 +130,33 @@ def test_gradient_matches_oracle():
     assert not g[off[5] + 3 * 64:].any()  # padding rows of the output layer get no gradient
 
 
+@pytest.mark.parametrize("n", [1, 129, 1000, 2500, 4096])
+def test_tcgen05_training_matches_mma_sync_and_oracle(n):
+    """The training pass on tcgen05 + TMEM (forward storing each layer's input, backward with the
+    transposed weights, weight gradients with K = the batch's rows; mma_kind 0) against the
+    mma.sync kernels (mma_kind 1) and the FP64 oracle, including partial 128-row tiles and
+    1024-row gradient chunks; no wait runs out."""
+    w = nrc.init_weights(31)
+    tc = Cache(LO, HI, batch=4096, mma_kind=0)
+    ms = Cache(LO, HI, batch=4096, mma_kind=1)
+    tc.set_weights(w)
+    ms.set_weights(w)
+    rec = _records(n, 8)
+    tgt = _target(rec)
+    rec_t, tgt_t = torch.from_numpy(rec).cuda(), torch.from_numpy(tgt).cuda()
+    g_tc, loss_tc = tc.gradient(rec_t, tgt_t)
+    g_ms, loss_ms = ms.gradient(rec_t, tgt_t)
+    tc.check()
+    lref, gref = nrc.loss_and_gradient(_enc_np(ms, rec_t), w, tgt)
+    assert abs(loss_tc - lref) <= 1e-3 * lref and abs(loss_tc - loss_ms) <= 1e-3 * loss_ms
+    off = nrc.offsets()
+    for l in range(nrc.LAYERS):
+        a, b, r = g_tc[off[l]:off[l + 1]], g_ms[off[l]:off[l + 1]], gref[off[l]:off[l + 1]]
+        assert np.linalg.norm(a - r) / np.linalg.norm(r) < 2e-2, (l, "vs oracle")
+        assert np.linalg.norm(a - b) / np.linalg.norm(b) < 2e-2, (l, "vs mma.sync")
+    assert not g_tc[off[5] + 3 * 64:].any()  # padding rows of the output layer get no gradient
+
+
 def test_adam_step_matches_oracle():
     cache = Cache(LO, HI, batch=2048, lr=1e-2, ema=0.5)
     w = nrc.init_weights(13)

@@ -445,6 +445,7 @@ struct AdamArgs {
     float *master, *m, *v, *ema;
     uint16_t *w_train, *w_ema;
     uint16_t *w_tc_train, *w_tc_ema;  // the same in the tcgen05 operand layout
+    uint16_t *w_tcT_train;            // layers 1..5 in the transposed operand layout
     int *step;   // [0] device step counter, advanced by the last block; [1] blocks done
     const int *n_dev;
     long long n_host, off;
@@ -490,6 +491,7 @@ __device__ __forceinline__ void k_adam_body(const AdamArgs &a) {
     const int ti = tc_index(l, local / layer_in(l), local % layer_in(l));
     a.w_tc_train[ti] = *reinterpret_cast<const uint16_t *>(&wb);
     a.w_tc_ema[ti] = *reinterpret_cast<const uint16_t *>(&eb);
+    if (l >= 1) a.w_tcT_train[tcT_index(l, local % layer_in(l), local / layer_in(l))] = *reinterpret_cast<const uint16_t *>(&wb);
 }
 
 __global__ void k_adam(AdamArgs a) { k_adam_body(a); }
@@ -523,7 +525,8 @@ struct tt_cache {
     float *master = nullptr, *m = nullptr, *v = nullptr, *ema = nullptr, *grad = nullptr;
     uint16_t *w_train = nullptr, *w_ema = nullptr;
     uint16_t *w_tc_train = nullptr, *w_tc_ema = nullptr;  // the same in the tcgen05 operand layout
-    unsigned *err = nullptr;                                // error word of the tcgen05 kernel
+    uint16_t *w_tcT_train = nullptr;                        // layers 1..5 transposed (tcgen05 backward)
+    unsigned *err = nullptr;                                // error word of the tcgen05 kernels
     int *step = nullptr;
     float *loss = nullptr;
     // training scratch for `p.batch` rows
@@ -605,6 +608,7 @@ tt_status upload_weights(tt_cache *c, const std::vector<float> &w) {
     TT_CUDA_C(cudaMemset(c->step, 0, sizeof(int)));
     tc_relayout(c->master, c->w_tc_train, nullptr);
     tc_relayout(c->ema, c->w_tc_ema, nullptr);
+    tcT_relayout(c->master, c->w_tcT_train, nullptr);
     TT_CUDA_C(cudaDeviceSynchronize());
     return TT_OK;
 }
@@ -638,25 +642,56 @@ tt_status train_pass(tt_cache *c, const float *rec, const float *target, long lo
     const long long rows = n_dev ? cap : (n_host - off < cap ? n_host - off : cap);
     MlpArgs a = train_args(c, rec, target, n_dev ? 0 : rows, n_dev, off, cap);
     if (!n_dev) a.off = 0, a.rec = rec + off * kRec, a.target = target + off * 3;
-    const int grid = fwd_grid(c, rows);
-    k_mlp_forward<true><<<grid, kThreads, kFwdSmem, s>>>(a);
-    k_mlp_backward<<<grid, kThreads, kWeightBytes, s>>>(a);
-    WgradArgs w;
-    std::memset(&w, 0, sizeof(w));
-    for (int l = 0; l < kLayers; l++) {
-        w.h[l] = c->h[l];
-        w.dz[l] = c->dz[l];
+    int chunks = c->chunks;
+    if (c->p.mma_kind == 0) {  // tcgen05 + TMEM: forward, backward, weight gradients
+        TcTrainArgs t;
+        std::memset(&t, 0, sizeof(t));
+        t.w_tc = c->w_tc_train;
+        t.w_tcT = c->w_tcT_train;
+        t.rec = rec + off * kRec;  // the pass's first row
+        t.target = target + off * 3;
+        t.n_host = a.n_host;
+        t.n_dev = n_dev;
+        t.off = n_dev ? off : 0;  // rows = clamp(*n_dev - off, 0, cap), or n_host
+        t.cap = cap;
+        for (int i = 0; i < 3; i++) {
+            t.lo[i] = a.enc.lo[i];
+            t.inv_ext[i] = a.enc.inv_ext[i];
+        }
+        t.y = c->y;
+        for (int l = 0; l < kLayers; l++) {
+            t.h[l] = c->h[l];
+            t.dz[l] = c->dz[l];
+        }
+        t.loss = c->loss;
+        t.partial = c->partial;
+        t.err = c->err;
+        t.num_sms = c->num_sms;
+        t.wait_cycles = c->p.wait_limit;
+        const tt_status st = tc_train(t, s);
+        if (st != TT_OK) return st;
+        chunks = tc_wgrad_chunks(rows);
+    } else {  // mma.sync
+        const int grid = fwd_grid(c, rows);
+        k_mlp_forward<true><<<grid, kThreads, kFwdSmem, s>>>(a);
+        k_mlp_backward<<<grid, kThreads, kWeightBytes, s>>>(a);
+        WgradArgs w;
+        std::memset(&w, 0, sizeof(w));
+        for (int l = 0; l < kLayers; l++) {
+            w.h[l] = c->h[l];
+            w.dz[l] = c->dz[l];
+        }
+        w.n_dev = n_dev;  // rows = clamp(*n_dev - off, 0, cap), or n_host
+        w.n_host = a.n_host;
+        w.off = n_dev ? off : 0;
+        w.cap = cap;
+        w.partial = c->partial;
+        k_mlp_wgrad<<<dim3(c->chunks, kLayers), kThreads, kWgradSmem, s>>>(w);
     }
-    w.n_dev = n_dev;  // rows = clamp(*n_dev - off, 0, cap), or n_host
-    w.n_host = a.n_host;
-    w.off = n_dev ? off : 0;
-    w.cap = cap;
-    w.partial = c->partial;
-    k_mlp_wgrad<<<dim3(c->chunks, kLayers), kThreads, kWgradSmem, s>>>(w);
     AdamArgs ad;
     std::memset(&ad, 0, sizeof(ad));
     ad.partial = c->partial;
-    ad.chunks = c->chunks;
+    ad.chunks = chunks;
     ad.grad = c->grad;
     ad.master = c->master;
     ad.m = c->m;
@@ -666,6 +701,7 @@ tt_status train_pass(tt_cache *c, const float *rec, const float *target, long lo
     ad.w_ema = c->w_ema;
     ad.w_tc_train = c->w_tc_train;
     ad.w_tc_ema = c->w_tc_ema;
+    ad.w_tcT_train = c->w_tcT_train;
     ad.step = c->step;
     ad.n_dev = n_dev;
     ad.n_host = a.n_host;
@@ -788,6 +824,7 @@ tt_status tt_cache_create(const tt_cache_params *p, tt_cache **out) {
     sizes.push_back(2 * tc_weight_elems());                                 // operand-layout weights
     sizes.push_back(2 * tc_weight_elems());
     sizes.push_back(256);                                                   // error word
+    sizes.push_back(2 * tcT_weight_elems());                                // transposed operand layout
     size_t total = 0;
     for (size_t s : sizes) total += al(s);
     e = cudaMalloc(&c->block, total);
@@ -819,6 +856,7 @@ tt_status tt_cache_create(const tt_cache_params *p, tt_cache **out) {
     c->w_tc_train = (uint16_t *)take();
     c->w_tc_ema = (uint16_t *)take();
     c->err = (unsigned *)take();
+    c->w_tcT_train = (uint16_t *)take();
     std::vector<float> w;
     init_weights(p->seed, w);
     const tt_status st = upload_weights(c, w);

@@ -3,8 +3,8 @@
 //
 // Network: encoded input (160) -> 64 -> 64 -> 64 -> 64 -> 64 -> 3, ReLU on the hidden layers, no
 // biases (the encoding carries a constant-1 feature), RGB radiance = exp(output). BF16 weights and
-// activations, FP32 accumulation (mma.sync m16n8k16 bf16 tensor-core instructions), FP32 master
-// weights and Adam state.
+// activations, FP32 accumulation on the tensor cores (tcgen05 with TMEM accumulators by default,
+// mma.sync m16n8k16 as the alternative kind), FP32 master weights and Adam state.
 //
 // Layers l = 0..5: Z_l = W_l H_l, H_{l+1} = relu(Z_l) for l < 5, Y = W_5 H_5. W_l is stored
 // [out][in]; the output layer is padded from 3 to 8 rows that stay zero.
@@ -59,6 +59,16 @@ constexpr int kTcWeights = tc_offset(kLayers);  // 27648 bf16
 __host__ __device__ inline int tc_index(int l, int n, int k) {
     const int ng = tc_out(l) / 8;
     return tc_offset(l) + ((k / 8) * ng + n / 8) * 64 + (n % 8) * 8 + (k % 8);
+}
+// The transposed operand layout the backward pass multiplies by: layer l >= 1 as N = layer_in(l)
+// rows of K = tc_out(l) values, element (n, k) = W_l[k][n] (k beyond the layer's outputs: 0), in 8 x
+// 8 core matrices, K-major.
+__host__ __device__ constexpr int tcT_offset(int l) { return l <= 1 ? 0 : tcT_offset(l - 1) + layer_in(l - 1) * tc_out(l - 1); }
+constexpr int kTcTWeights = tcT_offset(kLayers);  // 17408 bf16
+static_assert(kTcTWeights == 4 * 64 * 64 + 64 * 16, "transposed weights of layers 1..5");
+__host__ __device__ inline int tcT_index(int l, int n, int k) {
+    const int ng = layer_in(l) / 8;
+    return tcT_offset(l) + ((k / 8) * ng + n / 8) * 64 + (n % 8) * 8 + (k % 8);
 }
 
 

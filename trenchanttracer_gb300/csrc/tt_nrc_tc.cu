@@ -36,6 +36,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstring>
 
 #include "tt_nrc.cuh"
 #include "tt_nrc_tc.h"
@@ -158,14 +159,20 @@ struct TcEncoding {
 // Encoding values [32 f, 32 f + 32) of one row (tt_nrc.cuh) into ring slot S: four chunks of 8
 // BF16 values, each one 16-byte store (the 32 rows of a warp write 512 contiguous bytes per
 // chunk). f must be a compile-time constant after unrolling.
-__device__ __forceinline__ void encode_fill(const EncInputs &in, const float *rec, __nv_bfloat16 *S, int r, int f) {
+// gout (training): the row of H_0 in global memory, which gets the same values.
+__device__ __forceinline__ void encode_fill(const EncInputs &in, const float *rec, __nv_bfloat16 *S, int r, int f,
+                                            uint4 *gout) {
 #pragma unroll
-    for (int j = 0; j < kFillCols / 8; j++)
-        *reinterpret_cast<uint4 *>(S + a_offset(r, 8 * j)) = enc_chunk(in, rec, f * (kFillCols / 8) + j);
+    for (int j = 0; j < kFillCols / 8; j++) {
+        const uint4 v = enc_chunk(in, rec, f * (kFillCols / 8) + j);
+        *reinterpret_cast<uint4 *>(S + a_offset(r, 8 * j)) = v;
+        if (gout) gout[f * (kFillCols / 8) + j] = v;
+    }
 }
 
-// ReLU of this thread's 64 accumulator columns, rounded to BF16, into its row of the next A.
-__device__ __forceinline__ void relu_to_operand(uint32_t lane_addr, __nv_bfloat16 *A, int r) {
+// ReLU of this thread's 64 accumulator columns, rounded to BF16, into its row of the next A (and,
+// training, into the row of that layer's input H in global memory, gout).
+__device__ __forceinline__ void relu_to_operand(uint32_t lane_addr, __nv_bfloat16 *A, int r, uint4 *gout = nullptr) {
 #pragma unroll
     for (int c = 0; c < kHidden; c += 16) {
         float v[16];
@@ -179,25 +186,39 @@ __device__ __forceinline__ void relu_to_operand(uint32_t lane_addr, __nv_bfloat1
         }
         *reinterpret_cast<uint4 *>(A + a_offset(r, c)) = make_uint4(w[0], w[1], w[2], w[3]);
         *reinterpret_cast<uint4 *>(A + a_offset(r, c + 8)) = make_uint4(w[4], w[5], w[6], w[7]);
+        if (gout) {
+            gout[c / 8] = make_uint4(w[0], w[1], w[2], w[3]);
+            gout[c / 8 + 1] = make_uint4(w[4], w[5], w[6], w[7]);
+        }
     }
 }
 
 struct TcArgs {
     const uint16_t *w;  // weights in the operand layout (kTcWeights bf16)
-    const float *rec;
+    const float *rec;   // the call's first record
     long long n_host;
-    const int *n_dev;   // rows = min(*n_dev, cap) when set
-    long long cap;
+    const int *n_dev;   // rows = clamp(*n_dev - off, 0, cap) when set
+    long long off, cap;
     TcEncoding enc;
-    float *rgb;
+    float *rgb;         // inference: radiance, 3 per row
+    float *y;           // training: the raw outputs, 3 per row
+    uint16_t *h[kLayers];  // training: each layer's input H_l (BF16 rows of 160 or 64)
     unsigned *err;
     long long wait_cycles;  // budget of the waits in the main path (the drain at exit keeps ~1 s)
 };
+
+__device__ __forceinline__ long long tc_rows(long long n_host, const int *n_dev, long long off, long long cap) {
+    if (!n_dev) return n_host;
+    const long long n = (long long)*n_dev - off;
+    return n < 0 ? 0 : (n > cap ? cap : n);
+}
 
 __device__ __forceinline__ void group_sync(int group) {  // the 128 threads of one warpgroup
     asm volatile("bar.sync %0, 128;" ::"r"(1 + group) : "memory");
 }
 
+// kTrain: also writes every layer's input H_l and the raw outputs, for the backward pass.
+template <bool kTrain>
 __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(TcArgs a) {
     extern __shared__ __align__(128) uint8_t smem[];
     const int tid = threadIdx.x, group = tid >> 7, gt = tid & 127, warp_in_group = gt >> 5;
@@ -215,11 +236,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(TcArgs a) {
     int *ok = ok_w + 1 + group;                          // this group's waits all ended
     static_assert(8 * (1 + 5 * kTcGroups) + 4 + 4 * (1 + kTcGroups) <= kTcBarBytes, "barrier block");
 
-    long long n = a.n_host;
-    if (a.n_dev) {
-        n = *a.n_dev;
-        n = n < 0 ? 0 : (n > a.cap ? a.cap : n);
-    }
+    const long long n = tc_rows(a.n_host, a.n_dev, a.off, a.cap);
     const long long ntiles = (n + kTcRows - 1) / kTcRows;
     if ((long long)blockIdx.x * kTcGroups >= ntiles) return;  // uniform per block: nothing allocated yet
 
@@ -298,7 +315,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(TcArgs a) {
                 }
             }
             if (gt < rows) {
-                encode_fill(in, rec, S, gt, f);
+                encode_fill(in, rec, S, gt, f, kTrain ? reinterpret_cast<uint4 *>(a.h[0] + (r0 + gt) * kIn) : nullptr);
             } else {
                 for (int k = 0; k < kFillCols; k += 8)
                     *reinterpret_cast<uint4 *>(S + a_offset(gt, k)) = make_uint4(0u, 0u, 0u, 0u);
@@ -340,7 +357,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(TcArgs a) {
         group_sync(group);
         tc_fence_after();
         if (!*ok) break;
-        relu_to_operand(lane_addr, A, gt);  // the whole buffer: the ring is no longer read
+        // the whole buffer: the ring is no longer read
+        relu_to_operand(lane_addr, A, gt,
+                        kTrain && gt < rows ? reinterpret_cast<uint4 *>(a.h[1] + (r0 + gt) * kHidden) : nullptr);
         fence_async_smem();
         tc_fence_before();
         group_sync(group);
@@ -362,17 +381,25 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(TcArgs a) {
             tc_fence_after();
             if (!*ok) break;
             if (l < kLayers - 1) {
-                relu_to_operand(lane_addr, A, gt);
+                relu_to_operand(lane_addr, A, gt,
+                                kTrain && gt < rows ? reinterpret_cast<uint4 *>(a.h[l + 1] + (r0 + gt) * kHidden) : nullptr);
                 fence_async_smem();
             } else {
                 float v[16];
                 tmem_ld16(lane_addr, v);
                 tmem_wait_ld();
                 if (gt < rows) {
-                    float *o = a.rgb + (r0 + gt) * 3;
-                    o[0] = expf(fminf(v[0], 20.0f));
-                    o[1] = expf(fminf(v[1], 20.0f));
-                    o[2] = expf(fminf(v[2], 20.0f));
+                    if (kTrain) {
+                        float *o = a.y + (r0 + gt) * 3;
+                        o[0] = v[0];
+                        o[1] = v[1];
+                        o[2] = v[2];
+                    } else {
+                        float *o = a.rgb + (r0 + gt) * 3;
+                        o[0] = expf(fminf(v[0], 20.0f));
+                        o[1] = expf(fminf(v[1], 20.0f));
+                        o[2] = expf(fminf(v[2], 20.0f));
+                    }
                 }
             }
             tc_fence_before();
@@ -414,23 +441,421 @@ __global__ void k_tc_layout(const float *w, uint16_t *out) {
     out[i] = *reinterpret_cast<const uint16_t *>(&b);
 }
 
+__global__ void k_tcT_layout(const float *w, uint16_t *out) {
+    // compact [out][in] FP32 weights of layers 1..5 -> the transposed operand layout BF16
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kTcTWeights) return;
+    int l = 1;
+    while (l + 1 < kLayers && i >= tcT_offset(l + 1)) l++;
+    const int local = i - tcT_offset(l);
+    const int ng = layer_in(l) / 8;
+    const int core = local / 64, within = local % 64;
+    const int k8 = core / ng, n8 = core % ng;
+    const int n = n8 * 8 + within / 8, k = k8 * 8 + within % 8;  // n: input, k: output
+    const float v = k < layer_out(l) ? w[w_offset(l) + k * layer_in(l) + n] : 0.0f;
+    const __nv_bfloat16 b = __float2bfloat16_rn(v);
+    out[i] = *reinterpret_cast<const uint16_t *>(&b);
+}
+
+// ---- training: backward pass ---------------------------------------------------------------------
+// One warpgroup per tile of 128 rows (six per CTA, as in the forward kernel). Row r of the tile is
+// thread r and TMEM lane r. The loss gradient of the row's three outputs (relative L2 loss
+// sum_c (p - t)^2 / (p^2 + 0.01), p = exp(y), the denominator not differentiated, scaled by
+// 1 / rows) is the K = 16 operand dZ_5 (columns 3..15 zero). Then for l = 5 .. 1 one product
+// dH_l = dZ_l W_l (M = 128, N = 64, K = 16 or 64, B = the transposed weights), and the epilogue
+// reads the row's 64 columns, keeps those where H_l > 0 (the forward pass's stored BF16 input of
+// layer l, i.e. relu(Z_{l-1})), rounds to BF16 and writes dZ_{l-1} to global memory and, but for
+// l = 1, into the operand buffer for the next product. Every dZ row is stored as the weight
+// gradient needs it.
+struct TcBackArgs {
+    const uint16_t *wT;  // transposed operand-layout weights of layers 1..5 (kTcTWeights bf16)
+    const float *y, *target;
+    const uint16_t *h[kLayers];
+    uint16_t *dz[kLayers];
+    float *loss;  // loss sum over the rows / rows (atomic), or nullptr
+    long long n_host;
+    const int *n_dev;
+    long long off, cap;
+    unsigned *err;
+    long long wait_cycles;
+};
+constexpr int kTcTWeightBytes = kTcTWeights * 2;  // 34816
+constexpr int kTcBackSmem = kTcGroups * kABytes + kTcTWeightBytes + kTcBarBytes;
+static_assert(kTcBackSmem <= 232448 && kTcTWeightBytes % 16 == 0, "backward shared memory");
+
+__device__ __forceinline__ bool bf16_pos(uint32_t bits16) { return bits16 != 0u && !(bits16 & 0x8000u); }
+
+// dZ = dH * [H > 0] for this thread's 64 accumulator columns; H: the row's 64 BF16 values in
+// global memory (nullptr: a row past the end, all zero). Into the operand buffer (A != nullptr)
+// and to gout (!= nullptr).
+__device__ __forceinline__ void mask_to_operand(uint32_t lane_addr, const uint16_t *H, __nv_bfloat16 *A, int r,
+                                                uint4 *gout) {
+#pragma unroll
+    for (int c = 0; c < kHidden; c += 16) {
+        float v[16];
+        tmem_ld16(lane_addr + c, v);
+        tmem_wait_ld();
+        uint4 hv[2] = {make_uint4(0u, 0u, 0u, 0u), make_uint4(0u, 0u, 0u, 0u)};
+        if (H) {
+            hv[0] = *reinterpret_cast<const uint4 *>(H + c);
+            hv[1] = *reinterpret_cast<const uint4 *>(H + c + 8);
+        }
+        const uint32_t hw[8] = {hv[0].x, hv[0].y, hv[0].z, hv[0].w, hv[1].x, hv[1].y, hv[1].z, hv[1].w};
+        uint32_t w[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const float lo = bf16_pos(hw[j] & 0xffffu) ? v[2 * j] : 0.0f;
+            const float hi = bf16_pos(hw[j] >> 16) ? v[2 * j + 1] : 0.0f;
+            const __nv_bfloat162 b = __floats2bfloat162_rn(lo, hi);
+            w[j] = *reinterpret_cast<const uint32_t *>(&b);
+        }
+        if (A) {
+            *reinterpret_cast<uint4 *>(A + a_offset(r, c)) = make_uint4(w[0], w[1], w[2], w[3]);
+            *reinterpret_cast<uint4 *>(A + a_offset(r, c + 8)) = make_uint4(w[4], w[5], w[6], w[7]);
+        }
+        if (gout) {
+            gout[c / 8] = make_uint4(w[0], w[1], w[2], w[3]);
+            gout[c / 8 + 1] = make_uint4(w[4], w[5], w[6], w[7]);
+        }
+    }
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+    const __nv_bfloat162 b = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<const uint32_t *>(&b);
+}
+
+__global__ void __launch_bounds__(kTcThreads, 1) k_mlp_backward_tc(TcBackArgs a) {
+    extern __shared__ __align__(128) uint8_t smem[];
+    const int tid = threadIdx.x, group = tid >> 7, gt = tid & 127, warp_in_group = gt >> 5;
+    __nv_bfloat16 *A = reinterpret_cast<__nv_bfloat16 *>(smem + group * kABytes);
+    uint16_t *W = reinterpret_cast<uint16_t *>(smem + kTcGroups * kABytes);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kTcGroups * kABytes + kTcTWeightBytes);
+    uint64_t *bar_w = bars;                  // weights
+    uint64_t *bar_mma = bars + 1 + group;    // the group's products
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 1 + kTcGroups);
+    int *ok_w = reinterpret_cast<int *>(tmem_slot + 1);
+    int *ok = ok_w + 1 + group;
+    static_assert(8 * (1 + kTcGroups) + 4 + 4 * (1 + kTcGroups) <= kTcBarBytes, "barrier block");
+
+    const long long n = tc_rows(a.n_host, a.n_dev, a.off, a.cap);
+    const long long ntiles = (n + kTcRows - 1) / kTcRows;
+    if ((long long)blockIdx.x * kTcGroups >= ntiles) return;  // uniform per block: nothing allocated yet
+    if (tid == 0) {
+        mbar_init(bar_w, 1);
+        for (int g = 0; g < kTcGroups; g++) {
+            mbar_init(bars + 1 + g, 1);
+            ok_w[1 + g] = 1;
+        }
+        *ok_w = 1;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (tid < 32) tmem_alloc(tmem_slot, kTmemCols);
+    bool w_pending = false;
+    if (tid == 0) {
+        mbar_expect_tx(bar_w, kTcTWeightBytes);
+        bulk_load(W, a.wT, kTcTWeightBytes, bar_w);
+        if (!mbar_wait(bar_w, 0, a.wait_cycles)) {
+            *ok_w = 0;
+            w_pending = true;
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot + (uint32_t)(group * 64);
+    const uint32_t lane_addr = tmem + ((uint32_t)(warp_in_group * 32) << 16);
+    const bool weights_ok = *ok_w != 0;
+    if (!weights_ok && gt == 0) *ok = 0;
+    group_sync(group);
+    const float inv_n = 1.0f / (float)n;
+    float loss = 0.0f;
+    int mma_issued = 0, mma_done = 0;
+    const long long tstride = (long long)gridDim.x * kTcGroups;
+    for (long long tile = (long long)blockIdx.x * kTcGroups + group; weights_ok && tile < ntiles; tile += tstride) {
+        const long long r0 = tile * kTcRows, row = r0 + gt;
+        const bool own = row < n;
+        float dy[3] = {0.f, 0.f, 0.f};
+        if (own) {
+#pragma unroll
+            for (int c = 0; c < kOut; c++) {
+                const float yv = a.y[row * 3 + c];
+                const float p = expf(fminf(yv, 20.0f));
+                const float diff = p - a.target[row * 3 + c];
+                const float den = p * p + 0.01f;
+                loss += diff * diff / den;
+                dy[c] = yv < 20.0f ? 2.0f * diff / den * p * inv_n : 0.0f;
+            }
+        }
+        const uint4 d5 = make_uint4(pack_bf16(dy[0], dy[1]), pack_bf16(dy[2], 0.0f), 0u, 0u);
+        *reinterpret_cast<uint4 *>(A + a_offset(gt, 0)) = d5;
+        *reinterpret_cast<uint4 *>(A + a_offset(gt, 8)) = make_uint4(0u, 0u, 0u, 0u);
+        if (own) *reinterpret_cast<uint4 *>(a.dz[kLayers - 1] + row * kOutPad) = d5;
+        fence_async_smem();
+        tc_fence_before();
+        group_sync(group);
+        tc_fence_after();
+        bool failed = false;
+        for (int l = kLayers - 1; l >= 1; l--) {
+            const int K = tc_out(l), N = layer_in(l);
+            if (gt == 0) {
+                const uint32_t a0 = saddr(A), b0 = saddr(W + tcT_offset(l));
+                const uint32_t idesc = idesc_bf16(kTcRows, N);
+                for (int s2 = 0; s2 < K / 16; s2++)
+                    umma(tmem, sdesc(a0 + s2 * 2 * 2048, 2048, 128), sdesc(b0 + s2 * 2 * (N / 8) * 128, (N / 8) * 128, 128),
+                         idesc, s2 > 0 ? 1u : 0u);
+                umma_commit(bar_mma);
+                mma_issued++;
+                if (mbar_wait(bar_mma, (uint32_t)(mma_done & 1), a.wait_cycles)) mma_done++;
+                else *ok = 0;
+            }
+            group_sync(group);
+            tc_fence_after();
+            if (!*ok) {
+                failed = true;
+                break;
+            }
+            mask_to_operand(lane_addr, own ? a.h[l] + row * kHidden : nullptr, l > 1 ? A : nullptr, gt,
+                            own ? reinterpret_cast<uint4 *>(a.dz[l - 1] + row * kHidden) : nullptr);
+            fence_async_smem();
+            tc_fence_before();
+            group_sync(group);
+            tc_fence_after();
+        }
+        if (failed) break;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, o);
+    if ((tid & 31) == 0 && a.loss) atomicAdd(a.loss, loss * inv_n);
+    if (gt == 0) {
+        if (!*ok) atomicOr(a.err, kErrMlpWait);
+        while (mma_done < mma_issued && mbar_wait(bar_mma, (uint32_t)(mma_done & 1))) mma_done++;
+    }
+    if (tid == 0 && w_pending) mbar_wait(bar_w, 0);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (tid < 32) tmem_free(*tmem_slot, kTmemCols);
+}
+
+// ---- training: weight gradients ------------------------------------------------------------------
+// dW_l = dZ_l^T H_l over the batch's rows: one CTA (one warpgroup) per chunk of kWgRows rows and
+// layer, a product with M = 128 (the layer's outputs, zero beyond them), N = the layer's inputs
+// (160 or 64) and K = the chunk's rows, 128 at a time. Each thread stages one row: its dZ values
+// as column k of the A operand (dZ^T) and its H values as column k of the B operand (H^T), both
+// K-major; the sums stay in TMEM across the chunk, and each CTA writes its partial gradient,
+// which Adam sums over the chunks in chunk order (deterministic).
+constexpr int kWgRows = 1024;
+constexpr int kWgABytes = kTcRows * kTcRows * 2;  // 128 outputs x 128 rows
+constexpr int kWgBBytes = kIn * kTcRows * 2;      // up to 160 inputs x 128 rows
+constexpr int kWgSmem = kWgABytes + kWgBBytes + 256;
+// requested per CTA, so that at most two CTAs share an SM and their 256 TMEM columns each fit
+constexpr int kWgSmemReq = 80 * 1024;
+static_assert(kWgSmem <= kWgSmemReq && 3 * kWgSmemReq > 232448, "at most two CTAs per SM");
+constexpr int kWgTmemCols = 256;
+
+struct TcWgradArgs {
+    const uint16_t *h[kLayers];
+    const uint16_t *dz[kLayers];
+    long long n_host;
+    const int *n_dev;
+    long long off, cap;
+    float *partial;  // [chunk][kParams]
+    unsigned *err;
+    long long wait_cycles;
+};
+
+// bf16 index of element (r, k) of a K-major operand of R rows (R a multiple of 8)
+__device__ __forceinline__ int kmajor_offset(int r, int k, int R) { return ((k >> 3) * (R >> 3) + (r >> 3)) * 64 + (r & 7) * 8 + (k & 7); }
+
+__global__ void __launch_bounds__(kTcRows, 1) k_mlp_wgrad_tc(TcWgradArgs a) {
+    extern __shared__ __align__(128) uint8_t smem[];
+    uint16_t *As = reinterpret_cast<uint16_t *>(smem);
+    uint16_t *Bs = reinterpret_cast<uint16_t *>(smem + kWgABytes);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + kWgABytes + kWgBBytes);
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bar + 1);
+    int *ok = reinterpret_cast<int *>(tmem_slot + 1);
+    const int l = blockIdx.y, tid = threadIdx.x, warp = tid >> 5;
+    const int in = layer_in(l), out = layer_out(l);
+    const long long n = tc_rows(a.n_host, a.n_dev, a.off, a.cap);
+    const long long c0 = (long long)blockIdx.x * kWgRows, c1 = c0 + kWgRows < n ? c0 + kWgRows : n;
+    float *P = a.partial + (size_t)blockIdx.x * kParams + w_offset(l);
+    if (c0 >= n) {  // a chunk without rows adds nothing
+        for (int i = tid; i < out * in; i += kTcRows) P[i] = 0.0f;
+        return;
+    }
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        *ok = 1;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    for (int i = tid; i < kWgABytes / 16; i += kTcRows)  // A rows beyond the outputs stay zero
+        reinterpret_cast<uint4 *>(As)[i] = make_uint4(0u, 0u, 0u, 0u);
+    __syncthreads();
+    if (tid < 32) tmem_alloc(tmem_slot, kWgTmemCols);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    int issued = 0, done = 0;
+    for (long long k0 = c0; k0 < c1; k0 += kTcRows) {
+        const long long row = k0 + tid;
+        const bool own = row < c1;
+        // column tid of A = dZ^T (outputs 0 .. out-1)
+        for (int m0 = 0; m0 < out; m0 += 8) {
+            uint4 v = make_uint4(0u, 0u, 0u, 0u);
+            if (own) v = *reinterpret_cast<const uint4 *>(a.dz[l] + row * out + m0);
+            const uint16_t e[8] = {(uint16_t)(v.x & 0xffffu), (uint16_t)(v.x >> 16), (uint16_t)(v.y & 0xffffu),
+                                   (uint16_t)(v.y >> 16),     (uint16_t)(v.z & 0xffffu), (uint16_t)(v.z >> 16),
+                                   (uint16_t)(v.w & 0xffffu), (uint16_t)(v.w >> 16)};
+#pragma unroll
+            for (int j = 0; j < 8; j++) As[kmajor_offset(m0 + j, tid, kTcRows)] = e[j];
+        }
+        // column tid of B = H^T (inputs 0 .. in-1)
+        for (int n0 = 0; n0 < in; n0 += 8) {
+            uint4 v = make_uint4(0u, 0u, 0u, 0u);
+            if (own) v = *reinterpret_cast<const uint4 *>(a.h[l] + row * in + n0);
+            const uint16_t e[8] = {(uint16_t)(v.x & 0xffffu), (uint16_t)(v.x >> 16), (uint16_t)(v.y & 0xffffu),
+                                   (uint16_t)(v.y >> 16),     (uint16_t)(v.z & 0xffffu), (uint16_t)(v.z >> 16),
+                                   (uint16_t)(v.w & 0xffffu), (uint16_t)(v.w >> 16)};
+#pragma unroll
+            for (int j = 0; j < 8; j++) Bs[kmajor_offset(n0 + j, tid, in)] = e[j];
+        }
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (tid == 0) {
+            const uint32_t a0 = saddr(As), b0 = saddr(Bs);
+            const uint32_t idesc = idesc_bf16(kTcRows, in);
+            for (int s2 = 0; s2 < kTcRows / 16; s2++)
+                umma(tmem, sdesc(a0 + s2 * 2 * (kTcRows / 8) * 128, (kTcRows / 8) * 128, 128),
+                     sdesc(b0 + s2 * 2 * (in / 8) * 128, (in / 8) * 128, 128), idesc, (k0 > c0 || s2 > 0) ? 1u : 0u);
+            umma_commit(bar);
+            issued++;
+            if (mbar_wait(bar, (uint32_t)(done & 1), a.wait_cycles)) done++;
+            else *ok = 0;
+        }
+        __syncthreads();
+        tc_fence_after();
+        if (!*ok) break;  // the products may still read the operands: stage nothing more
+    }
+    if (*ok) {  // row m of the sums = TMEM lane m; warp w holds lanes 32w .. 32w + 31
+        const int m = warp * 32 + (tid & 31);
+        const uint32_t la = tmem + ((uint32_t)(warp * 32) << 16);
+        for (int c = 0; c < in; c += 16) {
+            float v[16];
+            tmem_ld16(la + c, v);
+            tmem_wait_ld();
+            if (m < out)
+#pragma unroll
+                for (int j = 0; j < 16; j++) P[m * in + c + j] = v[j];
+        }
+    }
+    if (tid == 0) {
+        if (!*ok) atomicOr(a.err, kErrMlpWait);
+        while (done < issued && mbar_wait(bar, (uint32_t)(done & 1))) done++;
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (tid < 32) tmem_free(*tmem_slot, kWgTmemCols);
+}
+
 tt_status tc_setup() {
-    const cudaError_t e =
-        cudaFuncSetAttribute(k_mlp_forward_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
+    cudaError_t e = cudaFuncSetAttribute(k_mlp_forward_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_mlp_forward_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_mlp_backward_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcBackSmem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_mlp_wgrad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kWgSmemReq);
     if (e != cudaSuccess) return fail(TT_ERR_CUDA, std::string("tensor-core MLP setup: ") + cudaGetErrorString(e));
     return TT_OK;
 }
 
 size_t tc_weight_elems() { return kTcWeights; }
+size_t tcT_weight_elems() { return kTcTWeights; }
 
 void tc_relayout(const float *w_f32, uint16_t *w_tc, cudaStream_t s) {
     k_tc_layout<<<(kTcWeights + 255) / 256, 256, 0, s>>>(w_f32, w_tc);
+}
+
+void tcT_relayout(const float *w_f32, uint16_t *w_tcT, cudaStream_t s) {
+    k_tcT_layout<<<(kTcTWeights + 255) / 256, 256, 0, s>>>(w_f32, w_tcT);
+}
+
+int tc_wgrad_chunks(long long rows) { return (int)((rows + kWgRows - 1) / kWgRows); }
+
+static int tc_grid(long long rows, int num_sms) {
+    const long long tiles = (rows + kTcRows - 1) / kTcRows;
+    const long long want = (tiles + kTcGroups - 1) / kTcGroups;  // blocks, each with kTcGroups groups
+    return (int)(want < 1 ? 1 : (want < num_sms ? want : num_sms));
+}
+
+tt_status tc_train(const TcTrainArgs &t, cudaStream_t s) {
+    const long long rows = t.n_dev ? t.cap : t.n_host;
+    const long long wc = t.wait_cycles > 0 ? t.wait_cycles : kWaitCycles;
+    TcArgs f;
+    std::memset(&f, 0, sizeof(f));
+    f.w = t.w_tc;
+    f.rec = t.rec;
+    f.n_host = t.n_host;
+    f.n_dev = t.n_dev;
+    f.off = t.off;
+    f.cap = t.cap;
+    for (int i = 0; i < 3; i++) {
+        f.enc.lo[i] = t.lo[i];
+        f.enc.inv_ext[i] = t.inv_ext[i];
+    }
+    f.y = t.y;
+    for (int l = 0; l < kLayers; l++) f.h[l] = t.h[l];
+    f.err = t.err;
+    f.wait_cycles = wc;
+    const int grid = tc_grid(rows, t.num_sms);
+    k_mlp_forward_tc<true><<<grid, kTcThreads, kTcSmem, s>>>(f);
+    TcBackArgs b;
+    std::memset(&b, 0, sizeof(b));
+    b.wT = t.w_tcT;
+    b.y = t.y;
+    b.target = t.target;
+    for (int l = 0; l < kLayers; l++) {
+        b.h[l] = t.h[l];
+        b.dz[l] = t.dz[l];
+    }
+    b.loss = t.loss;
+    b.n_host = t.n_host;
+    b.n_dev = t.n_dev;
+    b.off = t.off;
+    b.cap = t.cap;
+    b.err = t.err;
+    b.wait_cycles = wc;
+    k_mlp_backward_tc<<<grid, kTcThreads, kTcBackSmem, s>>>(b);
+    TcWgradArgs w;
+    std::memset(&w, 0, sizeof(w));
+    for (int l = 0; l < kLayers; l++) {
+        w.h[l] = t.h[l];
+        w.dz[l] = t.dz[l];
+    }
+    w.n_host = t.n_host;
+    w.n_dev = t.n_dev;
+    w.off = t.off;
+    w.cap = t.cap;
+    w.partial = t.partial;
+    w.err = t.err;
+    w.wait_cycles = wc;
+    k_mlp_wgrad_tc<<<dim3(tc_wgrad_chunks(rows), kLayers), kTcRows, kWgSmemReq, s>>>(w);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(TT_ERR_CUDA, std::string("tensor-core MLP training: ") + cudaGetErrorString(e));
+    return TT_OK;
 }
 
 tt_status tc_infer(const uint16_t *w_tc, const float *rec, long long n_host, const int *n_dev, long long cap,
                    const float lo[3], const float inv_ext[3], float *rgb, unsigned *err, int num_sms,
                    long long wait_cycles, cudaStream_t s) {
     TcArgs a;
+    std::memset(&a, 0, sizeof(a));
     a.wait_cycles = wait_cycles > 0 ? wait_cycles : kWaitCycles;
     a.w = w_tc;
     a.rec = rec;
@@ -447,7 +872,7 @@ tt_status tc_infer(const uint16_t *w_tc, const float *rec, long long n_host, con
     const long long tiles = (rows + kTcRows - 1) / kTcRows;
     const long long want = (tiles + kTcGroups - 1) / kTcGroups;  // blocks, each with kTcGroups groups
     const int grid = (int)(want < 1 ? 1 : (want < num_sms ? want : num_sms));
-    k_mlp_forward_tc<<<grid, kTcThreads, kTcSmem, s>>>(a);
+    k_mlp_forward_tc<false><<<grid, kTcThreads, kTcSmem, s>>>(a);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(TT_ERR_CUDA, std::string("tensor-core MLP: ") + cudaGetErrorString(e));
     return TT_OK;

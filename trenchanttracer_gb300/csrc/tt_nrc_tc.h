@@ -24,5 +24,31 @@ tt_status tc_infer(const uint16_t *w_tc, const float *rec, long long n_host, con
                    const float lo[3], const float inv_ext[3], float *rgb, unsigned *err, int num_sms,
                    long long wait_cycles, cudaStream_t s);
 
+// BF16 elements of the transposed operand layout of layers 1..5 (the backward pass's B operand)
+size_t tcT_weight_elems();
+void tcT_relayout(const float *w_f32, uint16_t *w_tcT, cudaStream_t s);
+// chunks (partial gradients) of a weight-gradient pass over `rows` rows
+int tc_wgrad_chunks(long long rows);
+
+// One training pass on the tensor cores over rows [0, rows) of the call (rows = clamp(*n_dev - off,
+// 0, cap) with n_dev set, else n_host): forward (storing each layer's input H_l and the raw
+// outputs y), backward (dZ_l, the loss) and the weight gradients, one partial per chunk of rows.
+struct TcTrainArgs {
+    const uint16_t *w_tc, *w_tcT;
+    const float *rec, *target;  // the pass's first row
+    long long n_host;
+    const int *n_dev;
+    long long off, cap;
+    float lo[3], inv_ext[3];
+    float *y;
+    uint16_t *h[6], *dz[6];
+    float *loss;
+    float *partial;
+    unsigned *err;
+    int num_sms;
+    long long wait_cycles;
+};
+tt_status tc_train(const TcTrainArgs &t, cudaStream_t s);
+
 }  // namespace nrc
 }  // namespace tt
