@@ -947,7 +947,7 @@ def run_mlp(args) -> None:
     rec = torch.rand((n, 16), generator=g, device=dev) * 2 - 1
     rec[:, 9:13] = rec[:, 9:13].abs()
     tgt = torch.rand((n, 3), generator=g, device=dev) + 0.1
-    cache = Cache([-1.0] * 3, [1.0] * 3)
+    cache = Cache([-1.0] * 3, [1.0] * 3, mma_kind=args.mma_kind)
     stream = torch.cuda.current_stream(dev)
     for _ in range(args.warmup):
         cache.infer(rec)
@@ -966,6 +966,22 @@ def run_mlp(args) -> None:
             inf_ms.append(e0.elapsed_time(e1))
             tr_ms.append(e1.elapsed_time(e2))
     assert torch.isfinite(out).all()
+    # the same training at 2^18 rows per Adam step, where the batch fills the GPU
+    big = Cache([-1.0] * 3, [1.0] * 3, batch=1 << 18, mma_kind=args.mma_kind)
+    for _ in range(2):
+        big.train(rec[:1 << 20], tgt[:1 << 20], steps=4)
+    torch.cuda.synchronize(dev)
+    big_ms = []
+    for _ in range(max(3, args.steps // 2)):
+        e0, e1 = torch.cuda.Event(True), torch.cuda.Event(True)
+        e0.record(stream)
+        big.train(rec[:1 << 20], tgt[:1 << 20], steps=4)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        big_ms.append(e0.elapsed_time(e1))
+    big_tr = float(np.median(big_ms))
+    big.check()
+    cache.check()
     inf = float(np.median(inf_ms))
     tr = float(np.median(tr_ms))
     inf_tf = 2.0 * MLP_MACS * n / (inf * 1e-3) / 1e12
@@ -976,13 +992,16 @@ def run_mlp(args) -> None:
         "ms_per_step": round(inf, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "bf16 (fp32 accumulation)", "data": "synthetic (random feature records)",
         "config": {"workload": f"MLP 160-64x5-3 (padded to 8 outputs), inference on {n} records incl. encoding; "
-                               "training = 4 Adam steps of 16,384 rows", "macs_per_row": MLP_MACS},
-        "training": {"ms_per_frame": round(tr, 4), "tflops": round(tr_tf, 2)},
+                               "training = 4 Adam steps of 16,384 rows", "macs_per_row": MLP_MACS,
+                   "kernels": "tcgen05 + TMEM" if args.mma_kind == 0 else "mma.sync m16n8k16"},
+        "training": {"ms_per_frame": round(tr, 4), "tflops": round(tr_tf, 2),
+                     "at_2^18_rows_per_step": {"ms_per_4_steps": round(big_tr, 4),
+                                               "tflops": round(3 * 2.0 * MLP_MACS * (1 << 20) / (big_tr * 1e-3) / 1e12, 2)}},
         "roofline": {"bound": "tensor", "achieved": round(inf_tf, 2), "peak": peak, "unit": "TFLOP/s",
                      "frac": round(inf_tf / peak, 4), "traffic": None,
                      "peak_source": "measured bf16_tflops (MEASURED_PEAKS.json)" if peaks else "fallback"},
         "clocks": clk.summary(),
-        "gpu_launches": args.steps * (1 + 4 * 5),
+        "gpu_launches": args.steps * (1 + 4 * 4),  # inference; per Adam step forward, backward, wgrad, Adam
     }
     print(json.dumps(line), flush=True)
 
@@ -996,6 +1015,8 @@ def main() -> None:
     ap.add_argument("--workload", choices=["terrain", "cornell", "multimaterial", "batch", "cache", "mlp"], default="terrain")
     ap.add_argument("--cache-scene", choices=["multimaterial", "terrain"], default="multimaterial")
     ap.add_argument("--views", type=int, default=64, help="batch: the first N of the 64 orbit views (profiling)")
+    ap.add_argument("--mma-kind", type=int, choices=[0, 1], default=0,
+                    help="mlp: the cache's tensor-core kernels, 0 tcgen05 + TMEM, 1 mma.sync (comparison)")
     ap.add_argument("--launch", default="",
                     help="batch: block,stack_shared,wave_paths,ordered,streamed instead of autotuning (profiling)")
     ap.add_argument("--width", type=int, default=1920)

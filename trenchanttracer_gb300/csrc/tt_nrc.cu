@@ -670,7 +670,7 @@ tt_status train_pass(tt_cache *c, const float *rec, const float *target, long lo
         t.wait_cycles = c->p.wait_limit;
         const tt_status st = tc_train(t, s);
         if (st != TT_OK) return st;
-        chunks = tc_wgrad_chunks(rows);
+        chunks = tc_wgrad_chunks(rows, c->num_sms);
     } else {  // mma.sync
         const int grid = fwd_grid(c, rows);
         k_mlp_forward<true><<<grid, kThreads, kFwdSmem, s>>>(a);
@@ -966,7 +966,8 @@ tt_status tt_cache_train(tt_cache *c, const float *d_records, const float *d_tar
     TT_CUDA_C(cudaMemsetAsync(c->loss, 0, sizeof(float), s));
     for (int k = 0; k < steps; k++) {
         const long long off = ((long long)k * c->p.batch) % n;
-        TT_CUDA_C(cudaMemsetAsync(c->partial, 0, sizeof(float) * (size_t)c->chunks * kParams, s));
+        // every partial that Adam sums is written by the weight-gradient kernel (zeros for chunks
+        // without rows), so the partials need no clearing
         const tt_status st = train_pass(c, d_records, d_targets, n, nullptr, off, 1, s);
         if (st != TT_OK) return st;
     }

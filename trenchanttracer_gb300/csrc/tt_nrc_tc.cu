@@ -62,7 +62,15 @@ static_assert(kABytes == kTcRows * kHidden * 2, "the hidden activations fill the
 constexpr int kTcWeightBytes = kTcWeights * 2;        // 55296
 // weights barrier; per group 2 record, 2 ring-slot and 1 product barriers; TMEM slot; flags
 constexpr int kTcBarBytes = 512;
-constexpr int kTcSmem = kTcGroups * (kABytes + kRecBufs * kRecBytes) + kTcWeightBytes + kTcBarBytes;
+// Shared memory and TMEM columns of a CTA of g warpgroups (inference: kTcGroups; training, whose
+// batches are a few hundred tiles: one, so that the tiles spread over every SM).
+__host__ __device__ constexpr int tc_smem(int g) {
+    return g * (kABytes + kRecBufs * kRecBytes) + kTcWeightBytes + kTcBarBytes;
+}
+__host__ __device__ constexpr int tc_tmem_cols(int g) {
+    return 64 * g <= 32 ? 32 : (64 * g <= 64 ? 64 : (64 * g <= 128 ? 128 : (64 * g <= 256 ? 256 : 512)));
+}
+constexpr int kTcSmem = tc_smem(kTcGroups);
 static_assert(kTcSmem <= 232448, "fits the 227 KB a CTA may use");
 static_assert(kTcWeightBytes % 16 == 0 && kABytes % 16 == 0 && kRecBytes % 16 == 0, "bulk copy sizes");
 static_assert(kTmemCols >= 64 * kTcGroups, "64 accumulator columns per group");
@@ -151,6 +159,10 @@ __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.
 __device__ __forceinline__ int a_offset(int r, int k) {  // bf16 element index in the A buffer
     return ((k >> 3) * 16 + (r >> 3)) * 64 + (r & 7) * 8 + (k & 7);
 }
+// bf16 index of element (r, k) of a K-major operand of R rows (R a multiple of 8)
+__device__ __forceinline__ int kmajor_offset(int r, int k, int R) {
+    return ((k >> 3) * (R >> 3) + (r >> 3)) * 64 + (r & 7) * 8 + (k & 7);
+}
 
 struct TcEncoding {
     float lo[3], inv_ext[3];
@@ -218,31 +230,31 @@ __device__ __forceinline__ void group_sync(int group) {  // the 128 threads of o
 }
 
 // kTrain: also writes every layer's input H_l and the raw outputs, for the backward pass.
-template <bool kTrain>
-__global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(TcArgs a) {
+template <bool kTrain, int kG>
+__global__ void __launch_bounds__(128 * kG, 1) k_mlp_forward_tc(TcArgs a) {
     extern __shared__ __align__(128) uint8_t smem[];
     const int tid = threadIdx.x, group = tid >> 7, gt = tid & 127, warp_in_group = gt >> 5;
     __nv_bfloat16 *A = reinterpret_cast<__nv_bfloat16 *>(smem + group * kABytes);
-    uint16_t *W = reinterpret_cast<uint16_t *>(smem + kTcGroups * kABytes);
-    float *R = reinterpret_cast<float *>(smem + kTcGroups * kABytes + kTcWeightBytes) +
+    uint16_t *W = reinterpret_cast<uint16_t *>(smem + kG * kABytes);
+    float *R = reinterpret_cast<float *>(smem + kG * kABytes + kTcWeightBytes) +
                (size_t)group * kRecBufs * kTcRows * kRec;  // this group's record buffers
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kTcGroups * (kABytes + kRecBufs * kRecBytes) + kTcWeightBytes);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kG * (kABytes + kRecBufs * kRecBytes) + kTcWeightBytes);
     uint64_t *bar_w = bars;                        // weights
     uint64_t *bar_rec = bars + 1 + 5 * group;      // [0] [1]: the group's record buffers
     uint64_t *bar_ring = bar_rec + 2;              // [0] [1]: the products that read each ring slot
     uint64_t *bar_mma = bar_rec + 4;               // the group's hidden and output layers
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 1 + 5 * kTcGroups);
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 1 + 5 * kG);
     int *ok_w = reinterpret_cast<int *>(tmem_slot + 1);  // the weights arrived
     int *ok = ok_w + 1 + group;                          // this group's waits all ended
-    static_assert(8 * (1 + 5 * kTcGroups) + 4 + 4 * (1 + kTcGroups) <= kTcBarBytes, "barrier block");
+    static_assert(8 * (1 + 5 * kG) + 4 + 4 * (1 + kG) <= kTcBarBytes, "barrier block");
 
     const long long n = tc_rows(a.n_host, a.n_dev, a.off, a.cap);
     const long long ntiles = (n + kTcRows - 1) / kTcRows;
-    if ((long long)blockIdx.x * kTcGroups >= ntiles) return;  // uniform per block: nothing allocated yet
+    if ((long long)blockIdx.x * kG >= ntiles) return;  // uniform per block: nothing allocated yet
 
     if (tid == 0) {
         mbar_init(bar_w, 1);
-        for (int g = 0; g < kTcGroups; g++) {
+        for (int g = 0; g < kG; g++) {
             for (int k = 0; k < 5; k++) mbar_init(bars + 1 + 5 * g + k, 1);
             ok_w[1 + g] = 1;
         }
@@ -250,14 +262,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(TcArgs a) {
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
-    if (tid < 32) tmem_alloc(tmem_slot, kTmemCols);
+    if (tid < 32) tmem_alloc(tmem_slot, tc_tmem_cols(kG));
     // Asynchronous operations of this group, counted by its issuing thread (gt == 0): the k-th
     // completion of a barrier is awaited with parity k & 1, and whatever was issued and not yet
     // awaited is drained (bounded) before the block exits.
     int rec_issued[2] = {0, 0}, rec_done[2] = {0, 0}, ring_issued[2] = {0, 0}, ring_done[2] = {0, 0};
     int mma_issued = 0, mma_done = 0;
-    const long long tstride = (long long)gridDim.x * kTcGroups;
-    const long long first = (long long)blockIdx.x * kTcGroups + group;
+    const long long tstride = (long long)gridDim.x * kG;
+    const long long first = (long long)blockIdx.x * kG + group;
     if (gt == 0 && first < ntiles) {  // the group's first records, while the weights come in
         const long long r0 = first * kTcRows;
         const uint32_t bytes = (uint32_t)((n - r0) < kTcRows ? (n - r0) : kTcRows) * kRec * 4;
@@ -422,7 +434,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_forward_tc(TcArgs a) {
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    if (tid < 32) tmem_free(*tmem_slot, kTmemCols);
+    if (tid < 32) tmem_free(*tmem_slot, tc_tmem_cols(kG));
 }
 
 __global__ void k_tc_layout(const float *w, uint16_t *out) {
@@ -480,8 +492,9 @@ struct TcBackArgs {
     long long wait_cycles;
 };
 constexpr int kTcTWeightBytes = kTcTWeights * 2;  // 34816
-constexpr int kTcBackSmem = kTcGroups * kABytes + kTcTWeightBytes + kTcBarBytes;
-static_assert(kTcBackSmem <= 232448 && kTcTWeightBytes % 16 == 0, "backward shared memory");
+__host__ __device__ constexpr int tc_back_smem(int g) { return g * kABytes + kTcTWeightBytes + kTcBarBytes; }
+static_assert(tc_back_smem(kTcGroups) <= 232448 && kTcTWeightBytes % 16 == 0, "backward shared memory");
+constexpr int kTrainGroups = 1;  // warpgroups per CTA of the training passes
 
 __device__ __forceinline__ bool bf16_pos(uint32_t bits16) { return bits16 != 0u && !(bits16 & 0x8000u); }
 
@@ -525,25 +538,26 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
     return *reinterpret_cast<const uint32_t *>(&b);
 }
 
-__global__ void __launch_bounds__(kTcThreads, 1) k_mlp_backward_tc(TcBackArgs a) {
+template <int kG>
+__global__ void __launch_bounds__(128 * kG, 1) k_mlp_backward_tc(TcBackArgs a) {
     extern __shared__ __align__(128) uint8_t smem[];
     const int tid = threadIdx.x, group = tid >> 7, gt = tid & 127, warp_in_group = gt >> 5;
     __nv_bfloat16 *A = reinterpret_cast<__nv_bfloat16 *>(smem + group * kABytes);
-    uint16_t *W = reinterpret_cast<uint16_t *>(smem + kTcGroups * kABytes);
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kTcGroups * kABytes + kTcTWeightBytes);
+    uint16_t *W = reinterpret_cast<uint16_t *>(smem + kG * kABytes);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + kG * kABytes + kTcTWeightBytes);
     uint64_t *bar_w = bars;                  // weights
     uint64_t *bar_mma = bars + 1 + group;    // the group's products
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 1 + kTcGroups);
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 1 + kG);
     int *ok_w = reinterpret_cast<int *>(tmem_slot + 1);
     int *ok = ok_w + 1 + group;
-    static_assert(8 * (1 + kTcGroups) + 4 + 4 * (1 + kTcGroups) <= kTcBarBytes, "barrier block");
+    static_assert(8 * (1 + kG) + 4 + 4 * (1 + kG) <= kTcBarBytes, "barrier block");
 
     const long long n = tc_rows(a.n_host, a.n_dev, a.off, a.cap);
     const long long ntiles = (n + kTcRows - 1) / kTcRows;
-    if ((long long)blockIdx.x * kTcGroups >= ntiles) return;  // uniform per block: nothing allocated yet
+    if ((long long)blockIdx.x * kG >= ntiles) return;  // uniform per block: nothing allocated yet
     if (tid == 0) {
         mbar_init(bar_w, 1);
-        for (int g = 0; g < kTcGroups; g++) {
+        for (int g = 0; g < kG; g++) {
             mbar_init(bars + 1 + g, 1);
             ok_w[1 + g] = 1;
         }
@@ -551,7 +565,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_backward_tc(TcBackArgs a)
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
-    if (tid < 32) tmem_alloc(tmem_slot, kTmemCols);
+    if (tid < 32) tmem_alloc(tmem_slot, tc_tmem_cols(kG));
     bool w_pending = false;
     if (tid == 0) {
         mbar_expect_tx(bar_w, kTcTWeightBytes);
@@ -572,8 +586,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_backward_tc(TcBackArgs a)
     const float inv_n = 1.0f / (float)n;
     float loss = 0.0f;
     int mma_issued = 0, mma_done = 0;
-    const long long tstride = (long long)gridDim.x * kTcGroups;
-    for (long long tile = (long long)blockIdx.x * kTcGroups + group; weights_ok && tile < ntiles; tile += tstride) {
+    const long long tstride = (long long)gridDim.x * kG;
+    for (long long tile = (long long)blockIdx.x * kG + group; weights_ok && tile < ntiles; tile += tstride) {
         const long long r0 = tile * kTcRows, row = r0 + gt;
         const bool own = row < n;
         float dy[3] = {0.f, 0.f, 0.f};
@@ -636,17 +650,19 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_mlp_backward_tc(TcBackArgs a)
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    if (tid < 32) tmem_free(*tmem_slot, kTmemCols);
+    if (tid < 32) tmem_free(*tmem_slot, tc_tmem_cols(kG));
 }
 
 // ---- training: weight gradients ------------------------------------------------------------------
-// dW_l = dZ_l^T H_l over the batch's rows: one CTA (one warpgroup) per chunk of kWgRows rows and
-// layer, a product with M = 128 (the layer's outputs, zero beyond them), N = the layer's inputs
-// (160 or 64) and K = the chunk's rows, 128 at a time. Each thread stages one row: its dZ values
-// as column k of the A operand (dZ^T) and its H values as column k of the B operand (H^T), both
-// K-major; the sums stay in TMEM across the chunk, and each CTA writes its partial gradient,
-// which Adam sums over the chunks in chunk order (deterministic).
-constexpr int kWgRows = 1024;
+// dW_l = dZ_l^T H_l over the batch's rows: one CTA per chunk of kWgRows rows and layer, a product
+// with M = 128 (the layer's outputs, zero beyond them), N = the layer's inputs (160 or 64) and K =
+// the chunk's rows, 128 at a time. The CTA stages each 128-row tile from the row-major H and dZ the
+// forward and backward passes wrote: one 16-byte row of a core matrix per item (eight consecutive
+// rows of one column; consecutive threads take consecutive columns, so each row's reads coalesce),
+// dZ^T as the A operand and H^T as the B operand, both K-major. The sums stay in TMEM across the
+// chunk, and each CTA writes its partial gradient, which Adam sums over the chunks in chunk order
+// (deterministic).
+constexpr int kWgMinRows = 256;  // rows per chunk: at least this, more for large batches (tc_wgrad_rows)
 constexpr int kWgABytes = kTcRows * kTcRows * 2;  // 128 outputs x 128 rows
 constexpr int kWgBBytes = kIn * kTcRows * 2;      // up to 160 inputs x 128 rows
 constexpr int kWgSmem = kWgABytes + kWgBBytes + 256;
@@ -654,10 +670,12 @@ constexpr int kWgSmem = kWgABytes + kWgBBytes + 256;
 constexpr int kWgSmemReq = 80 * 1024;
 static_assert(kWgSmem <= kWgSmemReq && 3 * kWgSmemReq > 232448, "at most two CTAs per SM");
 constexpr int kWgTmemCols = 256;
+constexpr int kWgThreads = 512;  // staging threads; warps 0-3 also read the sums out of TMEM
 
 struct TcWgradArgs {
     const uint16_t *h[kLayers];
     const uint16_t *dz[kLayers];
+    int chunk_rows;  // a multiple of 128
     long long n_host;
     const int *n_dev;
     long long off, cap;
@@ -666,10 +684,7 @@ struct TcWgradArgs {
     long long wait_cycles;
 };
 
-// bf16 index of element (r, k) of a K-major operand of R rows (R a multiple of 8)
-__device__ __forceinline__ int kmajor_offset(int r, int k, int R) { return ((k >> 3) * (R >> 3) + (r >> 3)) * 64 + (r & 7) * 8 + (k & 7); }
-
-__global__ void __launch_bounds__(kTcRows, 1) k_mlp_wgrad_tc(TcWgradArgs a) {
+__global__ void __launch_bounds__(kWgThreads, 1) k_mlp_wgrad_tc(TcWgradArgs a) {
     extern __shared__ __align__(128) uint8_t smem[];
     uint16_t *As = reinterpret_cast<uint16_t *>(smem);
     uint16_t *Bs = reinterpret_cast<uint16_t *>(smem + kWgABytes);
@@ -679,10 +694,10 @@ __global__ void __launch_bounds__(kTcRows, 1) k_mlp_wgrad_tc(TcWgradArgs a) {
     const int l = blockIdx.y, tid = threadIdx.x, warp = tid >> 5;
     const int in = layer_in(l), out = layer_out(l);
     const long long n = tc_rows(a.n_host, a.n_dev, a.off, a.cap);
-    const long long c0 = (long long)blockIdx.x * kWgRows, c1 = c0 + kWgRows < n ? c0 + kWgRows : n;
+    const long long c0 = (long long)blockIdx.x * a.chunk_rows, c1 = c0 + a.chunk_rows < n ? c0 + a.chunk_rows : n;
     float *P = a.partial + (size_t)blockIdx.x * kParams + w_offset(l);
     if (c0 >= n) {  // a chunk without rows adds nothing
-        for (int i = tid; i < out * in; i += kTcRows) P[i] = 0.0f;
+        for (int i = tid; i < out * in; i += kWgThreads) P[i] = 0.0f;
         return;
     }
     if (tid == 0) {
@@ -690,7 +705,7 @@ __global__ void __launch_bounds__(kTcRows, 1) k_mlp_wgrad_tc(TcWgradArgs a) {
         *ok = 1;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    for (int i = tid; i < kWgABytes / 16; i += kTcRows)  // A rows beyond the outputs stay zero
+    for (int i = tid; i < kWgABytes / 16; i += kWgThreads)  // A rows beyond the outputs stay zero
         reinterpret_cast<uint4 *>(As)[i] = make_uint4(0u, 0u, 0u, 0u);
     __syncthreads();
     if (tid < 32) tmem_alloc(tmem_slot, kWgTmemCols);
@@ -700,27 +715,22 @@ __global__ void __launch_bounds__(kTcRows, 1) k_mlp_wgrad_tc(TcWgradArgs a) {
     const uint32_t tmem = *tmem_slot;
     int issued = 0, done = 0;
     for (long long k0 = c0; k0 < c1; k0 += kTcRows) {
-        const long long row = k0 + tid;
-        const bool own = row < c1;
-        // column tid of A = dZ^T (outputs 0 .. out-1)
-        for (int m0 = 0; m0 < out; m0 += 8) {
-            uint4 v = make_uint4(0u, 0u, 0u, 0u);
-            if (own) v = *reinterpret_cast<const uint4 *>(a.dz[l] + row * out + m0);
-            const uint16_t e[8] = {(uint16_t)(v.x & 0xffffu), (uint16_t)(v.x >> 16), (uint16_t)(v.y & 0xffffu),
-                                   (uint16_t)(v.y >> 16),     (uint16_t)(v.z & 0xffffu), (uint16_t)(v.z >> 16),
-                                   (uint16_t)(v.w & 0xffffu), (uint16_t)(v.w >> 16)};
+        const int nk = (int)(c1 - k0 < kTcRows ? c1 - k0 : kTcRows);  // rows past the chunk are zero
+#pragma unroll 2
+        for (int it = tid; it < (out + in) * (kTcRows / 8); it += kWgThreads) {
+            const bool is_a = it < out * (kTcRows / 8);
+            const int w = is_a ? out : in, j = is_a ? it : it - out * (kTcRows / 8);
+            const int col = j % w, k8 = j / w;
+            const uint16_t *src = (is_a ? a.dz[l] : a.h[l]) + (k0 + 8 * k8) * w + col;
+            uint32_t pk[4];
 #pragma unroll
-            for (int j = 0; j < 8; j++) As[kmajor_offset(m0 + j, tid, kTcRows)] = e[j];
-        }
-        // column tid of B = H^T (inputs 0 .. in-1)
-        for (int n0 = 0; n0 < in; n0 += 8) {
-            uint4 v = make_uint4(0u, 0u, 0u, 0u);
-            if (own) v = *reinterpret_cast<const uint4 *>(a.h[l] + row * in + n0);
-            const uint16_t e[8] = {(uint16_t)(v.x & 0xffffu), (uint16_t)(v.x >> 16), (uint16_t)(v.y & 0xffffu),
-                                   (uint16_t)(v.y >> 16),     (uint16_t)(v.z & 0xffffu), (uint16_t)(v.z >> 16),
-                                   (uint16_t)(v.w & 0xffffu), (uint16_t)(v.w >> 16)};
-#pragma unroll
-            for (int j = 0; j < 8; j++) Bs[kmajor_offset(n0 + j, tid, in)] = e[j];
+            for (int q = 0; q < 4; q++) {
+                const uint32_t lo = 8 * k8 + 2 * q < nk ? src[(2 * q) * w] : 0u;
+                const uint32_t hi = 8 * k8 + 2 * q + 1 < nk ? src[(2 * q + 1) * w] : 0u;
+                pk[q] = lo | (hi << 16);
+            }
+            uint16_t *dst = is_a ? As + kmajor_offset(col, 8 * k8, kTcRows) : Bs + kmajor_offset(col, 8 * k8, in);
+            *reinterpret_cast<uint4 *>(dst) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
         }
         fence_async_smem();
         tc_fence_before();
@@ -741,7 +751,7 @@ __global__ void __launch_bounds__(kTcRows, 1) k_mlp_wgrad_tc(TcWgradArgs a) {
         tc_fence_after();
         if (!*ok) break;  // the products may still read the operands: stage nothing more
     }
-    if (*ok) {  // row m of the sums = TMEM lane m; warp w holds lanes 32w .. 32w + 31
+    if (*ok && warp < 4) {  // row m of the sums = TMEM lane m; warp w reads lanes 32w .. 32w + 31
         const int m = warp * 32 + (tid & 31);
         const uint32_t la = tmem + ((uint32_t)(warp * 32) << 16);
         for (int c = 0; c < in; c += 16) {
@@ -764,11 +774,20 @@ __global__ void __launch_bounds__(kTcRows, 1) k_mlp_wgrad_tc(TcWgradArgs a) {
 }
 
 tt_status tc_setup() {
-    cudaError_t e = cudaFuncSetAttribute(k_mlp_forward_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
+    cudaError_t e = cudaFuncSetAttribute(k_mlp_forward_tc<false, kTcGroups>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_mlp_forward_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
+        e = cudaFuncSetAttribute(k_mlp_forward_tc<true, kTrainGroups>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 tc_smem(kTrainGroups));
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_mlp_backward_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcBackSmem);
+        e = cudaFuncSetAttribute(k_mlp_forward_tc<true, kTcGroups>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 tc_smem(kTcGroups));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_mlp_backward_tc<kTrainGroups>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 tc_back_smem(kTrainGroups));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_mlp_backward_tc<kTcGroups>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 tc_back_smem(kTcGroups));
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_mlp_wgrad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kWgSmemReq);
     if (e != cudaSuccess) return fail(TT_ERR_CUDA, std::string("tensor-core MLP setup: ") + cudaGetErrorString(e));
@@ -786,12 +805,24 @@ void tcT_relayout(const float *w_f32, uint16_t *w_tcT, cudaStream_t s) {
     k_tcT_layout<<<(kTcTWeights + 255) / 256, 256, 0, s>>>(w_f32, w_tcT);
 }
 
-int tc_wgrad_chunks(long long rows) { return (int)((rows + kWgRows - 1) / kWgRows); }
+// rows per weight-gradient chunk: about two chunks per SM for each layer, 256 .. 4096 rows
+static int tc_wgrad_rows(long long rows, int num_sms) {
+    int c = kWgMinRows;
+    while (c < 4096 && (long long)c * 2 * num_sms < rows) c *= 2;
+    return c;
+}
 
-static int tc_grid(long long rows, int num_sms) {
+int tc_wgrad_chunks(long long rows, int num_sms) {
+    const int c = tc_wgrad_rows(rows, num_sms);
+    return (int)((rows + c - 1) / c);
+}
+
+// blocks of g groups for the tiles of `rows`, at most `per_sm` resident blocks per SM
+static int tc_grid(long long rows, int g, int num_sms, int per_sm) {
     const long long tiles = (rows + kTcRows - 1) / kTcRows;
-    const long long want = (tiles + kTcGroups - 1) / kTcGroups;  // blocks, each with kTcGroups groups
-    return (int)(want < 1 ? 1 : (want < num_sms ? want : num_sms));
+    const long long want = (tiles + g - 1) / g;
+    const long long most = (long long)num_sms * per_sm;
+    return (int)(want < 1 ? 1 : (want < most ? want : most));
 }
 
 tt_status tc_train(const TcTrainArgs &t, cudaStream_t s) {
@@ -813,8 +844,12 @@ tt_status tc_train(const TcTrainArgs &t, cudaStream_t s) {
     for (int l = 0; l < kLayers; l++) f.h[l] = t.h[l];
     f.err = t.err;
     f.wait_cycles = wc;
-    const int grid = tc_grid(rows, t.num_sms);
-    k_mlp_forward_tc<true><<<grid, kTcThreads, kTcSmem, s>>>(f);
+    // A batch of fewer tiles than six per SM: one group per block, so that the tiles spread over
+    // every SM (two blocks fit an SM); larger ones: six groups per block, as inference runs.
+    const bool wide = (rows + kTcRows - 1) / kTcRows >= (long long)kTcGroups * t.num_sms;
+    const int grid = wide ? tc_grid(rows, kTcGroups, t.num_sms, 1) : tc_grid(rows, kTrainGroups, t.num_sms, 2);
+    if (wide) k_mlp_forward_tc<true, kTcGroups><<<grid, 128 * kTcGroups, tc_smem(kTcGroups), s>>>(f);
+    else k_mlp_forward_tc<true, kTrainGroups><<<grid, 128 * kTrainGroups, tc_smem(kTrainGroups), s>>>(f);
     TcBackArgs b;
     std::memset(&b, 0, sizeof(b));
     b.wT = t.w_tcT;
@@ -831,7 +866,8 @@ tt_status tc_train(const TcTrainArgs &t, cudaStream_t s) {
     b.cap = t.cap;
     b.err = t.err;
     b.wait_cycles = wc;
-    k_mlp_backward_tc<<<grid, kTcThreads, kTcBackSmem, s>>>(b);
+    if (wide) k_mlp_backward_tc<kTcGroups><<<grid, 128 * kTcGroups, tc_back_smem(kTcGroups), s>>>(b);
+    else k_mlp_backward_tc<kTrainGroups><<<grid, 128 * kTrainGroups, tc_back_smem(kTrainGroups), s>>>(b);
     TcWgradArgs w;
     std::memset(&w, 0, sizeof(w));
     for (int l = 0; l < kLayers; l++) {
@@ -845,7 +881,8 @@ tt_status tc_train(const TcTrainArgs &t, cudaStream_t s) {
     w.partial = t.partial;
     w.err = t.err;
     w.wait_cycles = wc;
-    k_mlp_wgrad_tc<<<dim3(tc_wgrad_chunks(rows), kLayers), kTcRows, kWgSmemReq, s>>>(w);
+    w.chunk_rows = tc_wgrad_rows(rows, t.num_sms);
+    k_mlp_wgrad_tc<<<dim3(tc_wgrad_chunks(rows, t.num_sms), kLayers), kWgThreads, kWgSmemReq, s>>>(w);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(TT_ERR_CUDA, std::string("tensor-core MLP training: ") + cudaGetErrorString(e));
     return TT_OK;
@@ -869,10 +906,8 @@ tt_status tc_infer(const uint16_t *w_tc, const float *rec, long long n_host, con
     a.rgb = rgb;
     a.err = err;
     const long long rows = n_dev ? cap : n_host;
-    const long long tiles = (rows + kTcRows - 1) / kTcRows;
-    const long long want = (tiles + kTcGroups - 1) / kTcGroups;  // blocks, each with kTcGroups groups
-    const int grid = (int)(want < 1 ? 1 : (want < num_sms ? want : num_sms));
-    k_mlp_forward_tc<false><<<grid, kTcThreads, kTcSmem, s>>>(a);
+    const int grid = tc_grid(rows, kTcGroups, num_sms, 1);
+    k_mlp_forward_tc<false, kTcGroups><<<grid, kTcThreads, kTcSmem, s>>>(a);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return fail(TT_ERR_CUDA, std::string("tensor-core MLP: ") + cudaGetErrorString(e));
     return TT_OK;

@@ -28,7 +28,7 @@ tt_status tc_infer(const uint16_t *w_tc, const float *rec, long long n_host, con
 size_t tcT_weight_elems();
 void tcT_relayout(const float *w_f32, uint16_t *w_tcT, cudaStream_t s);
 // chunks (partial gradients) of a weight-gradient pass over `rows` rows
-int tc_wgrad_chunks(long long rows);
+int tc_wgrad_chunks(long long rows, int num_sms);
 
 // One training pass on the tensor cores over rows [0, rows) of the call (rows = clamp(*n_dev - off,
 // 0, cap) with n_dev set, else n_host): forward (storing each layer's input H_l and the raw
