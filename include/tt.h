@@ -474,7 +474,8 @@ typedef struct tt_cache_params {
     uint32_t seed;               /* weight initialisation (1) */
     int32_t use_ema;             /* render with the averaged weights (1) */
     float bbox_lo[3], bbox_hi[3];/* scene bounds of the position encoding */
-    int32_t mma_kind;            /* inference kernel: 0 tcgen05 + TMEM (default), 1 mma.sync */
+    int32_t mma_kind;            /* the tensor-core kernels of inference and training: 0 tcgen05 +
+                                    TMEM (default), 1 mma.sync */
     int32_t wait_limit;          /* tcgen05 inference: clock cycles one wait for a copy or a product
                                     may take before it counts as run out (0: about a second). A wait
                                     that runs out ends the launch with tt_cache_check reporting
