@@ -237,3 +237,35 @@ def test_ordered_queues_give_the_same_image():
     finally:
         r.set_launch(*old)
     assert np.array_equal(gpu.view(np.uint32), _oracle(bvh, sc, None, small, params).view(np.uint32))
+
+
+def test_launch_counter_matches_the_issued_sequence():
+    """tt_renderer_launches counts the kernels a render issues: in waves, per wave raygen,
+    accumulate and per bounce extend / shade / shadow (+ 4 ordering kernels and the hit gather, and
+    with an environment 4 more for the shadow queue); streamed, an init, per iteration plan,
+    accumulate, refill, extend, shade, shadow (+ the same ordering kernels) and a final plan and
+    accumulate, over ceil(paths / pool) * depth + depth iterations."""
+    import math
+    sc = Scene.from_mesh(scenes.cornell(subdiv=2))
+    sc.set_env(scenes.sky_env(32, 16))
+    _, _, r = _setup(sc)
+    cam = make_camera_meta(40, 30, [0.0, 0.0, 1.55], [0.0, 0.0, -1.0], fov=(45.0, 35.0))
+    depth, spp = 5, 3
+    paths = 40 * 30 * spp
+    params = render_params(spp=spp, max_depth=depth, rr_depth=3, seed=4)
+    old = r.launch
+    try:
+        for wave, ordered, streamed in [(1 << 22, 0, 1), (1 << 22, 1, 1), (1000, 0, 0), (1000, 1, 0), (1000, 0, 1),
+                                        (1000, 1, 1)]:
+            r.set_launch(128, 16, wave, ordered, streamed)
+            r.launches(reset=True)
+            _render(r, cam, params)
+            got = r.launches(reset=True)
+            if streamed and paths > wave:
+                iters = math.ceil(paths / wave) * depth + depth
+                want = 1 + iters * (6 + (9 if ordered else 0)) + 2
+            else:
+                want = math.ceil(paths / wave) * (2 + depth * (12 if ordered else 3))
+            assert got == want, (wave, ordered, streamed, got, want)
+    finally:
+        r.set_launch(*old)
