@@ -503,16 +503,15 @@ def run_ours(args) -> None:
 RENDER_CONFIGS = {
     "cornell": dict(desc="Cornell box (10 wall tris + 0.25 x 0.25 ceiling light 17,12,4) + subdivision-5 "
                          "icosphere r 0.3 (seed-42 noise 0.03, Lambert 0.8), 20,492 tris; 512 x 512, 16 spp, "
-                         "depth 8, Russian roulette from 4, PCG32", width=512, height=512, spp=16, depth=8,
-                    ordered=1),
+                         "depth 8, Russian roulette from 4, PCG32", width=512, height=512, spp=16, depth=8),
     "multimaterial": dict(desc="400 displaced subdivision-5 icospheres (8,192,002 tris incl. ground), Lambert / "
                                "GGX / dielectric 1.5; 2048 x 1024 sky with a 0.5-degree sun of 5e4, 2D-CDF light "
                                "sampling with MIS; 1920 x 1080, 64 spp, depth 16, Russian roulette from 4",
-                          width=1920, height=1080, spp=64, depth=16, ordered=0),
+                          width=1920, height=1080, spp=64, depth=16),
 }
-# ordered: whether the extension queues are ordered before tracing, the faster setting measured
-# on a GB300 (Cornell 921 vs 801 Msamples/s; multi-material 314 vs 325: pixel-order queues there
-# are coherent enough that the ordering passes cost more than they save)
+# The launch shape of a render (threads, shared stack, wave or pool size, ordered queues, streamed)
+# is picked by the batch autotuner on the view itself, outside the timed region, unless --launch
+# or --ordered fixes it.
 
 
 def render_scene(name: str, width: int, height: int):
@@ -594,13 +593,22 @@ def run_render(args) -> None:
     bvh = BVHCompact.build(sc, 1e-5, 1, 8)
     build_s = time.perf_counter() - t0
     r = Renderer(DeviceBVH(bvh), sc)
-    r.set_launch(128, 16, 1 << 22, cfg["ordered"] if args.ordered < 0 else args.ordered)
+    params = lambda k: render_params(spp=cfg["spp"], sample_offset=k * cfg["spp"], max_depth=cfg["depth"], rr_depth=4,
+                                     seed=1)
+    tune_s, trials = 0.0, 0
+    if args.launch:  # a given shape
+        r.set_launch(*[int(x) for x in args.launch.split(",")])
+    elif args.ordered >= 0:  # the fixed default shape, ordering as asked
+        r.set_launch(128, 16, 1 << 22, args.ordered)
+    else:  # the launch-shape autotuner on the view itself (a batch of one)
+        from trenchanttracer_gb300 import Batch
+        t0 = time.perf_counter()
+        trials = len(Batch(r, [(cam, cfg["spp"], 0, 1)], render_params(max_depth=cfg["depth"], rr_depth=4)).autotune())
+        tune_s = time.perf_counter() - t0
     npx = cfg["width"] * cfg["height"] * 3
     acc = torch.zeros(npx, dtype=torch.float32, device=dev)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=dev)
     stream = torch.cuda.current_stream(dev)
-    params = lambda k: render_params(spp=cfg["spp"], sample_offset=k * cfg["spp"], max_depth=cfg["depth"], rr_depth=4,
-                                     seed=1)
     for k in range(args.warmup):
         r.render_native(cam, params(k), acc, stream=stream.cuda_stream)
     torch.cuda.synchronize(dev)
@@ -643,7 +651,8 @@ def run_render(args) -> None:
         "ms_per_step": round(mean_ms, 3), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded procedural scene)",
         "config": {"workload": cfg["desc"], "tris": int(mesh.num_tris), "bvh_build_s": round(build_s, 2),
-                   "launch_shape": list(r.launch), "l2": "L2 flushed (256 MB write) between steps, untimed"},
+                   "launch_shape": list(r.launch), "autotune_s": round(tune_s, 2), "autotune_trials": trials,
+                   "l2": "L2 flushed (256 MB write) between steps, untimed"},
         "mrays_per_s": round(rays / mean_ms / 1e3, 1),
         "rays_per_step": {"extension": st["extension_rays"] // args.steps, "shadow": st["shadow_rays"] // args.steps},
         "e2e": {"value": round(paths / float(np.mean(e2e)) / 1e3, 2), "unit": "Msamples/s",
@@ -1018,11 +1027,12 @@ def main() -> None:
     ap.add_argument("--mma-kind", type=int, choices=[0, 1], default=0,
                     help="mlp: the cache's tensor-core kernels, 0 tcgen05 + TMEM, 1 mma.sync (comparison)")
     ap.add_argument("--launch", default="",
-                    help="batch: block,stack_shared,wave_paths,ordered,streamed instead of autotuning (profiling)")
+                    help="batch / cornell / multimaterial: block,stack_shared,wave_paths,ordered,streamed instead "
+                         "of autotuning (profiling)")
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--ordered", type=int, choices=[-1, 0, 1], default=-1,
-                    help="cornell / multimaterial: order each extension queue before tracing it "
-                         "(-1: the workload's measured setting)")
+                    help="cornell / multimaterial: the default launch shape with ordered queues (1) or not (0) "
+                         "instead of autotuning (-1)")
     ap.add_argument("--trace-width", type=int, default=WIDTH,
                     help="terrain workload: camera width; each ray set has width^2 rays (profiling a "
                          "smaller case of the same kernels)")
