@@ -8,9 +8,12 @@
 // atomic per warp) -> shadow (any hit), and finally accumulate (each pixel adds its samples in
 // sample order, in float or double, so the sum does not depend on how the waves fall). Every
 // kernel is a persistent grid that reads its queue length from device memory, so a wave needs no
-// host round trip and a whole batch is captured once as a CUDA graph (tt_batch_render). The
-// launch shape (threads per block, shared-memory traversal stack depth, paths per wave) is a
-// renderer setting that tt_batch_autotune picks by timing.
+// host round trip and a whole batch is captured once as a CUDA graph (tt_batch_render). A render
+// of more paths than one wave can instead stream them through a pool of wave_paths slots that is
+// refilled with new camera paths as paths end (issue_stream, StreamPlan in tt_native.cuh), with
+// the same image bits. The launch shape (threads per block, shared-memory traversal stack depth,
+// paths per wave, ordered queues, streamed) is a renderer setting that tt_batch_autotune picks by
+// timing.
 //
 // The integrator (all of it built from basic IEEE operations, tt_ptmath.cuh):
 //   camera     pinhole of the CameraMeta; pixel (x, y) with y = 0 at the top, jittered by two
@@ -27,8 +30,9 @@
 //   reference  Metal (Phong 30 lobe), Spec (mirror), Refr (dielectric, IOR 1.4), Coat (Fresnel
 //   kinds      choice between mirror and Lambert): sampled, treated as specular for MIS
 //   env        nearest texel of the equirectangular map in the reference's mapping; light
-//              sampling by a 2D CDF over luminance * sin(theta) (FP64 prefix sums); power
-//              heuristic MIS between light and BSDF sampling for Lambert and GGX vertices
+//              sampling by a 2D CDF over luminance * sin(theta) (FP64 prefix sums, searched
+//              between the entries of guide tables); power heuristic MIS between light and BSDF
+//              sampling for Lambert and GGX vertices
 //   roulette   from rr_depth on, survival max(beta) clamped to [0.05, 1]
 #include <cuda_runtime.h>
 
