@@ -1,6 +1,8 @@
-// The radiance cache's inference on 5th-generation tensor cores: tcgen05.mma with the FP32
+// The radiance cache's network on 5th-generation tensor cores: tcgen05.mma with the FP32
 // accumulator in tensor memory (TMEM), operands in shared memory, weights and feature records
-// brought in by bulk asynchronous copies (cp.async.bulk) that signal an mbarrier.
+// brought in by bulk asynchronous copies (cp.async.bulk) that signal an mbarrier. Inference is
+// described here; training (the same forward kernel storing each layer's input, a backward kernel
+// and a weight-gradient kernel) further down.
 //
 // One CTA per SM, six warpgroups of 128 threads (kTcGroups) sharing one copy of the network's
 // weights (55.3 KB, loaded once per CTA). Each warpgroup owns its own stream of tiles of 128 rows
