@@ -1,5 +1,7 @@
-// Learned radiance cache: the MLP's encoding, forward, backward, weight-gradient and Adam
-// kernels on BF16 tensor cores (mma.sync m16n8k16, FP32 accumulation), and its C ABI.
+// Learned radiance cache: the cache object and its C ABI, the Adam kernel, and the mma.sync kind
+// of the MLP's encoding, forward, backward and weight-gradient kernels (BF16 m16n8k16, FP32
+// accumulation; mma_kind = 1). The default kind runs the network on tcgen05 + TMEM
+// (tt_nrc_tc.cu); both write the same scratch layouts and partial gradients, which Adam sums.
 //
 // Fused forward / backward: each warp owns tiles of 16 rows. The encoding of a tile is built in
 // shared memory; every later activation stays in registers, because the FP32 accumulator
