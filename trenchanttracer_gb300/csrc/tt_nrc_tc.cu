@@ -656,14 +656,16 @@ __global__ void __launch_bounds__(128 * kG, 1) k_mlp_backward_tc(TcBackArgs a) {
 }
 
 // ---- training: weight gradients ------------------------------------------------------------------
-// dW_l = dZ_l^T H_l over the batch's rows: one CTA per chunk of kWgRows rows and layer, a product
-// with M = 128 (the layer's outputs, zero beyond them), N = the layer's inputs (160 or 64) and K =
-// the chunk's rows, 128 at a time. The CTA stages each 128-row tile from the row-major H and dZ the
-// forward and backward passes wrote: one 16-byte row of a core matrix per item (eight consecutive
-// rows of one column; consecutive threads take consecutive columns, so each row's reads coalesce),
-// dZ^T as the A operand and H^T as the B operand, both K-major. The sums stay in TMEM across the
-// chunk, and each CTA writes its partial gradient, which Adam sums over the chunks in chunk order
-// (deterministic).
+// dW_l = dZ_l^T H_l over the batch's rows: one CTA per chunk of rows and layer, a product with
+// M = 128 (the layer's outputs, zero beyond them), N = the layer's inputs (160 or 64) and K = the
+// chunk's rows, 128 at a time. Both operands are MN-major (the transpose bits of the instruction
+// descriptor): a core matrix is 8 consecutive rows of the batch x 16 bytes of consecutive columns,
+// which is a 16-byte piece of each of 8 rows of the row-major H and dZ that the forward and
+// backward passes wrote, so staging is 16-byte asynchronous copies (cp.async) with no
+// transposition. Core (c8, k8) of an operand of R columns sits at c8 * 128 + k8 * (R / 8) * 128
+// bytes: the descriptor's LBO is the stride between K-adjacent core matrices and SBO between
+// column-adjacent ones, as in the K-major layout. The sums stay in TMEM across the chunk, and each
+// CTA writes its partial gradient, which Adam sums over the chunks in chunk order (deterministic).
 constexpr int kWgMinRows = 256;  // rows per chunk: at least this, more for large batches (tc_wgrad_rows)
 constexpr int kWgABytes = kTcRows * kTcRows * 2;  // 128 outputs x 128 rows
 constexpr int kWgBBytes = kIn * kTcRows * 2;      // up to 160 inputs x 128 rows
@@ -707,7 +709,7 @@ __global__ void __launch_bounds__(kWgThreads, 1) k_mlp_wgrad_tc(TcWgradArgs a) {
         *ok = 1;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    for (int i = tid; i < kWgABytes / 16; i += kWgThreads)  // A rows beyond the outputs stay zero
+    for (int i = tid; i < kWgABytes / 16; i += kWgThreads)  // A columns beyond the outputs stay zero
         reinterpret_cast<uint4 *>(As)[i] = make_uint4(0u, 0u, 0u, 0u);
     __syncthreads();
     if (tid < 32) tmem_alloc(tmem_slot, kWgTmemCols);
@@ -718,29 +720,30 @@ __global__ void __launch_bounds__(kWgThreads, 1) k_mlp_wgrad_tc(TcWgradArgs a) {
     int issued = 0, done = 0;
     for (long long k0 = c0; k0 < c1; k0 += kTcRows) {
         const int nk = (int)(c1 - k0 < kTcRows ? c1 - k0 : kTcRows);  // rows past the chunk are zero
-#pragma unroll 2
-        for (int it = tid; it < (out + in) * (kTcRows / 8); it += kWgThreads) {
-            const bool is_a = it < out * (kTcRows / 8);
-            const int w = is_a ? out : in, j = is_a ? it : it - out * (kTcRows / 8);
-            const int col = j % w, k8 = j / w;
-            const uint16_t *src = (is_a ? a.dz[l] : a.h[l]) + (k0 + 8 * k8) * w + col;
-            uint32_t pk[4];
-#pragma unroll
-            for (int q = 0; q < 4; q++) {
-                const uint32_t lo = 8 * k8 + 2 * q < nk ? src[(2 * q) * w] : 0u;
-                const uint32_t hi = 8 * k8 + 2 * q + 1 < nk ? src[(2 * q + 1) * w] : 0u;
-                pk[q] = lo | (hi << 16);
+        // one 16-byte piece per item: row r of the tile, columns 8 p .. 8 p + 7 (consecutive items
+        // are consecutive pieces of a row, so each row is read whole by neighbouring threads)
+        const int pa = out / 8, pb = in / 8;
+        for (int it = tid; it < kTcRows * (pa + pb); it += kWgThreads) {
+            const bool is_a = it < kTcRows * pa;
+            const int np = is_a ? pa : pb, j = is_a ? it : it - kTcRows * pa;
+            const int r = j / np, p = j % np;
+            const int R = is_a ? kTcRows : in;  // columns of the operand in shared memory
+            uint8_t *dst = reinterpret_cast<uint8_t *>(is_a ? As : Bs) + p * 128 + (r >> 3) * (R / 8) * 128 + (r & 7) * 16;
+            if (r < nk) {
+                const uint16_t *src = (is_a ? a.dz[l] + (k0 + r) * out : a.h[l] + (k0 + r) * in) + 8 * p;
+                asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(saddr(dst)), "l"(src) : "memory");
+            } else {
+                *reinterpret_cast<uint4 *>(dst) = make_uint4(0u, 0u, 0u, 0u);
             }
-            uint16_t *dst = is_a ? As + kmajor_offset(col, 8 * k8, kTcRows) : Bs + kmajor_offset(col, 8 * k8, in);
-            *reinterpret_cast<uint4 *>(dst) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
         }
+        asm volatile("cp.async.wait_all;" ::: "memory");
         fence_async_smem();
         tc_fence_before();
         __syncthreads();
         tc_fence_after();
         if (tid == 0) {
             const uint32_t a0 = saddr(As), b0 = saddr(Bs);
-            const uint32_t idesc = idesc_bf16(kTcRows, in);
+            const uint32_t idesc = idesc_bf16(kTcRows, in) | (1u << 15) | (1u << 16);  // A and B MN-major
             for (int s2 = 0; s2 < kTcRows / 16; s2++)
                 umma(tmem, sdesc(a0 + s2 * 2 * (kTcRows / 8) * 128, (kTcRows / 8) * 128, 128),
                      sdesc(b0 + s2 * 2 * (in / 8) * 128, (in / 8) * 128, 128), idesc, (k0 > c0 || s2 > 0) ? 1u : 0u);
@@ -807,7 +810,9 @@ void tcT_relayout(const float *w_f32, uint16_t *w_tcT, cudaStream_t s) {
     k_tcT_layout<<<(kTcTWeights + 255) / 256, 256, 0, s>>>(w_f32, w_tcT);
 }
 
-// rows per weight-gradient chunk: about two chunks per SM for each layer, 256 .. 4096 rows
+// rows per weight-gradient chunk: about two chunks per SM for each layer, 256 .. 4096 rows (each
+// chunk's tiles run one after another, so more, shorter chunks finish sooner: 512-row chunks, one
+// round of CTAs at 16K rows, took 28 us against 22)
 static int tc_wgrad_rows(long long rows, int num_sms) {
     int c = kWgMinRows;
     while (c < 4096 && (long long)c * 2 * num_sms < rows) c *= 2;
