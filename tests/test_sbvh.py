@@ -184,10 +184,12 @@ def _soup_scene(tmp_path, name, mesh):
 
 
 @pytest.mark.skipif(not refhost.available(), reason="the reference's builder is not built on this host")
-@pytest.mark.parametrize("kind", ["soup", "flat", "dups"])
+@pytest.mark.parametrize("kind", ["soup", "flat", "dups", "copies"])
 def test_live_against_reference_builder(kind, tmp_path):
-    """Adversarial scenes: random triangle soup (spatial splits), a flat layer (zero-extent bins)
-    and duplicated triangles (ties in the sort key broken by triangle index)."""
+    """Adversarial scenes: random triangle soup (spatial splits), a flat layer (zero-extent bins),
+    duplicated triangles (ties in the sort key broken by triangle index) and 120 copies of one
+    triangle, which with one triangle per leaf splits one off per level down to the depth limit.
+    A leaf size floor above one makes leaves of the references in the order a node received them."""
     rng = np.random.default_rng(len(kind))
     if kind == "soup":
         v = rng.uniform(-1, 1, (900, 3)).astype(np.float32)
@@ -196,14 +198,17 @@ def test_live_against_reference_builder(kind, tmp_path):
         v = rng.uniform(-1, 1, (600, 3)).astype(np.float32)
         v[:, 1] = 0.25
         t = np.arange(600, dtype=np.int32).reshape(-1, 3)
-    else:
+    elif kind == "dups":
         base = rng.uniform(-1, 1, (150, 3)).astype(np.float32)
         v = np.concatenate([base, base, base])
         t = np.arange(450, dtype=np.int32).reshape(-1, 3)
+    else:
+        v = np.tile(rng.uniform(-1, 1, (3, 3)).astype(np.float32), (120, 1))
+        t = np.arange(360, dtype=np.int32).reshape(-1, 3)
     mesh = scenes.Mesh(v, scenes._normalize(v + 3.0), t, t.copy(), np.zeros(len(t), np.uint32),
                        [{"name": "m", "type": "Diff", "diffuseColor": [0.5, 0.5, 0.5]}])
     cfg = _soup_scene(tmp_path, kind, mesh)
-    for leaf_max in golden_scenes.LEAF_MAX:
-        refhost.build_json(str(cfg), str(tmp_path / "ref.cache"), 1e-5, 1, leaf_max)
-        BVHCompact.build(Scene.load_json(cfg), 1e-5, 1, leaf_max).save(tmp_path / "new.cache")
-        assert sha(tmp_path / "ref.cache") == sha(tmp_path / "new.cache")
+    for leaf_min, leaf_max in [(1, m) for m in golden_scenes.LEAF_MAX] + [(4, 1), (4, 8), (9, 16)]:
+        refhost.build_json(str(cfg), str(tmp_path / "ref.cache"), 1e-5, leaf_min, leaf_max)
+        BVHCompact.build(Scene.load_json(cfg), 1e-5, leaf_min, leaf_max).save(tmp_path / "new.cache")
+        assert sha(tmp_path / "ref.cache") == sha(tmp_path / "new.cache"), (leaf_min, leaf_max)

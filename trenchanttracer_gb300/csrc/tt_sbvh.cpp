@@ -28,6 +28,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <unordered_map>
 #include <omp.h>
 
 #include "tt_internal.h"
@@ -105,6 +106,31 @@ inline int f2i_trunc(float f) {
     return (int)f;
 }
 
+// The node's references sorted along each axis (centroid, then triangle index: a strict total
+// order). The reference re-sorts every node along all three axes (BVH.cpp:132-164); here each
+// node receives its three orders from its parent, which partitions them stably (a stable filter of
+// a sorted list is sorted) and merges in the few references a spatial split clipped, so a node
+// costs O(n) instead of O(n log n) and every set, order and split is the reference's.
+struct NodeRefs {
+    std::vector<Ref> s[3];
+    size_t size() const { return s[0].size(); }
+};
+
+// Centroid order along dim, ties by triangle index.
+struct ByCentroid {
+    int dim;
+    bool operator()(const Ref &a, const Ref &b) const {
+        const float ca = a.b.lo[dim] + a.b.hi[dim];
+        const float cb = b.b.lo[dim] + b.b.hi[dim];
+        if (ca < cb) return true;
+        if (ca > cb) return false;
+        return a.tri < b.tri;
+    }
+};
+
+// What the spatial partition did with one reference that straddles the plane.
+enum class Straddle : uint8_t { kLeft, kRight, kBoth };
+
 class Builder {
 public:
     Builder(const Scene &s, const BuildParams &p) : sc_(s), p_(p) {}
@@ -124,7 +150,16 @@ public:
         int threads = p_.threads > 0 ? p_.threads : omp_get_max_threads();
 #pragma omp parallel num_threads(threads)
 #pragma omp single
-        out = build(std::move(refs), root, 0);
+        {
+            NodeRefs nr;
+            for (int d = 0; d < 3; d++) {
+                nr.s[d] = refs;
+#pragma omp task firstprivate(d) shared(nr)
+                std::sort(nr.s[d].begin(), nr.s[d].end(), ByCentroid{d});
+            }
+#pragma omp taskwait
+            out = build(std::move(nr), root, 0, &refs);
+        }
         duplicates = dup_;
         return out;
     }
@@ -137,6 +172,7 @@ private:
 
     const V3 &vert(int tri, int k) const { return sc_.vertices[sc_.vidx[3 * tri + k]]; }
 
+    // refs in the order the reference holds them at that point (it emits them reversed)
     std::unique_ptr<Node> leaf(const std::vector<Ref> &refs, const AABB &b) {
         auto nd = std::make_unique<Node>();
         nd->leaf = true;
@@ -146,22 +182,13 @@ private:
         return nd;
     }
 
-    static void sort_dim(std::vector<Ref> &refs, int dim) {
-        std::sort(refs.begin(), refs.end(), [dim](const Ref &a, const Ref &b) {
-            float ca = a.b.lo[dim] + a.b.hi[dim];
-            float cb = b.b.lo[dim] + b.b.hi[dim];
-            if (ca < cb) return true;
-            if (ca > cb) return false;
-            return a.tri < b.tri;
-        });
-    }
-
-    ObjectSplit find_object_split(std::vector<Ref> &refs, float node_sah) {
+    // the reference's sweep over each axis's sorted order (BVH.cpp:132-155)
+    ObjectSplit find_object_split(const NodeRefs &nr, float node_sah) {
         ObjectSplit split;
-        const int n = (int)refs.size();
+        const int n = (int)nr.size();
         std::vector<AABB> right_bounds(n > 1 ? n - 1 : 1);
         for (int dim = 0; dim < 3; dim++) {
-            sort_dim(refs, dim);
+            const std::vector<Ref> &refs = nr.s[dim];
             AABB rb;
             for (int i = n - 1; i > 0; i--) {
                 rb.grow(refs[i].b);
@@ -260,10 +287,12 @@ private:
         return split;
     }
 
-    // Partitions `refs` in place (plus appended duplicates): left = [0, left_end),
-    // right = [left_end, size).
+    // The reference's partition (BVH.cpp:266-330) of `refs` (the node's references in the order it
+    // holds them: along axis 2) in place, plus appended duplicates: left = [0, left_n), right =
+    // [left_n, size). `decisions` receives what became of each straddling reference.
     void perform_spatial_split(std::vector<Ref> &refs, const SpatialSplit &split, int &left_n, AABB &left_b,
-                               int &right_n, AABB &right_b) {
+                               int &right_n, AABB &right_b,
+                               std::vector<std::pair<int32_t, Straddle>> &decisions) {
         const int dim = split.dim;
         const float pos = split.pos;
         int left_start = 0, left_end = 0, right_start = (int)refs.size();
@@ -278,6 +307,8 @@ private:
                 i--;
             }
         }
+        decisions.clear();
+        decisions.reserve(right_start - left_end);
         while (left_end < right_start) {
             Ref lr, rr;
             split_reference(lr, rr, refs[left_end], dim, pos);
@@ -295,12 +326,15 @@ private:
             float duplicate = ldb.area() * lbc + rdb.area() * rbc;
             float m = min1f(min1f(unsplit_left, unsplit_right), duplicate);
             if (m == unsplit_left) {
+                decisions.emplace_back(refs[left_end].tri, Straddle::kLeft);
                 left_b = lub;
                 left_end++;
             } else if (m == unsplit_right) {
+                decisions.emplace_back(refs[left_end].tri, Straddle::kRight);
                 right_b = rub;
                 std::swap(refs[left_end], refs[--right_start]);
             } else {
+                decisions.emplace_back(refs[left_end].tri, Straddle::kBoth);
                 left_b = ldb;
                 right_b = rdb;
                 refs[left_end++] = lr;
@@ -311,37 +345,111 @@ private:
         right_n = (int)refs.size() - right_start;
     }
 
-    std::unique_ptr<Node> build(std::vector<Ref> refs, AABB bounds, int level) {
-        const int n = (int)refs.size();
-        if (n <= p_.leaf_min || level >= kMaxDepth) return leaf(refs, bounds);
+    // Children's sorted orders after an object split: the left set is the first num_left
+    // references along its axis, so membership along the other axes is a comparison with the
+    // first right reference.
+    static void split_object_orders(NodeRefs &nr, const ObjectSplit &os, NodeRefs &L, NodeRefs &R) {
+        const int d = os.dim;
+        const size_t nl = (size_t)os.num_left;
+        const size_t n = nr.size();
+        const Ref pivot = nr.s[d][nl];
+        const ByCentroid cmp{d};
+        for (int e = 0; e < 3; e++) {
+            L.s[e].reserve(nl);
+            R.s[e].reserve(n - nl);
+            if (e == d) {
+                L.s[e].assign(nr.s[e].begin(), nr.s[e].begin() + nl);
+                R.s[e].assign(nr.s[e].begin() + nl, nr.s[e].end());
+            } else {
+                for (const Ref &r : nr.s[e]) (cmp(r, pivot) ? L : R).s[e].push_back(r);
+            }
+            std::vector<Ref>().swap(nr.s[e]);
+        }
+    }
+
+    // Children's sorted orders after a spatial split: each axis's order filtered by where its
+    // unclipped references went, with the clipped halves (sorted on their own) merged in.
+    void split_spatial_orders(NodeRefs &nr, const SpatialSplit &sp, const std::vector<Ref> &parted, int left_n,
+                              const std::vector<std::pair<int32_t, Straddle>> &decisions, NodeRefs &L, NodeRefs &R) {
+        const int dim = sp.dim;
+        const float pos = sp.pos;
+        std::unordered_map<int32_t, Straddle> fate(decisions.begin(), decisions.end());
+        // the clipped halves: every reference of `parted` whose triangle was split on both sides
+        std::vector<Ref> clipped_l, clipped_r;
+        for (size_t i = 0; i < parted.size(); i++) {
+            auto it = fate.find(parted[i].tri);
+            if (it != fate.end() && it->second == Straddle::kBoth) ((int)i < left_n ? clipped_l : clipped_r).push_back(parted[i]);
+        }
+        for (int e = 0; e < 3; e++) {
+            std::vector<Ref> l, r;
+            l.reserve(left_n);
+            r.reserve(parted.size() - left_n);
+            for (const Ref &ref : nr.s[e]) {
+                if (ref.b.hi[dim] <= pos) {
+                    l.push_back(ref);
+                } else if (ref.b.lo[dim] >= pos) {
+                    r.push_back(ref);
+                } else {
+                    const Straddle f = fate.at(ref.tri);
+                    if (f == Straddle::kLeft) l.push_back(ref);
+                    else if (f == Straddle::kRight) r.push_back(ref);
+                }
+            }
+            std::vector<Ref>().swap(nr.s[e]);
+            const ByCentroid cmp{e};
+            std::vector<Ref> cl = clipped_l, cr = clipped_r;
+            std::sort(cl.begin(), cl.end(), cmp);
+            std::sort(cr.begin(), cr.end(), cmp);
+            L.s[e].resize(l.size() + cl.size());
+            std::merge(l.begin(), l.end(), cl.begin(), cl.end(), L.s[e].begin(), cmp);
+            R.s[e].resize(r.size() + cr.size());
+            std::merge(r.begin(), r.end(), cr.begin(), cr.end(), R.s[e].begin(), cmp);
+        }
+    }
+
+    // `arrival` (may be null when the node is not small): the references in the order the
+    // reference would hold them on entering this node, which only a leaf made on entry uses.
+    std::unique_ptr<Node> build(NodeRefs nr, AABB bounds, int level, const std::vector<Ref> *arrival) {
+        const int n = (int)nr.size();
+        if (n <= p_.leaf_min || level >= kMaxDepth) return leaf(*arrival, bounds);
 
         const float area = bounds.area();
         const float leaf_sah = area * (float)n;
         const float node_sah = area * 2.0f;
-        ObjectSplit object = find_object_split(refs, node_sah);
+        ObjectSplit object = find_object_split(nr, node_sah);
 
         SpatialSplit spatial;
         if (level < kMaxSpatialDepth) {
             AABB overlap = object.left;
             overlap.intersect(object.right);
-            if (overlap.area() >= min_overlap_) spatial = find_spatial_split(refs, bounds, node_sah);
+            if (overlap.area() >= min_overlap_) spatial = find_spatial_split(nr.s[0], bounds, node_sah);
         }
 
         const float min_sah = min1f(min1f(leaf_sah, object.sah), spatial.sah);
-        if (min_sah == leaf_sah && n <= p_.leaf_max) return leaf(refs, bounds);
+        // after its sorts the reference holds the references along axis 2
+        if (min_sah == leaf_sah && n <= p_.leaf_max) return leaf(nr.s[2], bounds);
 
         int left_n = 0, right_n = 0;
         AABB left_b, right_b;
-        if (min_sah == spatial.sah) perform_spatial_split(refs, spatial, left_n, left_b, right_n, right_b);
-        if (!left_n || !right_n) {
-            // The references are sorted along axis 2 by find_object_split; sort along the
-            // chosen axis again exactly as the reference does (BVH.cpp:156-164).
-            if (refs.size() != (size_t)n) refs.resize(n);  // (never: no duplicates were appended)
-            sort_dim(refs, object.dim);
+        NodeRefs L, R;
+        std::vector<Ref> parted;  // the spatial partition's order (left part, then right part)
+        bool spatial_done = false;
+        if (min_sah == spatial.sah) {
+            parted = nr.s[2];
+            std::vector<std::pair<int32_t, Straddle>> decisions;
+            perform_spatial_split(parted, spatial, left_n, left_b, right_n, right_b, decisions);
+            if (left_n && right_n) {
+                split_spatial_orders(nr, spatial, parted, left_n, decisions, L, R);
+                spatial_done = true;
+            }
+        }
+        if (!spatial_done) {
+            // sorted along the chosen axis again, exactly as the reference does (BVH.cpp:156-164)
             left_n = object.num_left;
             left_b = object.left;
             right_n = n - object.num_left;
             right_b = object.right;
+            split_object_orders(nr, object, L, R);
         }
 
         const int total = left_n + right_n;
@@ -349,22 +457,32 @@ private:
 #pragma omp atomic
             dup_ += total - n;
         }
-        std::vector<Ref> right_refs(refs.begin() + left_n, refs.begin() + total);
-        refs.resize(left_n);
-        std::vector<Ref> left_refs = std::move(refs);
+        // the order each child arrives in (needed only by a child that becomes a leaf on entry)
+        const bool small_l = left_n <= p_.leaf_min || level + 1 >= kMaxDepth;
+        const bool small_r = right_n <= p_.leaf_min || level + 1 >= kMaxDepth;
+        std::vector<Ref> arrive_l, arrive_r;
+        if (small_l) {
+            if (spatial_done) arrive_l.assign(parted.begin(), parted.begin() + left_n);
+            else arrive_l = L.s[object.dim];
+        }
+        if (small_r) {
+            if (spatial_done) arrive_r.assign(parted.begin() + left_n, parted.end());
+            else arrive_r = R.s[object.dim];
+        }
+        std::vector<Ref>().swap(parted);
 
         auto nd = std::make_unique<Node>();
         nd->b = bounds;
         if (total >= kTaskThreshold) {
             std::unique_ptr<Node> r;
-#pragma omp task shared(r) firstprivate(right_b, level)
-            r = build(std::move(right_refs), right_b, level + 1);
-            nd->child[0] = build(std::move(left_refs), left_b, level + 1);
+#pragma omp task shared(r, R, arrive_r) firstprivate(right_b, level, small_r)
+            r = build(std::move(R), right_b, level + 1, small_r ? &arrive_r : nullptr);
+            nd->child[0] = build(std::move(L), left_b, level + 1, small_l ? &arrive_l : nullptr);
 #pragma omp taskwait
             nd->child[1] = std::move(r);
         } else {
-            nd->child[1] = build(std::move(right_refs), right_b, level + 1);
-            nd->child[0] = build(std::move(left_refs), left_b, level + 1);
+            nd->child[1] = build(std::move(R), right_b, level + 1, small_r ? &arrive_r : nullptr);
+            nd->child[0] = build(std::move(L), left_b, level + 1, small_l ? &arrive_l : nullptr);
         }
         return nd;
     }
