@@ -19,10 +19,13 @@
 //   - compact emission: DFS from an explicit stack, inner children addressed by float4 index,
 //     leaves by ~vertexIndex, -0.0 in vertex0.x rewritten to +0.0, a (0x80000000,0,0,0)
 //     terminator after each leaf (BVHCompact.cpp:88-192).
-// Sorting uses std::sort: within one node every triangle index appears at most once, so the
-// comparator is a strict total order and any correct sort yields the same permutation.
-// Subtrees are built as OpenMP tasks; each task owns the reference list of its node, in the
-// order the reference's shared stack would hold it, so the output does not depend on threads.
+// Within one node every triangle index appears at most once, so the centroid comparator is a
+// strict total order and a node's order along each axis is unique. The root is sorted once per
+// axis; every other node receives its three orders from its parent by stable partition (plus a
+// merge of the clipped halves of a spatial split), which yields that unique order without a sort.
+// Subtrees are built as OpenMP tasks; each task owns the reference lists of its node, and a leaf
+// lists its triangles in the order the reference's shared stack would hold them, so the output
+// does not depend on threads.
 #include <algorithm>
 #include <cfloat>
 #include <cstdio>
