@@ -31,6 +31,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <thread>
 #include <unordered_map>
 #include <omp.h>
 
@@ -43,6 +44,7 @@ constexpr int kMaxDepth = 64;
 constexpr int kMaxSpatialDepth = 48;
 constexpr int kBins = 32;
 constexpr int kTaskThreshold = 2048;
+constexpr int kAxisThreadsMin = 1 << 16;
 
 struct AABB {
     V3 lo{FLT_MAX, FLT_MAX, FLT_MAX};
@@ -74,11 +76,19 @@ struct Ref {
     AABB b;
 };
 
+// What the compact emission of an inner node's subtree writes, its own four node entries not
+// counted: the node entries of the inner nodes below it, and the vertex (= normal = index)
+// entries of the leaves below it, three per triangle plus a terminator per leaf.
+struct EmitSize {
+    int64_t nodes = 0, verts = 0, tris = 0, leaves = 0;
+};
+
 struct Node {
     AABB b;
     std::unique_ptr<Node> child[2];  // [0] = left, [1] = right
     std::vector<int32_t> tris;       // leaf triangles, in emission order
     bool leaf = false;
+    EmitSize below;                  // inner nodes only, filled before emission
 };
 
 struct ObjectSplit {
@@ -148,9 +158,10 @@ public:
             root.grow(refs[i].b);
         }
         min_overlap_ = root.area() * p_.split_alpha;
+        int threads = p_.threads > 0 ? p_.threads : omp_get_max_threads();
+        par_min_ = threads > 1 ? std::max(kAxisThreadsMin, n / 16) : INT32_MAX;
         std::unique_ptr<Node> out;
         dup_ = 0;
-        int threads = p_.threads > 0 ? p_.threads : omp_get_max_threads();
 #pragma omp parallel num_threads(threads)
 #pragma omp single
         {
@@ -172,6 +183,23 @@ private:
     BuildParams p_;
     float min_overlap_ = 0.0f;
     int64_t dup_ = 0;
+    int par_min_ = INT32_MAX;  // nodes of at least this many references split their axes over threads
+
+    // Runs f(0), f(1), f(2); with `par`, axes 1 and 2 on threads of their own. These are plain
+    // threads, not OpenMP tasks: a thread that waits for tasks may run any queued subtree task
+    // first, which held a node near the root up for seconds.
+    template <class F>
+    static void for_axes(bool par, F &&f) {
+        if (!par) {
+            for (int d = 0; d < 3; d++) f(d);
+            return;
+        }
+        std::thread t1([&] { f(1); });
+        std::thread t2([&] { f(2); });
+        f(0);
+        t1.join();
+        t2.join();
+    }
 
     const V3 &vert(int tri, int k) const { return sc_.vertices[sc_.vidx[3 * tri + k]]; }
 
@@ -185,31 +213,39 @@ private:
         return nd;
     }
 
-    // the reference's sweep over each axis's sorted order (BVH.cpp:132-155)
-    ObjectSplit find_object_split(const NodeRefs &nr, float node_sah) {
+    // The reference's sweep over one axis's sorted order (BVH.cpp:132-155): the first best split.
+    static ObjectSplit object_sweep(const std::vector<Ref> &refs, int dim, float node_sah) {
         ObjectSplit split;
-        const int n = (int)nr.size();
+        const int n = (int)refs.size();
         std::vector<AABB> right_bounds(n > 1 ? n - 1 : 1);
-        for (int dim = 0; dim < 3; dim++) {
-            const std::vector<Ref> &refs = nr.s[dim];
-            AABB rb;
-            for (int i = n - 1; i > 0; i--) {
-                rb.grow(refs[i].b);
-                right_bounds[i - 1] = rb;
-            }
-            AABB lb;
-            for (int i = 1; i < n; i++) {
-                lb.grow(refs[i - 1].b);
-                float sah = node_sah + lb.area() * (float)i + right_bounds[i - 1].area() * (float)(n - i);
-                if (sah < split.sah) {
-                    split.sah = sah;
-                    split.dim = dim;
-                    split.num_left = i;
-                    split.left = lb;
-                    split.right = right_bounds[i - 1];
-                }
+        AABB rb;
+        for (int i = n - 1; i > 0; i--) {
+            rb.grow(refs[i].b);
+            right_bounds[i - 1] = rb;
+        }
+        AABB lb;
+        for (int i = 1; i < n; i++) {
+            lb.grow(refs[i - 1].b);
+            float sah = node_sah + lb.area() * (float)i + right_bounds[i - 1].area() * (float)(n - i);
+            if (sah < split.sah) {
+                split.sah = sah;
+                split.dim = dim;
+                split.num_left = i;
+                split.left = lb;
+                split.right = right_bounds[i - 1];
             }
         }
+        return split;
+    }
+
+    // The reference sweeps axes 0, 1, 2 in turn, replacing its best only on a strictly lower cost:
+    // the first best of each axis, taken in axis order on the same strict comparison, is that split.
+    ObjectSplit find_object_split(const NodeRefs &nr, float node_sah, bool par) {
+        ObjectSplit per_axis[3];
+        for_axes(par, [&](int d) { per_axis[d] = object_sweep(nr.s[d], d, node_sah); });
+        ObjectSplit split;
+        for (int d = 0; d < 3; d++)
+            if (per_axis[d].sah < split.sah) split = per_axis[d];
         return split;
     }
 
@@ -240,30 +276,32 @@ private:
         right.b.intersect(ref.b);
     }
 
-    SpatialSplit find_spatial_split(const std::vector<Ref> &refs, const AABB &bounds, float node_sah) {
+    // One axis's bins (BVH.cpp:184-215): each reference is clipped at the planes it crosses, in
+    // order, and enters its first bin and exits its last. The axes do not share any state.
+    void bin_axis(const std::vector<Ref> &refs, int dim, float origin, float bin_size, float inv_bin,
+                  Bin *bins) const {
+        for (const Ref &ref : refs) {
+            const int first = clamp1i(f2i_trunc((ref.b.lo[dim] - origin) * inv_bin), 0, kBins - 1);
+            const int last = clamp1i(f2i_trunc((ref.b.hi[dim] - origin) * inv_bin), first, kBins - 1);
+            Ref curr = ref;
+            for (int i = first; i < last; i++) {
+                Ref lr, rr;
+                split_reference(lr, rr, curr, dim, origin + bin_size * (float)(i + 1));
+                bins[i].b.grow(lr.b);
+                curr = rr;
+            }
+            bins[last].b.grow(curr.b);
+            bins[first].enter++;
+            bins[last].exit++;
+        }
+    }
+
+    SpatialSplit find_spatial_split(const std::vector<Ref> &refs, const AABB &bounds, float node_sah, bool par) {
         const V3 origin = bounds.lo;
         const V3 bin_size = (bounds.hi - origin) * (1.0f / (float)kBins);
         const V3 inv_bin(1.0f / bin_size.x, 1.0f / bin_size.y, 1.0f / bin_size.z);
         Bin bins[3][kBins];
-        for (const Ref &ref : refs) {
-            V3 f = (ref.b.lo - origin) * inv_bin;
-            V3 l = (ref.b.hi - origin) * inv_bin;
-            int first[3], last[3];
-            for (int d = 0; d < 3; d++) first[d] = clamp1i(f2i_trunc(f[d]), 0, kBins - 1);
-            for (int d = 0; d < 3; d++) last[d] = clamp1i(f2i_trunc(l[d]), first[d], kBins - 1);
-            for (int dim = 0; dim < 3; dim++) {
-                Ref curr = ref;
-                for (int i = first[dim]; i < last[dim]; i++) {
-                    Ref lr, rr;
-                    split_reference(lr, rr, curr, dim, origin[dim] + bin_size[dim] * (float)(i + 1));
-                    bins[dim][i].b.grow(lr.b);
-                    curr = rr;
-                }
-                bins[dim][last[dim]].b.grow(curr.b);
-                bins[dim][first[dim]].enter++;
-                bins[dim][last[dim]].exit++;
-            }
-        }
+        for_axes(par, [&](int d) { bin_axis(refs, d, origin[d], bin_size[d], inv_bin[d], bins[d]); });
         SpatialSplit split;
         const int n = (int)refs.size();
         AABB right_bounds[kBins - 1];
@@ -351,13 +389,13 @@ private:
     // Children's sorted orders after an object split: the left set is the first num_left
     // references along its axis, so membership along the other axes is a comparison with the
     // first right reference.
-    static void split_object_orders(NodeRefs &nr, const ObjectSplit &os, NodeRefs &L, NodeRefs &R) {
+    static void split_object_orders(NodeRefs &nr, const ObjectSplit &os, NodeRefs &L, NodeRefs &R, bool par) {
         const int d = os.dim;
         const size_t nl = (size_t)os.num_left;
         const size_t n = nr.size();
         const Ref pivot = nr.s[d][nl];
         const ByCentroid cmp{d};
-        for (int e = 0; e < 3; e++) {
+        for_axes(par, [&](int e) {
             L.s[e].reserve(nl);
             R.s[e].reserve(n - nl);
             if (e == d) {
@@ -367,13 +405,14 @@ private:
                 for (const Ref &r : nr.s[e]) (cmp(r, pivot) ? L : R).s[e].push_back(r);
             }
             std::vector<Ref>().swap(nr.s[e]);
-        }
+        });
     }
 
     // Children's sorted orders after a spatial split: each axis's order filtered by where its
     // unclipped references went, with the clipped halves (sorted on their own) merged in.
-    void split_spatial_orders(NodeRefs &nr, const SpatialSplit &sp, const std::vector<Ref> &parted, int left_n,
-                              const std::vector<std::pair<int32_t, Straddle>> &decisions, NodeRefs &L, NodeRefs &R) {
+    static void split_spatial_orders(NodeRefs &nr, const SpatialSplit &sp, const std::vector<Ref> &parted, int left_n,
+                                     const std::vector<std::pair<int32_t, Straddle>> &decisions, NodeRefs &L,
+                                     NodeRefs &R, bool par) {
         const int dim = sp.dim;
         const float pos = sp.pos;
         std::unordered_map<int32_t, Straddle> fate(decisions.begin(), decisions.end());
@@ -383,7 +422,7 @@ private:
             auto it = fate.find(parted[i].tri);
             if (it != fate.end() && it->second == Straddle::kBoth) ((int)i < left_n ? clipped_l : clipped_r).push_back(parted[i]);
         }
-        for (int e = 0; e < 3; e++) {
+        for_axes(par, [&](int e) {
             std::vector<Ref> l, r;
             l.reserve(left_n);
             r.reserve(parted.size() - left_n);
@@ -407,7 +446,7 @@ private:
             std::merge(l.begin(), l.end(), cl.begin(), cl.end(), L.s[e].begin(), cmp);
             R.s[e].resize(r.size() + cr.size());
             std::merge(r.begin(), r.end(), cr.begin(), cr.end(), R.s[e].begin(), cmp);
-        }
+        });
     }
 
     // `arrival` (may be null when the node is not small): the references in the order the
@@ -419,13 +458,15 @@ private:
         const float area = bounds.area();
         const float leaf_sah = area * (float)n;
         const float node_sah = area * 2.0f;
-        ObjectSplit object = find_object_split(nr, node_sah);
+        // the three axes of a node near the root on three threads: few subtree tasks run yet
+        const bool par = n >= par_min_;
+        ObjectSplit object = find_object_split(nr, node_sah, par);
 
         SpatialSplit spatial;
         if (level < kMaxSpatialDepth) {
             AABB overlap = object.left;
             overlap.intersect(object.right);
-            if (overlap.area() >= min_overlap_) spatial = find_spatial_split(nr.s[0], bounds, node_sah);
+            if (overlap.area() >= min_overlap_) spatial = find_spatial_split(nr.s[0], bounds, node_sah, par);
         }
 
         const float min_sah = min1f(min1f(leaf_sah, object.sah), spatial.sah);
@@ -442,7 +483,7 @@ private:
             std::vector<std::pair<int32_t, Straddle>> decisions;
             perform_spatial_split(parted, spatial, left_n, left_b, right_n, right_b, decisions);
             if (left_n && right_n) {
-                split_spatial_orders(nr, spatial, parted, left_n, decisions, L, R);
+                split_spatial_orders(nr, spatial, parted, left_n, decisions, L, R, par);
                 spatial_done = true;
             }
         }
@@ -452,7 +493,7 @@ private:
             left_b = object.left;
             right_n = n - object.num_left;
             right_b = object.right;
-            split_object_orders(nr, object, L, R);
+            split_object_orders(nr, object, L, R, par);
         }
 
         const int total = left_n + right_n;
@@ -493,63 +534,120 @@ private:
 
 inline int32_t fbits(float f) { return (int32_t)f2u(f); }
 
-void emit_leaf(const Scene &sc, const Node &leaf, CompactBVH &out) {
+constexpr int64_t kEmitTaskVerts = 1 << 15;  // subtrees this large are emitted as tasks
+
+EmitSize size_subtree(Node &x, int depth) {
+    for (int i = 0; i < 2; i++) {
+        Node &c = *x.child[i];
+        if (c.leaf) continue;
+        if (depth < 10) {
+#pragma omp task firstprivate(i) shared(x)
+            size_subtree(*x.child[i], depth + 1);
+        } else {
+            size_subtree(c, depth + 1);
+        }
+    }
+#pragma omp taskwait
+    EmitSize e;
+    for (int i = 0; i < 2; i++) {
+        const Node &c = *x.child[i];
+        if (c.leaf) {
+            e.verts += 3 * (int64_t)c.tris.size() + 1;
+            e.tris += (int64_t)c.tris.size();
+            e.leaves += 1;
+        } else {
+            e.nodes += 4 + c.below.nodes;
+            e.verts += c.below.verts;
+            e.tris += c.below.tris;
+            e.leaves += c.below.leaves;
+        }
+    }
+    x.below = e;
+    return e;
+}
+
+// A leaf's triangles at vertex entry `at`, then the terminator (BVHCompact.cpp:127-171).
+void emit_leaf(const Scene &sc, const Node &leaf, CompactBVH &out, int64_t at) {
     for (int32_t id : leaf.tris) {
         V3 v[3], nrm[3];
         for (int k = 0; k < 3; k++) {
             v[k] = sc.vertices[sc.vidx[3 * id + k]];
             nrm[k] = sc.normals[sc.nidx[3 * id + k]];
         }
-        out.hdr.tri_count++;
         if (v[0].x == 0.0f) v[0].x = 0.0f;  // -0.0 would read as the leaf terminator
         for (int k = 0; k < 3; k++) {
-            out.vertices.push_back(I4{fbits(v[k].x), fbits(v[k].y), fbits(v[k].z), 0});
-            out.normals.push_back(I4{fbits(nrm[k].x), fbits(nrm[k].y), fbits(nrm[k].z), 0});
+            out.vertices[at + k] = I4{fbits(v[k].x), fbits(v[k].y), fbits(v[k].z), 0};
+            out.normals[at + k] = I4{fbits(nrm[k].x), fbits(nrm[k].y), fbits(nrm[k].z), 0};
+            out.tri_idx[at + k] = k == 0 ? id : 0;
+            out.mat_idx[at + k] = k == 0 ? sc.mat[id] : 0u;
         }
-        out.tri_idx.push_back(id);
-        out.tri_idx.push_back(0);
-        out.tri_idx.push_back(0);
-        out.mat_idx.push_back(sc.mat[id]);
-        out.mat_idx.push_back(0);
-        out.mat_idx.push_back(0);
+        at += 3;
     }
-    out.vertices.push_back(I4{(int32_t)0x80000000, 0, 0, 0});
-    out.normals.push_back(I4{(int32_t)0x80000000, 0, 0, 0});
-    out.tri_idx.push_back(0);
-    out.mat_idx.push_back(0);
-    out.hdr.leaf_count++;
+    out.vertices[at] = I4{(int32_t)0x80000000, 0, 0, 0};
+    out.normals[at] = I4{(int32_t)0x80000000, 0, 0, 0};
+    out.tri_idx[at] = 0;
+    out.mat_idx[at] = 0;
 }
 
-void emit_compact(const Scene &sc, const Node &root, CompactBVH &out) {
-    out.nodes.assign(4, I4{0, 0, 0, 0});
-    struct Entry {
-        const Node *node;
-        int32_t idx;
-    };
-    std::vector<Entry> stack{{&root, 0}};
-    while (!stack.empty()) {
-        Entry e = stack.back();
-        stack.pop_back();
-        const AABB *box[2];
-        int32_t cidx[2];
-        for (int i = 0; i < 2; i++) {
-            const Node *c = e.node->child[i].get();
-            box[i] = &c->b;
-            if (!c->leaf) {
-                cidx[i] = (int32_t)out.nodes.size();  // float4 index = bytes / 16
-                stack.push_back({c, (int32_t)out.nodes.size()});
-                out.nodes.resize(out.nodes.size() + 4, I4{0, 0, 0, 0});
-                continue;
-            }
-            cidx[i] = ~(int32_t)out.vertices.size();
-            emit_leaf(sc, *c, out);
+// The reference emits from an explicit stack (BVHCompact.cpp:101-125): it pops a node, gives each
+// inner child the next four node entries and writes each leaf child's triangles, then pushes the
+// inner children, so the right child's whole subtree comes before the left child's. With every
+// subtree's size known, that is a recursion whose two halves write disjoint, precomputed ranges,
+// so large subtrees are written as parallel tasks. `slot`: this node's first entry; `node_at`,
+// `vert_at`: where the entries this call writes begin.
+void emit_subtree(const Scene &sc, const Node &x, int64_t slot, int64_t node_at, int64_t vert_at,
+                  CompactBVH &out) {
+    int32_t cidx[2];
+    int64_t child_slot[2] = {0, 0};
+    for (int i = 0; i < 2; i++) {
+        const Node &c = *x.child[i];
+        if (!c.leaf) {
+            child_slot[i] = node_at;
+            cidx[i] = (int32_t)node_at;  // float4 index = bytes / 16
+            node_at += 4;
+        } else {
+            cidx[i] = ~(int32_t)vert_at;
+            emit_leaf(sc, c, out, vert_at);
+            vert_at += 3 * (int64_t)c.tris.size() + 1;
         }
-        I4 *dst = &out.nodes[e.idx];
-        dst[0] = I4{fbits(box[0]->lo.x), fbits(box[0]->hi.x), fbits(box[0]->lo.y), fbits(box[0]->hi.y)};
-        dst[1] = I4{fbits(box[1]->lo.x), fbits(box[1]->hi.x), fbits(box[1]->lo.y), fbits(box[1]->hi.y)};
-        dst[2] = I4{fbits(box[0]->lo.z), fbits(box[0]->hi.z), fbits(box[1]->lo.z), fbits(box[1]->hi.z)};
-        dst[3] = I4{cidx[0], cidx[1], 0, 0};
     }
+    const AABB *box[2] = {&x.child[0]->b, &x.child[1]->b};
+    I4 *dst = &out.nodes[slot];
+    dst[0] = I4{fbits(box[0]->lo.x), fbits(box[0]->hi.x), fbits(box[0]->lo.y), fbits(box[0]->hi.y)};
+    dst[1] = I4{fbits(box[1]->lo.x), fbits(box[1]->hi.x), fbits(box[1]->lo.y), fbits(box[1]->hi.y)};
+    dst[2] = I4{fbits(box[0]->lo.z), fbits(box[0]->hi.z), fbits(box[1]->lo.z), fbits(box[1]->hi.z)};
+    dst[3] = I4{cidx[0], cidx[1], 0, 0};
+    for (int i = 1; i >= 0; i--) {
+        const Node &c = *x.child[i];
+        if (c.leaf) continue;
+        if (c.below.verts >= kEmitTaskVerts) {
+#pragma omp task firstprivate(i, node_at, vert_at, child_slot) shared(sc, x, out)
+            emit_subtree(sc, *x.child[i], child_slot[i], node_at, vert_at, out);
+        } else {
+            emit_subtree(sc, c, child_slot[i], node_at, vert_at, out);
+        }
+        node_at += c.below.nodes;
+        vert_at += c.below.verts;
+    }
+#pragma omp taskwait
+}
+
+void emit_compact(const Scene &sc, Node &root, int threads, CompactBVH &out) {
+    if (threads <= 0) threads = omp_get_max_threads();
+#pragma omp parallel num_threads(threads)
+#pragma omp single
+    size_subtree(root, 0);
+    const EmitSize &e = root.below;
+    out.nodes.assign(4 + e.nodes, I4{0, 0, 0, 0});
+    out.vertices.resize(e.verts);
+    out.normals.resize(e.verts);
+    out.tri_idx.resize(e.verts);
+    out.mat_idx.resize(e.verts);
+    out.hdr.tri_count = (uint32_t)e.tris;
+    out.hdr.leaf_count = (uint32_t)e.leaves;
+#pragma omp parallel num_threads(threads)
+#pragma omp single
+    emit_subtree(sc, root, 0, 4, 0, out);
 }
 
 }  // namespace
@@ -590,7 +688,7 @@ tt_status build_compact(const Scene &sc, const BuildParams &p, CompactBVH &out) 
         top->child[1] = std::move(empty);
         root = std::move(top);
     }
-    emit_compact(sc, *root, out);
+    emit_compact(sc, *root, p.threads, out);
     out.hdr.nodes = (uint32_t)out.nodes.size();
     out.hdr.vertices = (uint32_t)out.vertices.size();
     out.hdr.normals = (uint32_t)out.normals.size();
