@@ -50,7 +50,8 @@ def test_oracle_sbvh_matches_reference_builder(name, leaf_max, golden, golden_sc
 
 
 def test_oracle_sbvh_matches_product_builder_on_a_larger_terrain(tmp_path):
-    sc = Scene.from_mesh(scenes.terrain(96, 8.0, seed=11))
+    """73,728 triangles: enough for the builder to split the root's axes over threads."""
+    sc = Scene.from_mesh(scenes.terrain(192, 8.0, seed=11))
     a = sc.arrays()
     oracle.sbvh_build(a["vertices"], a["normals"], a["vidx"], a["nidx"], a["mat"], tmp_path / "o.cache", 1e-5, 1, 8)
     BVHCompact.build(sc, 1e-5, 1, 8).save(tmp_path / "p.cache")
@@ -66,7 +67,7 @@ def test_scene_ingest_matches_reference_loader(name, golden, golden_scene_files)
 
 
 def test_build_is_independent_of_thread_count(tmp_path):
-    sc = Scene.from_mesh(scenes.terrain(96, 8.0, seed=11))
+    sc = Scene.from_mesh(scenes.terrain(192, 8.0, seed=11))
     paths = []
     for threads in (1, 3, 0):
         p = tmp_path / f"t{threads}.cache"
