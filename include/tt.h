@@ -156,7 +156,8 @@ void tt_scene_free(tt_scene *scene);
  * (src/bvh/BVH.cpp:3-63, src/bvh/BVHCompact.cpp:88-250). SAHHelper::setLeafPreferences
  * (src/bvh/SAHHelper.cpp:51-54) gives leaf_min/leaf_max; the reference defaults are
  * split_alpha 1e-5, leaf_min 1, leaf_max 0x7FFFFFF. threads <= 0 uses all host cores; the
- * output does not depend on the thread count. */
+ * output does not depend on the thread count. TT_ERR_INVALID for a triangle with a NaN or
+ * infinite vertex coordinate (the reference has no check; its sorts are undefined there). */
 tt_status tt_bvh_build(const tt_scene *scene, float split_alpha, int32_t leaf_min,
                        int32_t leaf_max, int32_t threads, tt_bvh **out);
 /* BVHCompact::save / BVHCompact(FILE*) (src/bvh/BVHCompact.cpp:319-375, :23-79). */

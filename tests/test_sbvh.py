@@ -153,6 +153,15 @@ def test_rejects_bad_input(tmp_path):
     v = np.zeros((3, 3), np.float32)
     with pytest.raises(TTError):
         Scene.from_arrays(v, v, np.array([[0, 1, 5]], np.int32))
+    # non-finite vertices are refused before any sort sees a NaN centroid
+    rng = np.random.default_rng(1)
+    for bad in (np.nan, np.inf, -np.inf):
+        w = rng.uniform(-1, 1, (3000, 3)).astype(np.float32)
+        w[1234, 1] = bad
+        sc = Scene.from_arrays(w, w, np.arange(3000, dtype=np.int32).reshape(-1, 3))
+        with pytest.raises(TTError) as e:
+            BVHCompact.build(sc, 1e-5, 1, 8)
+        assert e.value.status == 1 and "NaN or infinite" in str(e.value)
     p = tmp_path / "trunc.cache"
     good = tmp_path / "good.cache"
     BVHCompact.build(Scene.from_mesh(scenes.cornell(2)), 1e-5, 1, 8).save(good)

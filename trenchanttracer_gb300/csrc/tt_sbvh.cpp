@@ -28,6 +28,7 @@
 // does not depend on threads.
 #include <algorithm>
 #include <cfloat>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <memory>
@@ -659,6 +660,10 @@ tt_status build_compact(const Scene &sc, const BuildParams &p, CompactBVH &out) 
     for (int i = 0; i < 3 * n; i++) {
         if (sc.vidx[i] < 0 || (size_t)sc.vidx[i] >= sc.vertices.size())
             return fail(TT_ERR_INVALID, "vertex index out of range");
+        // a NaN or infinite coordinate makes a NaN centroid, which no sort order can place
+        const V3 &v = sc.vertices[sc.vidx[i]];
+        if (!std::isfinite(v.x) || !std::isfinite(v.y) || !std::isfinite(v.z))
+            return fail(TT_ERR_INVALID, "a triangle has a NaN or infinite vertex coordinate");
         if (sc.nidx[i] < 0 || (size_t)sc.nidx[i] >= sc.normals.size())
             return fail(TT_ERR_INVALID, "normal index out of range");
     }
