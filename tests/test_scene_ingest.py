@@ -1,7 +1,8 @@
 """Scene ingest beyond the golden scenes: the chunked parallel OBJ parser gives the same arrays as
 the reference's loader and as itself on any number of threads (chunk boundaries fall inside
 lines, groups and material switches); OBJs without normals or with fewer normals than vertices
-load (the reference rejects or misreads them)."""
+load (the reference rejects or misreads them); mutated scene, OBJ, material and RGBE files load or
+fail with an error status, never a crash."""
 import hashlib
 import json
 import os
@@ -121,3 +122,66 @@ def test_malformed_obj_reports_the_first_error(tmp_path):
     with pytest.raises(TTError) as e:
         Scene.load_json(cfg)
     assert "short v line" in str(e.value)
+
+
+_MUTATE_AND_LOAD = r"""
+import random, shutil, sys
+from pathlib import Path
+from trenchanttracer_gb300 import Scene, TTError
+base, work, seeds = Path(sys.argv[1]), Path(sys.argv[2]), int(sys.argv[3])
+names = sorted(p.name for p in base.iterdir())
+tokens = [b"-1", b"0", b"99999999999", b"-2147483648", b"1e39", b"nan", b"inf", b"//", b"/", b"f", b"v", b"vn",
+          b"usemtl", b"{", b"}", b"[", b"]", b'"', b",", b":", b"\n", b"\x00", b"\xff", b"#", b"1/2/3",
+          b"-5/-5/-5", b"0/0/0", b"-Y 100000 +X 100000", b"+Y 3 -X 2", b"\x02\x02", b"\x01\x01\x01\xff"]
+for seed in range(seeds):
+    rng = random.Random(seed)
+    shutil.rmtree(work, ignore_errors=True)
+    shutil.copytree(base, work)
+    cfg = work / "s.json"
+    cfg.write_text(cfg.read_text().replace(str(base), str(work)))
+    target = work / rng.choice(names)
+    b = bytearray(target.read_bytes())
+    for _ in range(rng.randint(1, 6)):
+        pos = rng.randrange(len(b) + 1)
+        k = rng.random()
+        if k < 0.25:
+            b[pos:pos + 1] = bytes([rng.randrange(256)])
+        elif k < 0.4:
+            del b[pos:]
+        elif k < 0.7:
+            b[pos:pos] = rng.choice(tokens)
+        elif k < 0.85:
+            del b[pos:pos + rng.randint(1, 64)]
+        else:
+            b[pos:pos] = b[pos:pos + rng.randint(1, 256)] * rng.randint(1, 4)
+    target.write_bytes(bytes(b))
+    print("seed", seed, target.name, flush=True)
+    try:
+        Scene.load_json(cfg).arrays()
+    except TTError:
+        pass
+"""
+
+
+def test_mutated_inputs_load_or_fail_cleanly(tmp_path):
+    """Seeded mutations (byte flips, truncation, inserted tokens, deleted and repeated spans) of a
+    scene's JSON config, OBJ, material JSON and RGBE picture. Each load must succeed or raise
+    TTError; it runs in a child process so that a crash fails this test instead of the run."""
+    from tests.golden import rgbe_files
+
+    base = tmp_path / "base"
+    base.mkdir()
+    cfg_path = _tricky_obj(base)
+    hdr = rgbe_files.write_all(tmp_path)["mixed"]
+    (base / "sky.hdr").write_bytes(hdr.read_bytes())
+    cfg = json.loads(cfg_path.read_text())
+    cfg["hdr-file-name"] = str(base / "sky.hdr")
+    cfg["objects"].append({"type": "Sphere", "radius": 0.5, "position": [1.0, 0.5, 0.0], "material": "a"})
+    cfg_path.write_text(json.dumps(cfg))
+    Scene.load_json(cfg_path)  # the unmutated scene loads
+    pr = subprocess.run([sys.executable, "-c", _MUTATE_AND_LOAD, str(base), str(tmp_path / "work"), "2000"],
+                        capture_output=True, text=True, timeout=600, cwd=ROOT,
+                        env={**os.environ, "PYTHONPATH": str(ROOT)})
+    seen = [line for line in pr.stdout.splitlines() if line.startswith("seed")]
+    assert pr.returncode == 0, (seen[-1:], pr.stderr[-2000:])
+    assert len(seen) == 2000

@@ -181,4 +181,5 @@ def lib() -> C.CDLL:
 def check(status: int) -> None:
     if status != TT_OK:
         msg = lib().tt_last_error_string()
-        raise TTError(status, msg.decode() if msg else "")
+        # the message may quote bytes of a malformed input file
+        raise TTError(status, msg.decode(errors="replace") if msg else "")
