@@ -178,6 +178,22 @@ def test_rejects_bad_input(tmp_path):
     p.write_bytes(bytes(bad))
     with pytest.raises(TTError):
         BVHCompact.load(p)
+    # a leaf address two entries before the end: in range, but its one "triangle" would read a
+    # vertex past the array
+    bad = bytearray(raw)
+    bad[off:off + 4] = np.int32(~(int(hdr[3]) - 2)).tobytes()
+    p.write_bytes(bytes(bad))
+    with pytest.raises(TTError) as e:
+        BVHCompact.load(p)
+    assert "without a terminator" in str(e.value)
+    # the last terminator overwritten: the walk from every leaf of the last run leaves the array
+    bad = bytearray(raw)
+    vstart = 28 + 16 * int(hdr[0])
+    last = vstart + 16 * (int(hdr[3]) - 1)
+    bad[last:last + 4] = np.float32(0.5).tobytes()
+    p.write_bytes(bytes(bad))
+    with pytest.raises(TTError):
+        BVHCompact.load(p)
 
 
 def _soup_scene(tmp_path, name, mesh):

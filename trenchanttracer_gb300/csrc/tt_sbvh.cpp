@@ -756,7 +756,13 @@ tt_status load_compact(const std::string &path, CompactBVH &out) {
     fclose(f);
     if (!ok) return fail(TT_ERR_FORMAT, "bvh.cache truncated: " + path);
     // Structural validation: every child address must land inside its array, so that a
-    // corrupt file is rejected here instead of steering a traversal out of bounds.
+    // corrupt file is rejected here instead of steering a traversal out of bounds. A leaf is read
+    // a triangle (three vertex entries) at a time, the second and third after the first was found
+    // not to be the terminator, so from every leaf address the walk in steps of three must meet a
+    // terminator inside the array. closed[i]: the walk from entry i does.
+    std::vector<uint8_t> closed(w[3], 0);
+    for (int64_t i = (int64_t)w[3] - 1; i >= 0; i--)
+        closed[i] = (uint32_t)out.vertices[i].x == 0x80000000u || (i + 3 < (int64_t)w[3] && closed[i + 3]);
     for (uint32_t i = 0; i < w[0]; i += 4) {
         const I4 &c = out.nodes[i + 3];
         for (int32_t a : {c.x, c.y}) {
@@ -765,11 +771,11 @@ tt_status load_compact(const std::string &path, CompactBVH &out) {
                     return fail(TT_ERR_FORMAT, "bvh.cache inner child address out of range");
             } else if ((uint32_t)(~a) >= w[3]) {
                 return fail(TT_ERR_FORMAT, "bvh.cache leaf address out of range");
+            } else if (!closed[~a]) {
+                return fail(TT_ERR_FORMAT, "bvh.cache leaf runs past the vertex array without a terminator");
             }
         }
     }
-    if (w[3] > 0 && (uint32_t)out.vertices[w[3] - 1].x != 0x80000000u)
-        return fail(TT_ERR_FORMAT, "bvh.cache vertex array does not end with a leaf terminator");
     return TT_OK;
 }
 
