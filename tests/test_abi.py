@@ -74,3 +74,41 @@ def test_struct_layouts_match_the_header(tmp_path):
         assert got[f"{cname} size"] == C.sizeof(py), cname
         for f, _ in py._fields_:
             assert got[f"{cname} {f}"] == getattr(py, f).offset, (cname, f)
+
+
+_NULL_CALLS = r"""
+import ctypes as C
+from trenchanttracer_gb300 import _lib
+lib = _lib.lib()
+ints = (C.c_int32, C.c_int64, C.c_uint32, C.c_uint64, C.c_int, C.c_size_t, C.c_longlong, C.c_ulonglong)
+for name, (res, args) in _lib.SIGNATURES.items():
+    if name in ("tt_version", "tt_last_error_string", "tt_wang_hash", "tt_trace_host_noalloc"):
+        continue  # no handle or pointer to check; n = 0 is the allocation-free warm-up call
+    vals = [0 if a in ints else 0.0 if a in (C.c_float, C.c_double) else None for a in args]
+    print(name, getattr(lib, name)(*vals), flush=True)
+"""
+
+
+def test_every_entry_point_refuses_null_handles_and_pointers():
+    """Each entry point called with NULL for every pointer and handle and 0 for every number
+    returns a status other than TT_OK (the free functions return nothing), without a crash. Runs
+    in a child process, so a crash names the last entry point reached."""
+    import os
+    import subprocess
+    import sys
+
+    pr = subprocess.run([sys.executable, "-c", _NULL_CALLS], capture_output=True, text=True, timeout=300, cwd=ROOT,
+                        env={**os.environ, "PYTHONPATH": str(ROOT)})
+    lines = pr.stdout.splitlines()
+    assert pr.returncode == 0, (lines[-1:], pr.stderr[-1000:])
+    seen = {}
+    for line in lines:
+        name, status = line.split()
+        seen[name] = status
+    free_fns = {n for n, (res, _) in _lib.SIGNATURES.items() if res is None}
+    for name, status in seen.items():
+        if name in free_fns:
+            assert status == "None", name
+        elif name not in ("tt_batch_free", "tt_cache_free"):  # freeing NULL is a no-op that succeeds
+            assert status != "0", f"{name} accepted NULL arguments"
+    assert len(seen) == len(_lib.SIGNATURES) - 4
