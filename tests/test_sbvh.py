@@ -58,6 +58,22 @@ def test_oracle_sbvh_matches_product_builder_on_a_larger_terrain(tmp_path):
     assert sha(tmp_path / "o.cache") == sha(tmp_path / "p.cache")
 
 
+def test_signed_zero_and_tied_centroids_match_oracle(tmp_path):
+    """Centroid sums of -0.0 and +0.0 compare equal in the reference's sort, so such references
+    order by triangle index; the builder's radix sort of the root must agree. Half the triangles
+    lie in the plane x = -0.0 or x = +0.0, a quarter are exact copies of others."""
+    rng = np.random.default_rng(9)
+    v = rng.uniform(-1, 1, (1800, 3)).astype(np.float32)
+    v[:900:2, 0] = -0.0
+    v[1:900:2, 0] = 0.0
+    v[1350:] = v[:450]
+    t = rng.permutation(1800).astype(np.int32).reshape(-1, 3)
+    for leaf_min, leaf_max in [(1, 8), (1, 0x7FFFFFF), (3, 2)]:
+        oracle.sbvh_build(v, v, t, t, np.zeros(600, np.uint32), tmp_path / "o.cache", 1e-5, leaf_min, leaf_max)
+        BVHCompact.build(Scene.from_arrays(v, v, t), 1e-5, leaf_min, leaf_max).save(tmp_path / "p.cache")
+        assert sha(tmp_path / "o.cache") == sha(tmp_path / "p.cache"), (leaf_min, leaf_max)
+
+
 @pytest.mark.parametrize("name", ["ico3", "terrain64", "cornell4", "mixed"])
 def test_scene_ingest_matches_reference_loader(name, golden, golden_scene_files):
     a = Scene.load_json(golden_scene_files[name]).arrays()

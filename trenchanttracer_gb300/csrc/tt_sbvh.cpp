@@ -142,6 +142,46 @@ struct ByCentroid {
     }
 };
 
+// `refs` (in triangle order) in ByCentroid{dim} order, by a stable LSD radix sort of the
+// centroid sums' bits mapped to unsigned order (-0 taken as +0, as the float comparison has it):
+// stability over the triangle-ordered input breaks ties by triangle index. Centroids are never
+// NaN (the build refuses non-finite vertices).
+std::vector<Ref> sorted_by_centroid(const std::vector<Ref> &refs, int dim) {
+    const size_t n = refs.size();
+    std::vector<uint32_t> key(n), key2(n);
+    std::vector<int32_t> idx(n), idx2(n);
+    for (size_t i = 0; i < n; i++) {
+        float c = refs[i].b.lo[dim] + refs[i].b.hi[dim];
+        if (c == 0.0f) c = 0.0f;
+        uint32_t u;
+        memcpy(&u, &c, 4);
+        key[i] = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+        idx[i] = (int32_t)i;
+    }
+    constexpr int kBits = 11, kDigits = 1 << kBits;
+    std::vector<size_t> count(kDigits);
+    for (int shift = 0; shift < 32; shift += kBits) {
+        std::fill(count.begin(), count.end(), 0);
+        for (size_t i = 0; i < n; i++) count[(key[i] >> shift) & (kDigits - 1)]++;
+        size_t sum = 0;
+        for (size_t &c : count) {
+            const size_t t = c;
+            c = sum;
+            sum += t;
+        }
+        for (size_t i = 0; i < n; i++) {
+            const size_t at = count[(key[i] >> shift) & (kDigits - 1)]++;
+            key2[at] = key[i];
+            idx2[at] = idx[i];
+        }
+        key.swap(key2);
+        idx.swap(idx2);
+    }
+    std::vector<Ref> out(n);
+    for (size_t i = 0; i < n; i++) out[i] = refs[idx[i]];
+    return out;
+}
+
 // What the spatial partition did with one reference that straddles the plane.
 enum class Straddle : uint8_t { kLeft, kRight, kBoth };
 
@@ -168,9 +208,8 @@ public:
         {
             NodeRefs nr;
             for (int d = 0; d < 3; d++) {
-                nr.s[d] = refs;
-#pragma omp task firstprivate(d) shared(nr)
-                std::sort(nr.s[d].begin(), nr.s[d].end(), ByCentroid{d});
+#pragma omp task firstprivate(d) shared(nr, refs)
+                nr.s[d] = sorted_by_centroid(refs, d);
             }
 #pragma omp taskwait
             out = build(std::move(nr), root, 0, &refs);
