@@ -1446,11 +1446,12 @@ static tt_status ensure_stream(tt_renderer *r, const PathSoA &ps, long long pool
 }
 
 // A streamed render of `total` paths through a pool of L.wave slots (see StreamPlan). The
-// iteration count is an upper bound fixed on the host, so the sequence can be captured: while
-// paths remain, every iteration extends a full pool, so ceil(total / pool) * max_depth
-// iterations extend every path of up to max_depth bounces, and max_depth more drain the pool;
-// iterations after the last path ends find empty queues and return at once. The final plan
-// flags the error word if any path had not ended.
+// iteration count is an upper bound fixed on the host, so the sequence can be captured. Path g
+// starts by the plan of iteration floor(g / pool) * max_depth (every earlier generation of pool
+// paths has ended by then, leaving it a slot and ring room) and ends within max_depth iterations,
+// so ceil(total / pool) * max_depth iterations end every path; the max_depth more issued here are
+// slack. Iterations after the last path ends find empty queues and return at once. The final
+// plan flags the error word if any path had not ended.
 static tt_status issue_stream(NativeArgs a, long long total, const Launch &L, const OrderPlan &plan, void *accum,
                               cudaStream_t s, tt_renderer *r) {
     const bool f64 = (a.p.flags & TT_RENDER_ACCUM_F64) != 0;
