@@ -185,3 +185,101 @@ def test_mutated_inputs_load_or_fail_cleanly(tmp_path):
     seen = [line for line in pr.stdout.splitlines() if line.startswith("seed")]
     assert pr.returncode == 0, (seen[-1:], pr.stderr[-2000:])
     assert len(seen) == 2000
+
+
+def _random_obj_scene(rng, d: Path) -> Path:
+    """A random OBJ in the forms the reference's loader reads (OBJLoader.cpp): several vertices on
+    one `v` line, floats as repr / %f / %e / %E / %g with a sign / integers / "1." / ".5", tabs and
+    runs of blanks, CRLF or LF, ignored `vt` / `vp` / `s` / `o` / comment lines, faces of 3-6
+    corners whose corners mix `v`, `v/t` and `v/t/n` (the texture and normal index of a corner
+    without them carry over from the previous corner of the line), and material switches."""
+    def num(x):
+        k = int(rng.integers(8))
+        if k == 0:
+            return repr(float(np.float32(x)))
+        if k == 1:
+            return "%.6f" % x
+        if k == 2:
+            return "%e" % x
+        if k == 3:
+            return ("+" if x >= 0 else "") + "%.4g" % x
+        if k == 4:
+            return "%.3E" % x
+        if k == 5:
+            return str(int(round(x)))
+        s = "%.5f" % x
+        if k == 6:
+            return s.rstrip("0")
+        return s.replace("0.", ".", 1) if s.startswith("0.") else s.replace("-0.", "-.", 1) if s.startswith("-0.") else s
+
+    def sep():
+        return [" ", "  ", "\t", " \t "][int(rng.integers(4))]
+
+    nv = int(rng.integers(3, 60))
+    verts = rng.uniform(-5, 5, (nv, 3))
+    norms = rng.uniform(-1, 1, (nv, 3))
+    lines = ["# random", "mtllib m.mtl"]
+    i = 0
+    while i < nv:
+        k = min(nv - i, [1, 1, 1, 2, 3][int(rng.integers(5))])
+        lines.append("v" + sep() + sep().join(num(c) for p in verts[i:i + k] for c in p) + ["", " ", "\t"][int(rng.integers(3))])
+        i += k
+        if rng.random() < 0.1:
+            lines.append(["", "# c", "vt 0.5 0.5", "vp 0.1", "s off", "o thing"][int(rng.integers(6))])
+    lines += ["vn" + sep() + sep().join(num(c) for c in p) for p in norms]
+    groups = int(rng.integers(1, 4))
+    for gi in range(groups):
+        lines += [f"g grp{gi}", "usemtl " + "abc"[int(rng.integers(3))]]
+        for _ in range(int(rng.integers(1, 12))):
+            corners = []
+            for _ in range(int(rng.integers(3, 7))):
+                v, t, n = int(rng.integers(1, nv + 1)), int(rng.integers(1, 5)), int(rng.integers(1, nv + 1))
+                form = int(rng.integers(5))
+                corners.append(str(v) if form == 0 else f"{v}/{t}" if form == 1 else f"{v}/{t}/{n}")
+            lines.append("f" + sep() + sep().join(corners) + ["", " "][int(rng.integers(2))])
+        if gi == groups - 1 and rng.random() < 0.3:
+            lines.append("usemtl " + "abc"[int(rng.integers(3))])
+    eol = "\r\n" if rng.random() < 0.5 else "\n"
+    (d / "m.obj").write_bytes((eol.join(lines) + eol).encode())
+    (d / "m.mtl").write_text(json.dumps({"a": {"type": "Diff", "diffuseColor": [0.5, 0.5, 0.5]},
+                                         "b": {"type": "Spec", "color": [0.9, 0.9, 0.9]},
+                                         "c": {"type": "Diff", "diffuseColor": [0.2, 0.7, 0.2]}}))
+    s = float(rng.uniform(0.5, 3))
+    cfg = {"work-dir": str(d), "samples": 1, "material-file": str(d / "m.mtl"), "hdr-file-name": "",
+           "bvh-reload": True, "material-reload": True,
+           "camera": {"width": 8, "height": 8, "position": [0.0, 0.0, 0.0], "yaw": 0.0, "pitch": 0.0,
+                      "focal": 1.0, "aperture": 0.0},
+           "objects": [{"type": "Mesh", "file": str(d / "m.obj"),
+                        "transform": {"scale": [s, s, s], "orientation": [float(rng.uniform(0, 90)), 20, 30],
+                                      "translate": [1, 2, 3]}}]}
+    (d / "s.json").write_text(json.dumps(cfg))
+    return d / "s.json"
+
+
+_REFERENCE_ARRAYS = r"""
+import sys, numpy as np
+from oracle import refhost
+for cfg in sys.argv[1:]:
+    np.savez(cfg + ".ref.npz", **refhost.scene_arrays(cfg))
+"""
+
+
+@pytest.mark.skipif(not refhost.available(), reason="the reference's loader is not built on this host")
+def test_random_objs_match_reference_loader(tmp_path):
+    """200 random OBJs (`_random_obj_scene`) give the reference loader's arrays bit for bit. The
+    reference runs in a child process: it prints as it loads, and would end the run on a crash."""
+    rng = np.random.default_rng(2026)
+    cfgs = []
+    for k in range(200):
+        d = tmp_path / f"s{k}"
+        d.mkdir()
+        cfgs.append(_random_obj_scene(rng, d))
+    pr = subprocess.run([sys.executable, "-c", _REFERENCE_ARRAYS, *map(str, cfgs)], capture_output=True, timeout=600,
+                        cwd=ROOT, env={**os.environ, "PYTHONPATH": str(ROOT)})
+    assert pr.returncode == 0, pr.stderr[-2000:]
+    for cfg in cfgs:
+        ref = np.load(str(cfg) + ".ref.npz")
+        mine = Scene.load_json(cfg).arrays()
+        for k in ["vertices", "normals", "vidx", "nidx", "mat"]:
+            a, b = np.asarray(mine[k]), np.asarray(ref[k])
+            assert a.shape == b.shape and np.array_equal(a.view(np.uint32), b.view(np.uint32)), (cfg, k)
