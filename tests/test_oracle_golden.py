@@ -93,3 +93,54 @@ def test_live_oracle_against_reference_host(bvhs, golden_scene_files, tmp_path):
         o = oracle.intersect(b.arrays(), rays, closest, arith=oracle.PLAIN)
         assert np.array_equal(r["id"], o["id"])
         assert np.array_equal(r["t"].view(np.uint32), o["t"].view(np.uint32))
+
+
+def _edge_rays(count: int, seed: int, lo, hi) -> np.ndarray:
+    """Random rays plus the cases the slab test treats specially: axis-aligned directions (zero
+    components take the 2^-80 inverse-direction guard), negative zeros, directions of 1e-30,
+    origins on box planes and at the scene's corners, t ranges that end before or start inside
+    the scene, and an empty range (tmin = tmax)."""
+    from trenchanttracer_gb300 import scenes
+    rng = np.random.default_rng(seed)
+    rays = scenes.random_rays(count, seed, lo, hi)
+    lo, hi = np.asarray(lo, np.float32), np.asarray(hi, np.float32)
+    n = count // 8
+    axes = np.eye(3, dtype=np.float32)[rng.integers(0, 3, n)] * rng.choice([-1.0, 1.0], (n, 1)).astype(np.float32)
+    rays[:n, 3:6] = axes
+    rays[n:2 * n, 3:6] = np.where(rng.random((n, 3)) < 0.5, np.float32(-0.0), rays[n:2 * n, 3:6])
+    rays[2 * n:3 * n, 3:6] = np.where(rng.random((n, 3)) < 0.3, np.float32(1e-30), rays[2 * n:3 * n, 3:6])
+    corner = np.where(rng.random((n, 3)) < 0.5, lo, hi)
+    rays[3 * n:4 * n, 0:3] = corner
+    rays[4 * n:5 * n, 6] = rng.uniform(0.0, 1.0, n).astype(np.float32)  # start inside the range
+    rays[5 * n:6 * n, 7] = rng.uniform(0.0, 0.5, n).astype(np.float32)  # end early
+    rays[6 * n:6 * n + 16, 6] = rays[6 * n:6 * n + 16, 7] = np.float32(0.25)
+    return rays
+
+
+@pytest.mark.skipif(not refhost.available(), reason="the reference's host code is not built on this host")
+@pytest.mark.parametrize("kind", ["soup", "flat", "terrain"])
+def test_live_oracle_on_edge_rays(kind, tmp_path):
+    """The oracle against the reference's host-compiled intersect() on scenes with spatial splits,
+    a flat layer (zero-extent boxes) and a terrain, with the slab test's special cases."""
+    from trenchanttracer_gb300 import scenes
+    rng = np.random.default_rng(len(kind))
+    if kind == "terrain":
+        mesh = scenes.terrain(48, 1.0, seed=5)
+        v, t = mesh.vertices, mesh.vidx
+    else:
+        v = rng.uniform(-1, 1, (1500, 3)).astype(np.float32)
+        if kind == "flat":
+            v[:, 1] = 0.25
+        t = np.arange(1500, dtype=np.int32).reshape(-1, 3)
+    b = BVHCompact.build(Scene.from_arrays(v, v, t), 1e-5, 1, 8)
+    b.save(tmp_path / "s.cache")
+    lo, hi = v.min(0) - 0.1, v.max(0) + 0.1
+    rays = _edge_rays(40000, 3 + len(kind), lo, hi)
+    for closest in (True, False):
+        r = refhost.intersect(str(tmp_path / "s.cache"), rays, closest)
+        o = oracle.intersect(b.arrays(), rays, closest, arith=oracle.PLAIN, normals=True)
+        assert np.array_equal(r["id"], o["id"]), (kind, closest)
+        assert np.array_equal(r["t"].view(np.uint32), o["t"].view(np.uint32)), (kind, closest)
+        hit = o["id"] >= 0
+        assert hit.any() and (~hit).any()
+        assert np.array_equal(r["normal"].view(np.uint32)[hit], o["normal"].view(np.uint32)[hit]), (kind, closest)
