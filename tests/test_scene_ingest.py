@@ -244,14 +244,21 @@ def _random_obj_scene(rng, d: Path) -> Path:
     (d / "m.mtl").write_text(json.dumps({"a": {"type": "Diff", "diffuseColor": [0.5, 0.5, 0.5]},
                                          "b": {"type": "Spec", "color": [0.9, 0.9, 0.9]},
                                          "c": {"type": "Diff", "diffuseColor": [0.2, 0.7, 0.2]}}))
-    s = float(rng.uniform(0.5, 3))
+    objects = []
+    for _ in range(int(rng.integers(1, 4))):  # the same file placed up to three times
+        tr = {}
+        if rng.random() < 0.8:
+            tr["scale"] = [float(x) for x in rng.uniform(0.2, 3, 3)]
+        if rng.random() < 0.8:
+            tr["orientation"] = [float(x) for x in rng.uniform(-180, 180, 3)]
+        if rng.random() < 0.8:
+            tr["translate"] = [float(x) for x in rng.uniform(-10, 10, 3)]
+        objects.append({"type": "Mesh", "file": str(d / "m.obj"), **({"transform": tr} if tr else {})})
     cfg = {"work-dir": str(d), "samples": 1, "material-file": str(d / "m.mtl"), "hdr-file-name": "",
            "bvh-reload": True, "material-reload": True,
            "camera": {"width": 8, "height": 8, "position": [0.0, 0.0, 0.0], "yaw": 0.0, "pitch": 0.0,
                       "focal": 1.0, "aperture": 0.0},
-           "objects": [{"type": "Mesh", "file": str(d / "m.obj"),
-                        "transform": {"scale": [s, s, s], "orientation": [float(rng.uniform(0, 90)), 20, 30],
-                                      "translate": [1, 2, 3]}}]}
+           "objects": objects}
     (d / "s.json").write_text(json.dumps(cfg))
     return d / "s.json"
 
