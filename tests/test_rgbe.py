@@ -49,3 +49,27 @@ def test_truncated_rgbe_keeps_the_complete_rows(tmp_path):
     want = (rows[..., :3].astype(np.float32) / 256.0) * np.ldexp(np.float32(1.0), e)[..., None].astype(np.float32)
     assert np.array_equal(img[:3], want.astype(np.float32))
     assert not img[3:].any()  # the scanline the data ends in, and the rows after it, stay zero
+
+
+@pytest.mark.skipif(not refhost.available(), reason="the reference's loader is not built on this host")
+def test_random_rgbe_pictures_match_reference_loader(tmp_path):
+    """60 random pictures, 1-400 pixels wide and 1-12 rows high, each row in a coding drawn at
+    random (flat, flat with repeat pixels, adaptive run-length where the width allows it), decode
+    to the reference loader's floats bit for bit."""
+    from tests.golden import rgbe_files as rf
+    rng = np.random.default_rng(31)
+    for k in range(60):
+        w, h = int(rng.integers(1, 401)), int(rng.integers(1, 13))
+        rows = []
+        for row in rf._pixels(rng, w, h):
+            c = int(rng.integers(3))
+            if c == 0 and 8 <= w < 32768:
+                rows.append(rf._rle_row(rng, row))
+            elif c == 1 and w > 3:
+                rows.append(rf._flat_row_with_repeats(rng, row))
+            else:
+                rows.append(rf._flat_row(row))
+        p = tmp_path / f"r{k}.hdr"
+        p.write_bytes(rf.HEADER + f"-Y {h} +X {w}\n".encode() + b"".join(rows))
+        img = _load(tmp_path, p)
+        assert np.array_equal(img.view(np.uint32), refhost.load_hdr(str(p)).view(np.uint32)), (k, w, h)
