@@ -254,3 +254,28 @@ def test_live_against_reference_builder(kind, tmp_path):
         refhost.build_json(str(cfg), str(tmp_path / "ref.cache"), 1e-5, leaf_min, leaf_max)
         BVHCompact.build(Scene.load_json(cfg), 1e-5, leaf_min, leaf_max).save(tmp_path / "new.cache")
         assert sha(tmp_path / "ref.cache") == sha(tmp_path / "new.cache"), (leaf_min, leaf_max)
+
+
+@pytest.mark.skipif(not refhost.available(), reason="the reference's builder is not built on this host")
+def test_random_scenes_and_settings_against_reference_builder(tmp_path):
+    """Thirty random scenes (soups of small and large triangles, clustered and spread, some with
+    duplicates) at random split alphas (0 lets every node try spatial splits; 1 almost none) and
+    leaf settings: byte-identical bvh.cache files."""
+    rng = np.random.default_rng(4242)
+    for k in range(30):
+        n = int(rng.integers(50, 1500))
+        centres = rng.normal(0, 1, (n, 1, 3)) * (rng.uniform(0.2, 3, (1, 1, 3)) if k % 2 else 1.0)
+        size = rng.uniform(0.01, 0.6) * (rng.lognormal(0, 1, (n, 1, 1)) if k % 3 == 0 else 1.0)
+        v = (centres + rng.normal(0, 1, (n, 3, 3)) * size).reshape(-1, 3).astype(np.float32)
+        if k % 4 == 1:
+            v[-30:] = v[:30]  # ten repeated triangles
+        t = np.arange(len(v), dtype=np.int32).reshape(-1, 3)
+        mesh = scenes.Mesh(v, scenes._normalize(v + 3.0), t, t.copy(), np.zeros(len(t), np.uint32),
+                           [{"name": "m", "type": "Diff", "diffuseColor": [0.5, 0.5, 0.5]}])
+        cfg = _soup_scene(tmp_path, f"r{k}", mesh)
+        alpha = float([0.0, 1e-7, 1e-5, 1e-3, 0.1, 1.0][int(rng.integers(6))])
+        leaf_min = int(rng.integers(1, 6))
+        leaf_max = int([1, 2, 4, 8, 16, 0x7FFFFFF][int(rng.integers(6))])
+        refhost.build_json(str(cfg), str(tmp_path / "ref.cache"), alpha, leaf_min, leaf_max)
+        BVHCompact.build(Scene.load_json(cfg), alpha, leaf_min, leaf_max).save(tmp_path / "new.cache")
+        assert sha(tmp_path / "ref.cache") == sha(tmp_path / "new.cache"), (k, alpha, leaf_min, leaf_max)
