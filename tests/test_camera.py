@@ -87,3 +87,10 @@ def test_random_cameras_match_reference(tmp_path):
         got = np.array(list(cm.position) + list(cm.view) + list(cm.up) + list(cm.fov) + [cm.aperture, cm.focal],
                        np.float32)
         assert np.array_equal(got.view(np.uint32), np.array(w, np.float32).view(np.uint32)), (cfg, got, w)
+
+
+@pytest.mark.skipif(not refhost.available(), reason="the reference's host code is not built on this host")
+def test_wang_hash_matches_reference_on_random_words():
+    rng = np.random.default_rng(5)
+    for a in list(rng.integers(0, 2**32, 20000, dtype=np.uint64)) + [0, 1, 2**31 - 1, 2**31, 2**32 - 1]:
+        assert _lib.lib().tt_wang_hash(int(a)) == refhost.wang_hash(int(a)), int(a)
