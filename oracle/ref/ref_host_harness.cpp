@@ -15,7 +15,14 @@
 #include <bvh/BVHCompact.h>
 #include <bvh/SAHHelper.h>
 #include <core/Camera.h>
+#include <core/Group.h>
 #include <core/Scene.h>
+#include <geometry/Plane.h>
+#include <geometry/Sphere.h>
+#include <material/Coat.h>
+#include <material/Diff.h>
+#include <material/Metal.h>
+#include <material/Spec.h>
 #include <hdr/HDRImage.h>
 #include <loader/HDRLoader.h>
 #include <loader/SceneLoader.h>
@@ -92,6 +99,56 @@ int ref_camera_meta(const char *config_path, float fovx, float *out) {
 }
 
 unsigned ref_wang_hash(unsigned a) { return WangHash::encode(a); }
+
+// The materials and analytic objects the reference's loader leaves in the Scene, flattened.
+// counts[0..1] = materials, analytic objects; pass NULL buffers to query the counts. Per material
+// 10 floats: type, emission xyz, the first colour xyz (Diff / Coat: diffuseColor, Metal / Spec:
+// color), the second xyz (Coat: specularColor), zeros where a kind has none. Per analytic object
+// 13 floats: type, material index, radius (Sphere), 0, then p0 (Sphere: position), p1, p2.
+int ref_scene_materials(const char *config_path, int *counts, float *mats, float *geoms) {
+    try {
+        Config config(config_path);
+        SceneLoader loader(&config);
+        Scene *scene = loader.load();
+        counts[0] = scene->getMaterialNum();
+        counts[1] = scene->getGeometryNum();
+        for (int i = 0; mats && i < counts[0]; i++) {
+            const Material *m = scene->getMaterial(i);
+            float *o = mats + 10 * i;
+            memset(o, 0, 10 * sizeof(float));
+            o[0] = (float)m->type;
+            o[1] = m->emission.x, o[2] = m->emission.y, o[3] = m->emission.z;
+            Vec3f a(0, 0, 0), b(0, 0, 0);
+            if (m->type == DIFF) a = ((const Diff *)m)->diffuseColor;
+            if (m->type == METAL) a = ((const Metal *)m)->color;
+            if (m->type == SPEC) a = ((const Spec *)m)->color;
+            if (m->type == COAT) a = ((const Coat *)m)->diffuseColor, b = ((const Coat *)m)->specularColor;
+            o[4] = a.x, o[5] = a.y, o[6] = a.z, o[7] = b.x, o[8] = b.y, o[9] = b.z;
+        }
+        for (int i = 0; geoms && i < counts[1]; i++) {
+            const Group *g = scene->getGeometry(i);
+            const Geometry *geo = g->getGeometry();
+            float *o = geoms + 13 * i;
+            memset(o, 0, 13 * sizeof(float));
+            o[0] = (float)geo->type;
+            o[1] = (float)g->getMaterial()->index;
+            if (geo->type == SPHERE) {
+                const Sphere *sp = (const Sphere *)geo;
+                o[2] = sp->radius;
+                o[4] = sp->position.x, o[5] = sp->position.y, o[6] = sp->position.z;
+            } else if (geo->type == PLANE) {
+                const Plane *pl = (const Plane *)geo;
+                const Vec3f *p[3] = {&pl->p0, &pl->p1, &pl->p2};
+                for (int k = 0; k < 3; k++) o[4 + 3 * k] = p[k]->x, o[5 + 3 * k] = p[k]->y, o[6 + 3 * k] = p[k]->z;
+            }
+        }
+        delete scene;
+        return 0;
+    } catch (const std::exception &e) {
+        fprintf(stderr, "ref_scene_materials: %s\n", e.what());
+        return -1;
+    }
+}
 
 // The reference's intersect() compiled for the host (ballot -> this lane only; video min/max ->
 // integer min/max), over n rays of 8 floats under OpenMP. Loads the BVH from bvh.cache with

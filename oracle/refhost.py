@@ -36,6 +36,8 @@ def _load():
         h.ref_scene_arrays.argtypes = [C.c_char_p, C.POINTER(C.c_int)] + [C.c_void_p] * 5
         h.ref_camera_meta.restype = C.c_int
         h.ref_camera_meta.argtypes = [C.c_char_p, C.c_float, C.c_void_p]
+        h.ref_scene_materials.restype = C.c_int
+        h.ref_scene_materials.argtypes = [C.c_char_p, C.POINTER(C.c_int), C.c_void_p, C.c_void_p]
         h.ref_wang_hash.restype = C.c_uint
         h.ref_wang_hash.argtypes = [C.c_uint]
         h.ref_load_hdr.restype = C.c_int
@@ -64,6 +66,18 @@ def scene_arrays(config: str) -> dict:
     h.ref_scene_arrays(os.fsencode(config), counts, *(out[k].ctypes.data for k in
                                                          ["vertices", "normals", "vidx", "nidx", "mat"]))
     return out
+
+
+def scene_materials(config: str) -> tuple[np.ndarray, np.ndarray]:
+    """(materials (m, 10), analytic objects (g, 13)) as ref_scene_materials flattens them."""
+    h = _load()
+    counts = (C.c_int * 2)()
+    if h.ref_scene_materials(os.fsencode(config), counts, None, None) != 0:
+        raise RuntimeError("reference scene load failed")
+    mats = np.zeros((counts[0], 10), np.float32)
+    geoms = np.zeros((counts[1], 13), np.float32)
+    h.ref_scene_materials(os.fsencode(config), counts, mats.ctypes.data, geoms.ctypes.data)
+    return mats, geoms
 
 
 def camera_meta(config: str, fovx: float = 45.0) -> np.ndarray:

@@ -290,3 +290,99 @@ def test_random_objs_match_reference_loader(tmp_path):
         for k in ["vertices", "normals", "vidx", "nidx", "mat"]:
             a, b = np.asarray(mine[k]), np.asarray(ref[k])
             assert a.shape == b.shape and np.array_equal(a.view(np.uint32), b.view(np.uint32)), (cfg, k)
+
+
+_REFERENCE_MATERIALS = r"""
+import sys, numpy as np
+from oracle import refhost
+for cfg in sys.argv[1:]:
+    m, g = refhost.scene_materials(cfg)
+    np.savez(cfg + ".mat.npz", materials=m, geometries=g)
+"""
+
+
+def _random_material(rng) -> dict:
+    def num(lo, hi):
+        x = float(rng.uniform(lo, hi))
+        k = int(rng.integers(3))
+        return x if k == 0 else float("%.2e" % x) if k == 1 else int(round(x))
+
+    kind = ["Diff", "Metal", "Spec", "Refr", "Coat"][int(rng.integers(5))]
+    m = {"type": kind}
+    if kind in ("Diff", "Coat"):
+        m["diffuseColor"] = [num(0, 1) for _ in range(3)]
+    if kind in ("Metal", "Spec"):
+        m["color"] = [num(0, 1) for _ in range(3)]
+    if kind == "Coat":
+        m["specularColor"] = [num(0, 1) for _ in range(3)]
+    if rng.random() < 0.3:
+        m["emission"] = [num(0, 50) for _ in range(3)]
+    return m
+
+
+def _random_name(rng) -> str:
+    chars = "abcXYZ019_-"
+    return "".join(chars[int(i)] for i in rng.integers(0, len(chars), int(rng.integers(1, 6))))
+
+
+@pytest.mark.skipif(not refhost.available(), reason="the reference's loader is not built on this host")
+def test_random_materials_and_objects_match_reference_loader(tmp_path):
+    """40 random scenes: a master material file and per-OBJ material files of random names (the
+    reference keeps each pool in name order) and kinds, with or without emission, planes and
+    spheres using master materials, and meshes. Materials (kind, emission, colours), analytic
+    objects (kind, material index, radius, points) and triangle material indices all equal the
+    reference loader's, bit for bit."""
+    rng = np.random.default_rng(99)
+    cfgs = []
+    for k in range(40):
+        d = tmp_path / f"m{k}"
+        d.mkdir()
+        master = {}
+        while len(master) < int(rng.integers(1, 7)):
+            master[_random_name(rng)] = _random_material(rng)
+        (d / "master.mtl").write_text(json.dumps(master))
+        names = list(master)
+        objects = []
+        for j in range(int(rng.integers(0, 3))):
+            pool = {}
+            while len(pool) < int(rng.integers(1, 4)):
+                pool[_random_name(rng)] = _random_material(rng)
+            (d / f"o{j}.mtl").write_text(json.dumps(pool))
+            lines = [f"mtllib o{j}.mtl", "v 0 0 0", "v 1 0 0", "v 0 1 0", "v 1 1 0", "vn 0 0 1", "vn 0 0 1",
+                     "vn 0 0 1", "vn 0 0 1"]
+            for gi, name in enumerate(pool):
+                lines += [f"g g{gi}", f"usemtl {name}", "f 1/1/1 2/1/2 3/1/3", "f 2/1/2 4/1/4 3/1/3"]
+            (d / f"o{j}.obj").write_text("\n".join(lines) + "\n")
+            objects.append({"type": "Mesh", "file": str(d / f"o{j}.obj")})
+        for _ in range(int(rng.integers(0, 5))):
+            mat = names[int(rng.integers(len(names)))]
+            if rng.random() < 0.5:
+                objects.append({"type": "Sphere", "radius": float(rng.uniform(0.1, 3)),
+                                "position": [float(x) for x in rng.uniform(-5, 5, 3)], "material": mat})
+            else:
+                objects.append({"type": "Plane", "material": mat,
+                                **{p: [float(x) for x in rng.uniform(-5, 5, 3)] for p in ("p0", "p1", "p2")}})
+        if not any(o["type"] == "Mesh" for o in objects):  # every scene holds triangles
+            (d / "t.mtl").write_text(json.dumps({"t": {"type": "Diff", "diffuseColor": [0.5, 0.5, 0.5]}}))
+            (d / "t.obj").write_text("mtllib t.mtl\nv 0 0 0\nv 1 0 0\nv 0 1 0\nvn 0 0 1\nvn 0 0 1\nvn 0 0 1\n"
+                                     "g g\nusemtl t\nf 1/1/1 2/1/2 3/1/3\n")
+            objects.insert(int(rng.integers(len(objects) + 1)), {"type": "Mesh", "file": str(d / "t.obj")})
+        cfg = {"work-dir": str(d), "samples": 1, "material-file": str(d / "master.mtl"), "hdr-file-name": "",
+               "bvh-reload": True, "material-reload": True,
+               "camera": {"width": 8, "height": 8, "position": [0.0, 0.0, 0.0], "yaw": 0.0, "pitch": 0.0,
+                          "focal": 1.0, "aperture": 0.0},
+               "objects": objects}
+        (d / "s.json").write_text(json.dumps(cfg))
+        cfgs.append(d / "s.json")
+    pr = subprocess.run([sys.executable, "-c", _REFERENCE_MATERIALS, *map(str, cfgs)], capture_output=True, timeout=600,
+                        cwd=ROOT, env={**os.environ, "PYTHONPATH": str(ROOT)})
+    assert pr.returncode == 0, pr.stderr[-2000:]
+    for cfg in cfgs:
+        ref = np.load(str(cfg) + ".mat.npz")
+        sc = Scene.load_json(cfg)
+        mats = np.array([[m.kind, *m.emission, *m.color, *m.color2] for m in sc.materials_raw()], np.float32)
+        geoms = np.array([[g.kind, g.material, g.radius, 0.0, *g.p0, *g.p1, *g.p2] for g in sc.geometries_raw()],
+                         np.float32).reshape(-1, 13)
+        assert np.array_equal(mats.view(np.uint32), ref["materials"].view(np.uint32)), cfg
+        assert np.array_equal(geoms.view(np.uint32), ref["geometries"].view(np.uint32)), cfg
+        assert np.array_equal(sc.arrays()["mat"], refhost.scene_arrays(str(cfg))["mat"]), cfg
