@@ -56,7 +56,7 @@ struct tt_renderer {
     size_t cache_bytes = 0;
     long long cache_queries = 0, cache_records = 0;
     // streamed renders (more paths than one wave, refilled as paths end): the radiance ring, the
-    // pool's path indices, its free-slot stack and the plan record, one allocation
+    // second copy of the path state, both copies' path indices and the plan record, one allocation
     void *stream_mem = nullptr;
     size_t stream_bytes = 0;
 };
