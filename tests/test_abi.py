@@ -112,3 +112,25 @@ def test_every_entry_point_refuses_null_handles_and_pointers():
         elif name not in ("tt_batch_free", "tt_cache_free"):  # freeing NULL is a no-op that succeeds
             assert status != "0", f"{name} accepted NULL arguments"
     assert len(seen) == len(_lib.SIGNATURES) - 4
+
+
+def test_scene_setters_refuse_unknown_kinds():
+    """Material kinds are 0-6 (the reference's five and GGX, dielectric), analytic objects are
+    spheres (0) and planes (3); anything else is refused before it reaches a renderer."""
+    import numpy as np
+    from trenchanttracer_gb300 import Scene
+    v = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)
+    sc = Scene.from_arrays(v, v, np.array([[0, 1, 2]], np.int32))
+    lib = _lib.lib()
+    mats = (_lib.Material * 2)()
+    mats[0].kind, mats[1].kind = 6, 7
+    assert lib.tt_scene_set_materials(sc._h, mats, 1) == 0
+    assert lib.tt_scene_set_materials(sc._h, mats, 2) == 1
+    assert b"unknown kind 7" in lib.tt_last_error_string()
+    mats[1].kind = -1
+    assert lib.tt_scene_set_materials(sc._h, mats, 2) == 1
+    geoms = (_lib.Geometry * 3)()
+    geoms[0].kind, geoms[1].kind, geoms[2].kind = 0, 3, 1
+    assert lib.tt_scene_set_geometries(sc._h, geoms, 2) == 0
+    assert lib.tt_scene_set_geometries(sc._h, geoms, 3) == 1
+    assert len(sc.geometries_raw()) == 2  # a refused call leaves the scene as it was

@@ -137,6 +137,10 @@ tt_status tt_scene_materials(const tt_scene *scene, tt_material *out) {
 
 tt_status tt_scene_set_materials(tt_scene *scene, const tt_material *materials, int32_t count) {
     if (!scene || count < 0 || (count && !materials)) return fail(TT_ERR_INVALID, "bad materials");
+    for (int32_t i = 0; i < count; i++)
+        if (materials[i].kind < MAT_DIFF || materials[i].kind > MAT_DIELECTRIC)
+            return fail(TT_ERR_INVALID, "material " + std::to_string(i) + ": unknown kind " +
+                                            std::to_string(materials[i].kind));
     TT_GUARD_BEGIN
     Scene &sc = scene->s;
     sc.materials.resize(count);
@@ -154,6 +158,10 @@ tt_status tt_scene_geometries(const tt_scene *scene, tt_geometry *out) {
 
 tt_status tt_scene_set_geometries(tt_scene *scene, const tt_geometry *geometries, int32_t count) {
     if (!scene || count < 0 || (count && !geometries)) return fail(TT_ERR_INVALID, "bad geometries");
+    for (int32_t i = 0; i < count; i++)
+        if (geometries[i].kind != GEOM_SPHERE && geometries[i].kind != GEOM_PLANE)
+            return fail(TT_ERR_INVALID, "analytic object " + std::to_string(i) + ": unknown kind " +
+                                            std::to_string(geometries[i].kind));
     TT_GUARD_BEGIN
     scene->s.geoms.resize(count);
     if (count) memcpy(scene->s.geoms.data(), geometries, sizeof(GeomRec) * count);
