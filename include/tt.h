@@ -142,9 +142,12 @@ tt_status tt_scene_arrays(const tt_scene *scene, float *vertices, float *normals
 /* The environment map HDRLoader::load read for the scene (src/loader/HDRLoader.cpp:5-65):
  * width, height and, when rgb != NULL, w*h*3 linear floats, row 0 first. 0 x 0 = none. */
 tt_status tt_scene_env(const tt_scene *scene, int32_t *width, int32_t *height, float *rgb);
-/* Replaces the environment map (width*height*3 linear floats, row 0 first; 0 x 0 = none). */
+/* Replaces the environment map (width*height*3 linear floats, row 0 first; 0 x 0 = none).
+ * TT_ERR_INVALID, leaving the scene's map in place, for a negative, infinite or NaN texel. */
 tt_status tt_scene_set_env(tt_scene *scene, int32_t width, int32_t height, const float *rgb);
-/* Materials and analytic objects: counts via tt_scene_counts; `out` may be NULL. */
+/* Materials and analytic objects: counts via tt_scene_counts; `out` may be NULL. The setters
+ * refuse (TT_ERR_INVALID) material kinds outside 0-6 and analytic objects other than spheres (0)
+ * and planes (3). */
 tt_status tt_scene_materials(const tt_scene *scene, tt_material *out);
 tt_status tt_scene_set_materials(tt_scene *scene, const tt_material *materials, int32_t count);
 tt_status tt_scene_geometries(const tt_scene *scene, tt_geometry *out);

@@ -134,3 +134,20 @@ def test_scene_setters_refuse_unknown_kinds():
     assert lib.tt_scene_set_geometries(sc._h, geoms, 2) == 0
     assert lib.tt_scene_set_geometries(sc._h, geoms, 3) == 1
     assert len(sc.geometries_raw()) == 2  # a refused call leaves the scene as it was
+
+
+def test_environment_setter_refuses_non_finite_or_negative_texels():
+    import numpy as np
+    import pytest
+    from trenchanttracer_gb300 import Scene, TTError
+    v = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)
+    sc = Scene.from_arrays(v, v, np.array([[0, 1, 2]], np.int32))
+    good = np.ones((4, 8, 3), np.float32)
+    sc.set_env(good)
+    for bad in (np.nan, np.inf, -1e-3):
+        env = good.copy()
+        env[2, 5, 1] = bad
+        with pytest.raises(TTError) as e:
+            sc.set_env(env)
+        assert e.value.status == 1 and "texel value" in str(e.value)
+    assert np.array_equal(sc.env(), good)  # a refused map leaves the scene's own in place

@@ -1,4 +1,5 @@
 // Host-side C ABI: error reporting, scene creation and the SBVH / bvh.cache entry points.
+#include <cfloat>
 #include <cstring>
 #include <new>
 #include <string>
@@ -120,10 +121,16 @@ tt_status tt_scene_set_env(tt_scene *scene, int32_t width, int32_t height, const
     if (!scene || width < 0 || height < 0 || ((width > 0) != (height > 0)) || (width > 0 && !rgb))
         return fail(TT_ERR_INVALID, "bad environment map");
     TT_GUARD_BEGIN
+    std::vector<float> texels(rgb, rgb + 3ll * width * height);
+    // radiance is finite and not negative; anything else would poison the sampling tables
+    for (size_t i = 0; i < texels.size(); i++)
+        if (!(texels[i] >= 0.0f && texels[i] <= FLT_MAX))
+            return fail(TT_ERR_INVALID, "environment texel value " + std::to_string(i) +
+                                            " is negative, infinite or NaN");
     Scene &sc = scene->s;
     sc.env_w = width;
     sc.env_h = height;
-    sc.env_rgb.assign(rgb, rgb + 3ll * width * height);
+    sc.env_rgb.swap(texels);
     return TT_OK;
     TT_GUARD_END
 }
