@@ -274,7 +274,7 @@ def test_random_scenes_and_settings_against_reference_builder(tmp_path):
                            [{"name": "m", "type": "Diff", "diffuseColor": [0.5, 0.5, 0.5]}])
         cfg = _soup_scene(tmp_path, f"r{k}", mesh)
         alpha = float([0.0, 1e-7, 1e-5, 1e-3, 0.1, 1.0][int(rng.integers(6))])
-        leaf_min = int(rng.integers(1, 6))
+        leaf_min = int(rng.integers(0, 6))
         leaf_max = int([1, 2, 4, 8, 16, 0x7FFFFFF][int(rng.integers(6))])
         refhost.build_json(str(cfg), str(tmp_path / "ref.cache"), alpha, leaf_min, leaf_max)
         BVHCompact.build(Scene.load_json(cfg), alpha, leaf_min, leaf_max).save(tmp_path / "new.cache")
