@@ -151,3 +151,24 @@ def test_environment_setter_refuses_non_finite_or_negative_texels():
             sc.set_env(env)
         assert e.value.status == 1 and "texel value" in str(e.value)
     assert np.array_equal(sc.env(), good)  # a refused map leaves the scene's own in place
+
+
+def test_a_missing_library_fails_loudly(tmp_path):
+    """The package has no fallback: a copy of it without libtt.so raises on first use instead of
+    computing anything another way."""
+    import os
+    import shutil
+    import subprocess
+    import sys
+    pkg = tmp_path / "trenchanttracer_gb300"
+    shutil.copytree(ROOT / "trenchanttracer_gb300", pkg,
+                    ignore=shutil.ignore_patterns("libtt.so", "_build", "__pycache__", "*.o", "csrc"))
+    assert not (pkg / "libtt.so").exists()
+    code = ("import numpy as np\n"
+            "from trenchanttracer_gb300 import Scene\n"
+            "v = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)\n"
+            "Scene.from_arrays(v, v, np.array([[0, 1, 2]], np.int32))\n")
+    pr = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=300, cwd=tmp_path,
+                        env={**os.environ, "PYTHONPATH": str(tmp_path)})
+    assert pr.returncode != 0
+    assert "libtt.so is missing" in pr.stderr
