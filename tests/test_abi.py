@@ -172,3 +172,16 @@ def test_a_missing_library_fails_loudly(tmp_path):
                         env={**os.environ, "PYTHONPATH": str(tmp_path)})
     assert pr.returncode != 0
     assert "libtt.so is missing" in pr.stderr
+
+
+def test_binding_argument_counts_match_the_header():
+    """Each ctypes declaration takes as many arguments as the prototype in include/tt.h."""
+    protos = {}
+    for h in (ROOT / "include").glob("*.h"):
+        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        for m in re.finditer(r"\b(tt_[a-z0-9_]+)\s*\(([^;{]*?)\)\s*;", text, re.S):
+            params = m.group(2).strip()
+            protos[m.group(1)] = 0 if params in ("", "void") else params.count(",") + 1
+    assert len(protos) >= 60
+    for name, n in protos.items():
+        assert len(_lib.SIGNATURES[name][1]) == n, (name, n, len(_lib.SIGNATURES[name][1]))
