@@ -190,7 +190,8 @@ def test_mutated_inputs_load_or_fail_cleanly(tmp_path):
 def _random_obj_scene(rng, d: Path) -> Path:
     """A random OBJ in the forms the reference's loader reads (OBJLoader.cpp): several vertices on
     one `v` line, floats as repr / %f / %e / %E / %g with a sign / integers / "1." / ".5", tabs and
-    runs of blanks, CRLF or LF, ignored `vt` / `vp` / `s` / `o` / comment lines, faces of 3-6
+    runs of blanks, CRLF or LF, a last line with or without its end of line, ignored `vt` / `vp` /
+    `s` / `o` / comment lines, faces of 3-6
     corners whose corners mix `v`, `v/t` and `v/t/n` (the texture and normal index of a corner
     without them carry over from the previous corner of the line), and material switches."""
     def num(x):
@@ -240,7 +241,8 @@ def _random_obj_scene(rng, d: Path) -> Path:
         if gi == groups - 1 and rng.random() < 0.3:
             lines.append("usemtl " + "abc"[int(rng.integers(3))])
     eol = "\r\n" if rng.random() < 0.5 else "\n"
-    (d / "m.obj").write_bytes((eol.join(lines) + eol).encode())
+    end = [eol, "", eol + eol + "   " + eol + "# end"][int(rng.integers(3))]  # the file's last line may lack one
+    (d / "m.obj").write_bytes((eol.join(lines) + end).encode())
     (d / "m.mtl").write_text(json.dumps({"a": {"type": "Diff", "diffuseColor": [0.5, 0.5, 0.5]},
                                          "b": {"type": "Spec", "color": [0.9, 0.9, 0.9]},
                                          "c": {"type": "Diff", "diffuseColor": [0.2, 0.7, 0.2]}}))
